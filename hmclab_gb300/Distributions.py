@@ -1,0 +1,606 @@
+"""Target distributions of the HMC hot path, evaluated on the GPU.
+
+The classes keep the reference's plugin API (larsgeb/hmclab,
+`hmclab/Distributions/base.py:21-374`): an integer `dimensions`,
+`misfit(m) -> float` and `gradient(m) -> (d,1) ndarray` on column vectors,
+optional `lower_bounds` / `upper_bounds`, `corrector`, `update_bounds`,
+`misfit_bounds`, `misfit_v`.  Single-vector calls run the FP64 kernels on one
+chain.  The batched API takes a device tensor M of shape (d, C) (one chain per
+column, chain index fastest in memory) and is what the sampler calls:
+
+    misfit_batch(M)   -> float64 tensor (C,)
+    gradient_batch(M) -> tensor (d, C) of M's dtype
+
+Every evaluation goes through the CUDA library; there is no CPU fallback.
+"""
+from abc import abstractmethod as _abstractmethod
+from typing import List as _List, Union as _Union
+
+import numpy as _numpy
+import scipy.sparse as _sparse
+
+from hmclab_gb300 import _device as _dev
+from hmclab_gb300 import _lib
+from hmclab_gb300.Helpers.CustomExceptions import AbstractMethodError as _AbstractMethodError
+from hmclab_gb300.Helpers.CustomExceptions import InvalidCaseError as _InvalidCaseError
+
+__all__ = [
+    "_AbstractDistribution",
+    "Normal",
+    "Laplace",
+    "AdditiveDistribution",
+    "BayesRule",
+    "LinearMatrix",
+    "SourceLocation3D",
+]
+
+
+def _column(coordinates, dimensions):
+    m = _numpy.asarray(coordinates, dtype=_numpy.float64)
+    if m.size != dimensions:
+        raise ValueError(f"coordinates of size {m.size} do not match dimensions {dimensions}")
+    return m.reshape(dimensions, 1)
+
+
+class _AbstractDistribution:
+    """Plugin base class (reference `base.py:21-374`).
+
+    Subclasses set `self.dimensions` and implement `_device_misfit` and
+    `_device_gradient`, which write (or accumulate into) device buffers for a
+    (d, C) batch of models."""
+
+    name: str = None
+    lower_bounds: _Union[_numpy.ndarray, None] = None
+    upper_bounds: _Union[_numpy.ndarray, None] = None
+    normalized: bool = False
+    normalization_constant: float = 0.0
+
+    # ---- reference-facing single-vector API -------------------------------
+    def misfit(self, coordinates: _numpy.ndarray) -> float:
+        """chi(m) for one column vector (d,1), in FP64 on the GPU
+        (reference `base.py:70-105`); +inf outside the bounds."""
+        m = _column(coordinates, self.dimensions)
+        x = self.misfit_batch(_dev.upload(m, "float64"))
+        return float(x.cpu()[0]) + self.normalization_constant + self.misfit_bounds(m)
+
+    def gradient(self, coordinates: _numpy.ndarray) -> _numpy.ndarray:
+        """d chi / d m for one column vector, in FP64 on the GPU (reference
+        `base.py:140-168`); the bound misfit (0 or +inf) is added like the
+        reference does."""
+        m = _column(coordinates, self.dimensions)
+        g = self.gradient_batch(_dev.upload(m, "float64"))
+        return g.cpu().numpy().reshape(self.dimensions, 1) + self.misfit_bounds(m)
+
+    def misfit_v(self, coordinates: _numpy.ndarray, vectors_in_dim=None):
+        """Misfits of many vectors at once (reference `base.py:107-138`), as
+        one batched launch instead of a Python loop."""
+        c = _numpy.asarray(coordinates, dtype=_numpy.float64)
+        if c.size == self.dimensions:
+            return self.misfit(c)
+        if vectors_in_dim is None:
+            if c.ndim != 2:
+                raise AttributeError("Can only take 1D or 2D arrays as input if not specifying vector input dimension")
+            if c.shape[0] == self.dimensions:
+                vectors_in_dim = 0
+            elif c.shape[1] == self.dimensions:
+                vectors_in_dim = 1
+            else:
+                raise AttributeError(f"Don't know what to do with input of shape {c.shape}.")
+        M = _numpy.moveaxis(c, vectors_in_dim, 0).reshape(self.dimensions, -1)
+        x = self.misfit_batch(_dev.upload(M, "float64")).cpu().numpy()
+        x = x + self.normalization_constant + _numpy.array([self.misfit_bounds(M[:, [k]]) for k in range(M.shape[1])])
+        return x.reshape(_numpy.moveaxis(c, vectors_in_dim, 0).shape[1:])
+
+    # ---- batched device API -------------------------------------------------
+    def _check_batch(self, M):
+        if not (hasattr(M, "is_cuda") and M.is_cuda):
+            raise ValueError("batched evaluation needs a CUDA tensor of shape (dimensions, chains)")
+        if M.dim() != 2 or M.shape[0] != self.dimensions:
+            raise ValueError(f"expected shape ({self.dimensions}, C), got {tuple(M.shape)}")
+        if not M.is_contiguous():
+            raise ValueError("the model batch must be contiguous (chains fastest)")
+        return _dev.normalise_dtype(M.dtype)
+
+    def misfit_batch(self, M, out=None, accumulate=False, stream=None):
+        """chi for every column of M (device, (d, C)); returns float64 (C,).
+        Bounds are not applied here (the sampler tracks them per chain)."""
+        dtype = self._check_batch(M)
+        if out is None:
+            out = _dev.zeros((M.shape[1],), "float64", M.device)
+        self._device_misfit(M, out, bool(accumulate), dtype, _dev.stream_handle(stream))
+        return out
+
+    def gradient_batch(self, M, out=None, accumulate=False, stream=None):
+        """d chi / d m for every column of M; returns a (d, C) tensor of M's dtype."""
+        dtype = self._check_batch(M)
+        if out is None:
+            out = _dev.zeros(tuple(M.shape), dtype, M.device)
+        self._device_gradient(M, out, bool(accumulate), dtype, _dev.stream_handle(stream))
+        return out
+
+    @_abstractmethod
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        raise _AbstractMethodError()
+
+    @_abstractmethod
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        raise _AbstractMethodError()
+
+    # ---- device parameter / scratch caches ---------------------------------
+    def _params(self, dtype):
+        cache = self.__dict__.setdefault("_param_cache", {})
+        if dtype not in cache:
+            cache[dtype] = self._make_params(dtype)
+        return cache[dtype]
+
+    def _make_params(self, dtype):
+        return {}
+
+    def _scratch(self, name, shape, dtype, device):
+        cache = self.__dict__.setdefault("_scratch_cache", {})
+        key = (name, tuple(shape), dtype)
+        t = cache.get(key)
+        if t is None:
+            t = _dev.empty(shape, dtype, device)
+            cache[key] = t
+        return t
+
+    def __getstate__(self):
+        state = self.__dict__.copy()
+        state.pop("_param_cache", None)
+        state.pop("_scratch_cache", None)
+        return state
+
+    # ---- reference API kept as is -----------------------------------------
+    def normalize(self):
+        raise AttributeError("This distribution is not normalizable.")
+
+    def generate(self, repeat=1, rng=_numpy.random.default_rng()) -> _numpy.ndarray:
+        raise NotImplementedError("Generating samples from this distribution is not implemented or supported.")
+
+    @staticmethod
+    def create_default(dimensions: int) -> "_AbstractDistribution":
+        raise NotImplementedError()
+
+    def corrector(self, coordinates: _numpy.ndarray, momentum: _numpy.ndarray):
+        """Reflect at the bounds in place (reference `base.py:239-270`).  The
+        sampler applies the same rule on the device after every drift."""
+        if self.lower_bounds is not None:
+            too_low = coordinates < self.lower_bounds
+            coordinates[too_low] += 2 * (self.lower_bounds[too_low] - coordinates[too_low])
+            momentum[too_low] *= -1.0
+        if self.upper_bounds is not None:
+            too_high = coordinates > self.upper_bounds
+            coordinates[too_high] += 2 * (self.upper_bounds[too_high] - coordinates[too_high])
+            momentum[too_high] *= -1.0
+
+    def update_bounds(self, lower=None, upper=None):
+        """Set bounds with the reference's validation (`base.py:272-359`)."""
+        old = (self.lower_bounds, self.upper_bounds)
+        if type(upper) == list:
+            upper = _numpy.array(upper)[:, None]
+        if type(lower) == list:
+            lower = _numpy.array(lower)[:, None]
+        self.upper_bounds, self.lower_bounds = upper, lower
+        if lower is not None and type(lower) is not _numpy.ndarray:
+            self.lower_bounds, self.upper_bounds = old
+            raise ValueError("Lower bounds object not understood.")
+        if upper is not None and type(upper) is not _numpy.ndarray:
+            self.lower_bounds, self.upper_bounds = old
+            raise ValueError("Upper bounds object not understood.")
+        if (self.lower_bounds is not None and self.lower_bounds.shape != (self.dimensions, 1)) or (
+            self.upper_bounds is not None and self.upper_bounds.shape != (self.dimensions, 1)
+        ):
+            self.lower_bounds, self.upper_bounds = old
+            raise ValueError("Bounds vectors are of incorrect size.")
+        if (
+            self.lower_bounds is not None
+            and self.upper_bounds is not None
+            and _numpy.any(self.upper_bounds <= self.lower_bounds)
+        ):
+            self.lower_bounds, self.upper_bounds = old
+            raise ValueError("Bounds vectors are incompatible.")
+
+    def misfit_bounds(self, coordinates: _numpy.ndarray) -> float:
+        """0 inside the bounds, +inf outside (reference `base.py:361-374`)."""
+        if (self.lower_bounds is not None and _numpy.any(coordinates < self.lower_bounds)) or (
+            self.upper_bounds is not None and _numpy.any(coordinates > self.upper_bounds)
+        ):
+            return _numpy.inf
+        return 0.0
+
+
+# ---------------------------------------------------------------------------
+class Normal(_AbstractDistribution):
+    """Normal distribution (reference `base.py:427-643`): diagonal (scalar or
+    (d,1) variances) or full (d,d) covariance."""
+
+    def __init__(self, means, covariance, inverse_covariance=None, lower_bounds=None, upper_bounds=None):
+        self.name = "Gaussian (normal) distribution"
+        if type(means) == list:
+            means = _numpy.array(means)[:, None]
+        if type(covariance) == list:
+            covariance = _numpy.array(covariance)[:, None]
+        if type(means) == float or type(means) == int:
+            self.dimensions = 1
+            means = _numpy.ones((1, 1)) * means
+        else:
+            self.dimensions = int(means.size)
+            means = _numpy.asarray(means, dtype=_numpy.float64).reshape(self.dimensions, 1)
+        self.means = means
+        self.normalization_constant = 0.0
+        self.generate_ready = False
+        if isinstance(covariance, (float, int, _numpy.floating)):
+            covariance = _numpy.float64(covariance)
+            self.diagonal = True
+        elif covariance.shape == (means.size, means.size):
+            self.diagonal = False
+        else:
+            self.diagonal = True
+            covariance = _numpy.asarray(covariance, dtype=_numpy.float64).reshape(self.dimensions, 1)
+        self.covariance = covariance
+        if inverse_covariance is not None:
+            self.inverse_covariance = inverse_covariance
+        elif self.diagonal:
+            self.inverse_covariance = 1.0 / self.covariance
+        else:
+            self.inverse_covariance = _numpy.linalg.inv(self.covariance)
+        if self.dimensions == 1:
+            self.diagonal = True
+        self.update_bounds(lower_bounds, upper_bounds)
+
+    def _make_params(self, dtype):
+        if self.diagonal:
+            iv = _numpy.broadcast_to(_numpy.asarray(self.inverse_covariance, _numpy.float64).reshape(-1, 1),
+                                     (self.dimensions, 1))
+            return {"mean": _dev.upload(self.means[:, 0], dtype), "iv": _dev.upload(iv[:, 0], dtype)}
+        return {
+            "mean": _dev.upload(self.means[:, 0], dtype),
+            "icov": _dev.upload(_numpy.asarray(self.inverse_covariance), dtype),
+        }
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        d, C = M.shape
+        if self.diagonal:
+            _lib.call("hmc_normal_diag_misfit", _dev.dtype_code(dtype), d, C, M.data_ptr(), p["mean"].data_ptr(),
+                      p["iv"].data_ptr(), out.data_ptr(), int(accumulate), stream)
+        else:
+            work = self._scratch("work2", (2, d, C), dtype, M.device)
+            _lib.call("hmc_normal_full_misfit", _dev.dtype_code(dtype), d, C, M.data_ptr(), p["mean"].data_ptr(),
+                      p["icov"].data_ptr(), work.data_ptr(), out.data_ptr(), int(accumulate), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        d, C = M.shape
+        if self.diagonal:
+            _lib.call("hmc_normal_diag_gradient", _dev.dtype_code(dtype), d, C, M.data_ptr(), p["mean"].data_ptr(),
+                      p["iv"].data_ptr(), out.data_ptr(), int(accumulate), stream)
+        else:
+            work = self._scratch("work1", (d, C), dtype, M.device)
+            _lib.call("hmc_normal_full_gradient", _dev.dtype_code(dtype), d, C, M.data_ptr(), p["mean"].data_ptr(),
+                      p["icov"].data_ptr(), work.data_ptr(), out.data_ptr(), int(accumulate), stream)
+
+    def normalize(self):
+        cov = self.covariance
+        if isinstance(cov, (float, int, _numpy.floating)):
+            det = cov**self.dimensions
+        elif cov.shape == (self.means.size, self.means.size):
+            det = _numpy.linalg.det(cov)
+        else:
+            det = _numpy.prod(cov)
+        self.normalization_constant = 0.5 * (_numpy.log(_numpy.abs(det)) + self.dimensions * _numpy.log(2 * _numpy.pi))
+        self.normalized = True
+
+    def generate(self, repeat=1, rng=_numpy.random.default_rng()) -> _numpy.ndarray:
+        if self.diagonal:
+            return rng.normal(size=(self.dimensions, repeat)) * _numpy.sqrt(self.covariance) + self.means
+        return _numpy.linalg.cholesky(self.covariance) @ rng.normal(size=(self.dimensions, repeat)) + self.means
+
+    @staticmethod
+    def create_default(dimensions: int, diagonal=True) -> "Normal":
+        means = _numpy.random.rand(dimensions, 1)
+        std = _numpy.random.rand(dimensions, 1) + 1
+        return Normal(means, std * std)
+
+
+class Laplace(_AbstractDistribution):
+    """Laplace (L1) distribution (reference `base.py:646-744`)."""
+
+    def __init__(self, means, dispersions, lower_bounds=None, upper_bounds=None):
+        if type(means) == list:
+            means = _numpy.array(means)[:, None]
+        if type(dispersions) == list:
+            dispersions = _numpy.array(dispersions)[:, None]
+        means = _numpy.asarray(means, dtype=_numpy.float64)
+        self.dimensions = int(means.size)
+        self.means = means.reshape(self.dimensions, 1)
+        dispersions = _numpy.asarray(dispersions, dtype=_numpy.float64)
+        if dispersions.size == 1:
+            dispersions = _numpy.full((self.dimensions, 1), float(dispersions))
+        self.dispersions = dispersions.reshape(self.dimensions, 1)
+        self.inverse_dispersions = 1.0 / self.dispersions
+        self.normalization_constant = 0.0
+        self.update_bounds(lower_bounds, upper_bounds)
+
+    def _make_params(self, dtype):
+        return {"mean": _dev.upload(self.means[:, 0], dtype), "iw": _dev.upload(self.inverse_dispersions[:, 0], dtype)}
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        _lib.call("hmc_laplace_misfit", _dev.dtype_code(dtype), M.shape[0], M.shape[1], M.data_ptr(),
+                  p["mean"].data_ptr(), p["iw"].data_ptr(), out.data_ptr(), int(accumulate), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        _lib.call("hmc_laplace_gradient", _dev.dtype_code(dtype), M.shape[0], M.shape[1], M.data_ptr(),
+                  p["mean"].data_ptr(), p["iw"].data_ptr(), out.data_ptr(), int(accumulate), stream)
+
+    def normalize(self):
+        self.normalization_constant = _numpy.log(
+            1.0 / (2.0 * (_numpy.prod(self.dispersions) ** (1.0 / self.dimensions)))
+        )
+        self.normalized = True
+
+    def generate(self, repeat=1, rng=_numpy.random.default_rng()) -> _numpy.ndarray:
+        return rng.laplace(loc=self.means, scale=self.dispersions, size=(self.dimensions, repeat))
+
+    @staticmethod
+    def create_default(dimensions: int) -> "Laplace":
+        return Laplace(_numpy.random.rand(dimensions, 1), 10 ** _numpy.random.rand(dimensions, 1))
+
+
+class AdditiveDistribution(_AbstractDistribution):
+    """Sum of misfits and gradients of several distributions, with bounds
+    collapsed to the tightest set (reference `base.py:1005-1142`)."""
+
+    def __init__(self, list_of_distributions: _List[_AbstractDistribution], lower_bounds=None, upper_bounds=None):
+        self.name = "additive distribution"
+        self.dimensions = list_of_distributions[0].dimensions
+        self.separate_distributions = list(list_of_distributions)
+        for dist in self.separate_distributions:
+            assert dist.dimensions == self.dimensions
+        self.lower_bounds = lower_bounds
+        self.upper_bounds = upper_bounds
+        self.collapse_bounds()
+
+    def misfit(self, coordinates):
+        m = _column(coordinates, self.dimensions)
+        x = self.misfit_batch(_dev.upload(m, "float64"))
+        const = sum(d.normalization_constant for d in self.separate_distributions)
+        bounds = sum(d.misfit_bounds(m) for d in self.separate_distributions)
+        return float(x.cpu()[0]) + const + bounds + self.misfit_bounds(m)
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        for k, dist in enumerate(self.separate_distributions):
+            dist._device_misfit(M, out, accumulate or k > 0, dtype, stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        for k, dist in enumerate(self.separate_distributions):
+            dist._device_gradient(M, out, accumulate or k > 0, dtype, stream)
+
+    def collapse_bounds(self):
+        for dist in self.separate_distributions:
+            if dist.lower_bounds is not None:
+                assert dist.lower_bounds.shape == (self.dimensions, 1)
+                self.lower_bounds = (
+                    dist.lower_bounds if self.lower_bounds is None else _numpy.maximum(self.lower_bounds, dist.lower_bounds)
+                )
+            if dist.upper_bounds is not None:
+                assert dist.upper_bounds.shape == (self.dimensions, 1)
+                self.upper_bounds = (
+                    dist.upper_bounds if self.upper_bounds is None else _numpy.minimum(self.upper_bounds, dist.upper_bounds)
+                )
+
+    def add_distribution(self, distribution: _AbstractDistribution):
+        assert distribution.dimensions == self.dimensions
+        self.separate_distributions.append(distribution)
+        self.collapse_bounds()
+
+
+class BayesRule(AdditiveDistribution):
+    """Unnormalised Bayes' rule: the sum of prior and likelihood misfits."""
+
+
+# ---------------------------------------------------------------------------
+class LinearMatrix(_AbstractDistribution):
+    """Linear forward model G m = d with Gaussian data errors (reference
+    `LinearMatrix.py:15-135`): dense or sparse G with a scalar or (n,1) data
+    variance.  Full data covariances are not part of the HMC path built here
+    and raise NotImplementedError.
+
+    Precision follows the reference: G and d are rounded to `dtype` (default
+    single) as the reference's `_LinearMatrix_*_simple_covariance` classes do
+    (`LinearMatrix.py:148-177, 318-323`), while the premultiplied GtG, Gtd0 and
+    dtd are formed in FP64 exactly as there (Gtd0 from the unrounded G).  FP64
+    chains use the reference's formulas; FP32 chains use GtG for the gradient
+    and the residual form for the misfit, with FP64 per-chain sums."""
+
+    def __init__(self, G, d, data_covariance, dtype=None, premultiplication: bool = None, use_mkl: bool = False):
+        d = _numpy.asarray(d)
+        if not (d.ndim == 2 and d.shape == (d.size, 1)):
+            raise ValueError("Didn't understand the data vector object. Should be a NumPy column vector.")
+        self.dense = not _sparse.issparse(G)
+        if self.dense and not (isinstance(G, _numpy.ndarray) and G.ndim == 2 and G.shape[0] == d.size):
+            raise ValueError("Didn't understand the forward model matrix object.")
+        if not self.dense and G.shape[0] != d.size:
+            raise ValueError("Didn't understand the forward model matrix object.")
+        self.dimensions = int(G.shape[1])
+        self.n_data = int(d.size)
+        if isinstance(data_covariance, (float, _numpy.floating)):
+            var = _numpy.full((self.n_data, 1), float(data_covariance))
+            scalar_variance = True
+        elif isinstance(data_covariance, _numpy.ndarray) and data_covariance.shape == (d.size, 1):
+            var = _numpy.asarray(data_covariance, dtype=_numpy.float64)
+            scalar_variance = False
+        elif isinstance(data_covariance, _numpy.ndarray) and data_covariance.shape == (d.size, d.size):
+            raise NotImplementedError("full data covariance matrices are not on the GPU HMC path")
+        else:
+            raise ValueError("Didn't understand the data covariance object.")
+        store = _numpy.dtype(dtype) if dtype is not None else _numpy.dtype(_numpy.single)
+        self.storage_dtype = store
+        if not scalar_variance:
+            var = var.astype(store).astype(_numpy.float64)
+        self.data_variance = var
+        self.inv_var = 1.0 / var
+        if self.dense:
+            G = _numpy.asarray(G)
+            self.G = G.astype(store).astype(_numpy.float64)
+        else:
+            Gc = _sparse.csr_matrix(G, dtype=store)
+            Gc.sort_indices()
+            self.G = Gc.astype(_numpy.float64)
+        self.d = d.astype(store).astype(_numpy.float64)
+        self.premultiplication = (
+            premultiplication if premultiplication is not None else self.G.shape[0] > self.G.shape[1]
+        )
+        if self.premultiplication:
+            iv = self.inv_var
+            if self.dense:
+                self.GtG = self.G.T @ (iv * self.G)
+                self.Gtd0 = _numpy.asarray(G, dtype=_numpy.float64).T @ (iv * self.d)
+            else:
+                self.GtG = (self.G.T @ _sparse.diags(iv[:, 0]) @ self.G).toarray()
+                self.Gtd0 = _sparse.csr_matrix(G).astype(_numpy.float64).T @ (iv * self.d)
+            self.dtd = (self.d.T @ (iv * self.d)).item()
+
+    def forward(self, coordinates):
+        return self.G @ coordinates
+
+    def _make_params(self, dtype):
+        p = {}
+        if self.dense:
+            p["G"] = _dev.upload(self.G, dtype)
+            if not self.premultiplication or dtype == "float32":
+                p["Gt"] = _dev.upload(self.G.T, dtype)
+        else:
+            G = self.G
+            Gt = self.G.T.tocsr()
+            Gt.sort_indices()
+            p["rp"], p["col"], p["val"] = _dev.upload_int32(G.indptr), _dev.upload_int32(G.indices), _dev.upload(G.data, dtype)
+            p["trp"], p["tcol"], p["tval"] = (
+                _dev.upload_int32(Gt.indptr),
+                _dev.upload_int32(Gt.indices),
+                _dev.upload(Gt.data, dtype),
+            )
+        p["data"] = _dev.upload(self.d[:, 0], dtype)
+        p["iv"] = _dev.upload(self.inv_var[:, 0], dtype)
+        if self.premultiplication:
+            p["GtG"] = _dev.upload(self.GtG, dtype)
+            p["Gtd0"] = _dev.upload(self.Gtd0[:, 0], dtype)
+        return p
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        d, C = M.shape
+        code = _dev.dtype_code(dtype)
+        if self.premultiplication and dtype == "float64":
+            work = self._scratch("work", (d, C), dtype, M.device)
+            _lib.call("hmc_dense_premul_misfit", code, d, C, M.data_ptr(), p["GtG"].data_ptr(), p["Gtd0"].data_ptr(),
+                      float(self.dtd), work.data_ptr(), out.data_ptr(), int(accumulate), stream)
+            return
+        resid = self._scratch("resid", (self.n_data, C), dtype, M.device)
+        if self.dense:
+            _lib.call("hmc_dense_resid_misfit", code, self.n_data, d, C, M.data_ptr(), p["G"].data_ptr(),
+                      p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(), int(accumulate), stream)
+        else:
+            _lib.call("hmc_csr_misfit", code, self.n_data, d, C, M.data_ptr(), p["rp"].data_ptr(), p["col"].data_ptr(),
+                      p["val"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(),
+                      int(accumulate), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        p = self._params(dtype)
+        d, C = M.shape
+        code = _dev.dtype_code(dtype)
+        if self.premultiplication:
+            _lib.call("hmc_dense_premul_gradient", code, d, C, M.data_ptr(), p["GtG"].data_ptr(),
+                      p["Gtd0"].data_ptr(), out.data_ptr(), int(accumulate), stream)
+            return
+        resid = self._scratch("resid", (self.n_data, C), dtype, M.device)
+        if self.dense:
+            _lib.call("hmc_dense_resid_gradient", code, self.n_data, d, C, M.data_ptr(), p["G"].data_ptr(),
+                      p["Gt"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(),
+                      int(accumulate), stream)
+        else:
+            _lib.call("hmc_csr_gradient", code, self.n_data, d, C, M.data_ptr(), p["rp"].data_ptr(),
+                      p["col"].data_ptr(), p["val"].data_ptr(), p["trp"].data_ptr(), p["tcol"].data_ptr(),
+                      p["tval"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(),
+                      out.data_ptr(), int(accumulate), stream)
+
+    @staticmethod
+    def create_default(dimensions: int, dtype=_numpy.dtype("float64")) -> "LinearMatrix":
+        return LinearMatrix(_numpy.eye(dimensions, dtype=dtype), _numpy.ones(dimensions)[:, None], 1.0, dtype=dtype)
+
+
+# ---------------------------------------------------------------------------
+class SourceLocation3D(_AbstractDistribution):
+    """Earthquake location with straight rays in a homogeneous medium
+    (reference `SourceLocation.py:369-713`).  Parameters are interleaved
+    x1, y1, z1, t1, ..., xn, yn, zn, tn (, v when `infer_velocity`)."""
+
+    name = "Earthquake source location in 3D"
+
+    def __init__(self, receiver_array_x, receiver_array_y, receiver_array_z, observed_data, data_std,
+                 infer_velocity: bool = True, medium_velocity=None):
+        rx = _numpy.array(receiver_array_x, dtype=_numpy.float64).reshape(1, -1)
+        ry = _numpy.array(receiver_array_y, dtype=_numpy.float64).reshape(1, -1)
+        rz = _numpy.array(receiver_array_z, dtype=_numpy.float64).reshape(1, -1)
+        self.receiver_array_x, self.receiver_array_y, self.receiver_array_z = rx, ry, rz
+        self.infer_velocity = infer_velocity
+        if not infer_velocity:
+            assert medium_velocity is not None
+            self.medium_velocity = float(_numpy.asarray(medium_velocity).reshape(-1)[0])
+        else:
+            self.medium_velocity = None
+        observed_data = _numpy.array(observed_data, dtype=_numpy.float64)
+        assert observed_data.size % rx.size == 0
+        self.number_of_events = int(observed_data.size // rx.size)
+        self.number_of_stations = int(rz.size)
+        self.number_of_datums = self.number_of_events * self.number_of_stations
+        shape = (self.number_of_events, self.number_of_stations)
+        if observed_data.shape != shape:
+            observed_data = observed_data.T
+            assert observed_data.shape == shape, "Wrong shape for the observed data, not sure what to do."
+        self.observed_data = observed_data
+        if isinstance(data_std, float):
+            data_std = _numpy.ones_like(observed_data) * data_std
+        data_std = _numpy.array(data_std, dtype=_numpy.float64)
+        if data_std.shape != shape:
+            data_std = data_std.T
+            assert data_std.shape == shape, "Wrong shape for the data uncertainty, not sure what to do."
+        self.data_std = data_std
+        self.dimensions = self.number_of_events * 4 + int(self.infer_velocity)
+
+    def _make_params(self, dtype):
+        return {
+            "rx": _dev.upload(self.receiver_array_x[0], dtype),
+            "ry": _dev.upload(self.receiver_array_y[0], dtype),
+            "rz": _dev.upload(self.receiver_array_z[0], dtype),
+            "obs": _dev.upload(self.observed_data, dtype),
+            "iv": _dev.upload(1.0 / self.data_std**2, dtype),
+        }
+
+    def _args(self, M, dtype):
+        p = self._params(dtype)
+        return (_dev.dtype_code(dtype), self.number_of_events, self.number_of_stations, M.shape[1], M.data_ptr(),
+                p["rx"].data_ptr(), p["ry"].data_ptr(), p["rz"].data_ptr(), p["obs"].data_ptr(), p["iv"].data_ptr(),
+                int(self.infer_velocity), float(self.medium_velocity or 0.0))
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        _lib.call("hmc_srcloc3d_misfit", *self._args(M, dtype), out.data_ptr(), int(accumulate), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        _lib.call("hmc_srcloc3d_gradient", *self._args(M, dtype), out.data_ptr(), int(accumulate), stream)
+
+    @staticmethod
+    def split_vector(model_vector, velocity=None):
+        if velocity is None:
+            assert model_vector.size % 4 == 1
+            return (model_vector[0:-1:4], model_vector[1:-1:4], model_vector[2:-1:4], model_vector[3:-1:4],
+                    model_vector[-1])
+        assert model_vector.size % 4 == 0
+        return model_vector[0::4], model_vector[1::4], model_vector[2::4], model_vector[3::4], velocity
+
+    @staticmethod
+    def forward(x, y, z, T, v, receiver_array_x, receiver_array_y, receiver_array_z):
+        return T + ((x - receiver_array_x) ** 2 + (y - receiver_array_y) ** 2 + (z - receiver_array_z) ** 2) ** 0.5 / v

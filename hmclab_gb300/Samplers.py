@@ -1,0 +1,539 @@
+"""Batched Hamiltonian Monte Carlo on one GPU.
+
+`HMC(seed).sample(...)` keeps the reference signature (larsgeb/hmclab,
+`hmclab/Samplers.py:1180-1311`) and semantics — position-Verlet leapfrog
+(`:1524-1584`), 3-/4-stage integrators (`:1586-1726`), bound reflection after
+every drift, FP64 Metropolis accept `exp(H0 - H1) > u` (`:1471-1492`),
+optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
+(`:675-678`), `max_time`, interrupts — and adds batched keyword arguments:
+
+  chains        number of independent chains advanced together (default 1)
+  dtype         'float64' (default for one chain) or 'float32' (default for
+                batches): arithmetic type of positions, momenta, gradients;
+                Hamiltonian sums and the accept test are always FP64
+  rng_streams   None: counter-based Philox draws on the device (production);
+                "numpy": replay `numpy.random.default_rng(seed + c)` per chain
+                in the reference's draw order (reproduces the reference's
+                chain for chains=1); or an explicit tuple (z, f, u) of arrays
+                shaped [P][d][C], [P][C], [P][C]
+  graph         capture each block of proposals in a CUDA graph (default True)
+  keep_samples  keep every thinned sample on the device (`samples_device`)
+
+Each proposal is issued as: begin (momentum, K0, first drift) -> for every
+kick: gradient of the target on the device, then kick+drift -> misfit at the
+end point -> accept/record.  All of it runs on one CUDA stream; blocks of
+proposals are captured once and replayed as CUDA graphs.
+"""
+import ctypes as _ct
+import os as _os
+import time as _time
+from datetime import datetime as _datetime
+
+import numpy as _numpy
+
+from hmclab_gb300 import _device as _dev
+from hmclab_gb300 import _lib
+from hmclab_gb300.Distributions import _AbstractDistribution
+from hmclab_gb300.MassMatrices import Unit as _Unit, _AbstractMassMatrix
+from hmclab_gb300.Samples import Samples as _Samples
+
+try:
+    import torch as _torch
+except ImportError:  # pragma: no cover
+    _torch = None
+
+# Integrator coefficients (Samplers.py:1588-1592, 1666-1669).
+_A1_3S, _B1_3S = 0.11888010966548, 0.29619504261126
+_A1_4S, _A2_4S, _B1_4S = 0.071353913450279725904, 0.268548791161230105820, 0.191667800000000000000
+
+
+def integrator_ops(integrator, amount_of_steps):
+    """The integrator as a list of ('d', a) drifts and ('k', b) kicks, where a
+    and b multiply the step size."""
+    ops = []
+    if integrator == "lf":
+        ops.append(("d", 0.5))
+        for _ in range(amount_of_steps - 1):
+            ops += [("k", 1.0), ("d", 1.0)]
+        ops += [("k", 1.0), ("d", 0.5)]
+    elif integrator == "3s":
+        a1, b1 = _A1_3S, _B1_3S
+        a2, b2 = 0.5 - a1, 1.0 - 2.0 * b1
+        for _ in range(amount_of_steps):
+            ops += [("d", a1), ("k", b1), ("d", a2), ("k", b2), ("d", a2), ("k", b1), ("d", a1)]
+    elif integrator == "4s":
+        a1, a2, b1 = _A1_4S, _A2_4S, _B1_4S
+        a3, b2 = 1.0 - 2.0 * a1 - 2.0 * a2, 0.5 - b1
+        for _ in range(amount_of_steps):
+            ops += [("d", a1), ("k", b1), ("d", a2), ("k", b2), ("d", a3), ("k", b2), ("d", a2), ("k", b1), ("d", a1)]
+    else:
+        raise ValueError(f"Unknown integrator used. Choices are: {list(HMC.integrators_full_names)}")
+    return ops
+
+
+def compile_schedule(ops):
+    """(first_drift, [(needs_gradient, kick, drift), ...]) for the device."""
+    assert ops[0][0] == "d"
+    first = ops[0][1]
+    steps = []
+    i = 1
+    while i < len(ops):
+        kind, c = ops[i]
+        if kind == "k":
+            drift = ops[i + 1][1] if i + 1 < len(ops) and ops[i + 1][0] == "d" else 0.0
+            steps.append((True, c, drift))
+            i += 2 if drift != 0.0 else 1
+        else:
+            steps.append((False, 0.0, c))
+            i += 1
+    return first, steps
+
+
+class HMC:
+    """Hamiltonian Monte Carlo over many chains on one GPU."""
+
+    name = "Hamiltonian Monte Carlo"
+    integrators_full_names = {"lf": "leapfrog integrator", "3s": "three stage integrator", "4s": "four stage integrator"}
+    available_integrators = integrators_full_names.keys()
+    minimal_stepsize = 1e-18
+
+    def __init__(self, seed: int = None):
+        self.seed = seed
+        self.rng = _numpy.random.default_rng(seed)
+        self.philox_seed = (
+            int(seed) & 0xFFFFFFFFFFFFFFFF if seed is not None else int.from_bytes(_os.urandom(8), "little")
+        )
+        self.current_proposal = 0
+        self.accepted_proposals = 0
+        self.samples_device = None
+        self.timings = {}
+
+    # ------------------------------------------------------------------
+    def sample(
+        self,
+        samples_filename,
+        distribution: _AbstractDistribution,
+        stepsize=0.1,
+        randomize_stepsize: bool = True,
+        amount_of_steps: int = 10,
+        mass_matrix: _AbstractMassMatrix = None,
+        integrator: str = "lf",
+        initial_model=None,
+        proposals: int = 100,
+        online_thinning: int = 1,
+        diagnostic_mode: bool = False,
+        overwrite_existing_file: bool = False,
+        max_time: float = None,
+        autotuning: bool = False,
+        target_acceptance_rate: float = 0.65,
+        learning_rate: float = 0.75,
+        queue=None,
+        disable_progressbar=False,
+        chains: int = None,
+        dtype=None,
+        rng_streams=None,
+        graph: bool = True,
+        proposals_per_graph: int = None,
+        keep_samples: bool = False,
+    ):
+        """Run `proposals` HMC proposals for every chain; returns self.
+
+        Raises AssertionError / ValueError / TypeError / FileExistsError for
+        invalid arguments like the reference."""
+        self.disable_progressbar = disable_progressbar
+        self._parse(
+            samples_filename, distribution, stepsize, randomize_stepsize, amount_of_steps, mass_matrix, integrator,
+            initial_model, proposals, online_thinning, diagnostic_mode, overwrite_existing_file, max_time, autotuning,
+            target_acceptance_rate, learning_rate, chains, dtype, rng_streams, graph, proposals_per_graph, keep_samples,
+        )
+        self._setup_device()
+        self._open_files()
+        self._run()
+        return self
+
+    # ------------------------------------------------------------------
+    def _parse(self, samples_filename, distribution, stepsize, randomize_stepsize, amount_of_steps, mass_matrix,
+               integrator, initial_model, proposals, online_thinning, diagnostic_mode, overwrite_existing_file,
+               max_time, autotuning, target_acceptance_rate, learning_rate, chains, dtype, rng_streams, graph,
+               proposals_per_graph, keep_samples):
+        assert samples_filename is None or isinstance(samples_filename, (str, list, tuple)), (
+            "First argument should be a string containing the path of the file to which to write samples."
+        )
+        assert issubclass(type(distribution), _AbstractDistribution), (
+            "The passed target distribution should be a derived class of _AbstractDistribution."
+        )
+        assert type(distribution.dimensions) == int and distribution.dimensions > 0, (
+            "The passed target distribution should have an integer dimension larger than zero."
+        )
+        self.distribution = distribution
+        self.dimensions = distribution.dimensions
+        assert type(proposals) == int and proposals > 0, (
+            "The amount of proposal requested (`proposals`) should be an integer number larger than zero."
+        )
+        assert type(online_thinning) == int and online_thinning > 0, (
+            "The amount of online thinning (`online_thinning`) should be an integer number larger than zero."
+        )
+        assert proposals % online_thinning == 0, (
+            "The amount of proposals (`proposals`) needs to be a multiple of the online thinning "
+            "(`online_thinning`) number, to prevent sample wastage."
+        )
+        self.proposals = proposals
+        self.online_thinning = online_thinning
+        self.proposals_after_thinning = proposals // online_thinning
+        chains = 1 if chains is None else int(chains)
+        assert chains > 0, "The number of chains should be a positive integer."
+        self.chains = chains
+        self.dtype = _dev.normalise_dtype(dtype) if dtype is not None else ("float64" if chains == 1 else "float32")
+        # step size: scalar or one per chain
+        eps = _numpy.asarray(stepsize, dtype=_numpy.float64).reshape(-1)
+        assert eps.size in (1, chains), "stepsize must be a scalar or one value per chain"
+        assert _numpy.all(eps > 0.0), "Stepsize should be a float larger than zero."
+        self.stepsize = float(eps[0]) if eps.size == 1 else eps.copy()
+        self._eps0 = _numpy.broadcast_to(eps, (chains,)).astype(_numpy.float64).copy()
+        self.randomize_stepsize = bool(randomize_stepsize)
+        assert type(amount_of_steps) == int, (
+            "The amount of steps (amount_of_steps) the HMC integrator should make should be an integer."
+        )
+        assert amount_of_steps > 0, (
+            "The amount of steps (amount_of_steps) the HMC integrator should make should be larger than zero."
+        )
+        self.amount_of_steps = amount_of_steps
+        if mass_matrix is None:
+            mass_matrix = _Unit(self.dimensions)
+        mass_matrix.rng = self.rng
+        assert isinstance(mass_matrix, _AbstractMassMatrix), (
+            "The passed mass matrix (mass_matrix) should be a class derived from _AbstractMassMatrix."
+        )
+        assert mass_matrix.dimensions == self.dimensions, (
+            "The passed mass matrix (mass_matrix) should have dimensions equal to the target distribution. "
+            f"Passed: {mass_matrix.dimensions}, required: {self.dimensions}."
+        )
+        self.mass_matrix = mass_matrix
+        self.integrator = str(integrator)
+        if self.integrator not in self.available_integrators:
+            raise ValueError(f"Unknown integrator used. Choices are: {self.available_integrators}")
+        self.autotuning = bool(autotuning)
+        if self.autotuning:
+            assert 0.5 < learning_rate <= 1.0, (
+                "The learning rate should be larger than 0.5 and smaller than or equal to 1.0, otherwise the "
+                f"Markov chain does not converge. Chosen: {learning_rate}"
+            )
+        self.target_acceptance_rate = float(target_acceptance_rate)
+        self.learning_rate = float(learning_rate)
+        # initial model: (d,1) broadcast to every chain, or (d, C)
+        if initial_model is None:
+            q0 = _numpy.zeros((self.dimensions, chains))
+        else:
+            q0 = _numpy.array(initial_model, dtype=_numpy.float64)
+            if q0.size == self.dimensions:
+                q0 = _numpy.repeat(q0.reshape(self.dimensions, 1), chains, axis=1)
+            assert q0.shape == (self.dimensions, chains), (
+                "The initial model (`initial_model`) dimension is incompatible with the target distribution. "
+                f"Supplied model shape: {q0.shape}. Required shape: {(self.dimensions, 1)} or "
+                f"{(self.dimensions, chains)}"
+            )
+        self._q0 = q0
+        if max_time is not None:
+            max_time = float(max_time)
+            assert max_time > 0.0, "The maximal runtime (`max_time`) should be a float larger than zero."
+        self.max_time = max_time
+        self.diagnostic_mode = bool(diagnostic_mode)
+        self.overwrite_existing_file = overwrite_existing_file
+        self.samples_filename = samples_filename
+        self.rng_streams = rng_streams
+        self.use_graph = bool(graph)
+        self.keep_samples = bool(keep_samples)
+        if proposals_per_graph is None:
+            k = max(1, 32 // online_thinning) * online_thinning
+            proposals_per_graph = min(k, proposals)
+        assert proposals_per_graph % online_thinning == 0, "proposals_per_graph must be a multiple of online_thinning"
+        self.proposals_per_graph = int(proposals_per_graph)
+        self._schedule = compile_schedule(integrator_ops(self.integrator, self.amount_of_steps))
+
+    # ------------------------------------------------------------------
+    def _filenames(self):
+        fn = self.samples_filename
+        if fn is None:
+            return None
+        if isinstance(fn, (list, tuple)):
+            assert len(fn) == self.chains, "one samples filename per chain is required"
+            return list(fn)
+        if self.chains == 1:
+            return [fn]
+        stem, ext = _os.path.splitext(fn)
+        return [f"{stem}.chain{c}{ext or '.npy'}" for c in range(self.chains)]
+
+    def _open_files(self):
+        names = self._filenames()
+        self._writers = None
+        if names is None:
+            return
+        writers = []
+        try:
+            for n in names:
+                writers.append(_Samples(n, mode="w", overwrite=self.overwrite_existing_file))
+        except Exception:
+            for w in writers:
+                w.close()
+            raise
+        self._writers = writers
+        for w in writers:
+            w.write_attribute("stepsize", self.stepsize if self.chains == 1 else list(self._eps0))
+            w.write_attribute("amount_of_steps", self.amount_of_steps)
+            w.write_attribute("mass_matrix", self.mass_matrix.name)
+            w.write_attribute("integrator", self.integrators_full_names[self.integrator])
+            w.write_attribute("proposals", self.proposals)
+            w.write_attribute("acceptance_rate", 0)
+            w.write_attribute("online_thinning", self.online_thinning)
+            w.write_attribute("start_time", _datetime.now().strftime("%d-%b-%Y (%H:%M:%S.%f)"))
+            w.write_attribute("sampler", self.name)
+
+    # ------------------------------------------------------------------
+    def _setup_device(self):
+        dev = _dev.require_cuda()
+        d, C, dt = self.dimensions, self.chains, self.dtype
+        self.device = dev
+        self.stream = _torch.cuda.Stream(device=dev)
+        E = lambda shape, dtype=dt: _dev.empty(shape, dtype, dev)  # noqa: E731
+        Z = lambda shape, dtype=dt: _dev.zeros(shape, dtype, dev)  # noqa: E731
+        self.q_cur = _dev.upload(self._q0, dt, dev)
+        self.q = self.q_cur.clone()
+        self.p = Z((d, C))
+        self.g = Z((d, C))
+        self.v = Z((d, C)) if self.mass_matrix.kind == _lib.HMC_MASS_FULL else None
+        self.eps = _dev.upload(self._eps0, dt, dev)
+        self.eps_local = Z((C,))
+        self.x_cur = Z((C,), "float64")
+        self.x_prop = Z((C,), "float64")
+        self.k_cur = Z((C,), "float64")
+        self.k_prop = Z((C,), "float64")
+        self.accepted = _torch.zeros((C,), dtype=_torch.int64, device=dev)
+        self.flags = _torch.zeros((C,), dtype=_torch.int32, device=dev)
+        self.control = _torch.zeros((2,), dtype=_torch.int64, device=dev)
+        lo, hi = self.distribution.lower_bounds, self.distribution.upper_bounds
+        self.lower = _dev.upload(lo[:, 0], dt, dev) if lo is not None else None
+        self.upper = _dev.upload(hi[:, 0], dt, dev) if hi is not None else None
+        mp = self.mass_matrix.device_params(dt)
+        # ring of thinned samples
+        k = self.proposals_per_graph
+        slots = self.proposals_after_thinning if self.keep_samples else k // self.online_thinning
+        self.ring_slots = slots
+        self.ring_q = E((slots, d, C))
+        self.ring_x = E((slots, C), "float64")
+        if self.autotuning:
+            self.rec_eps = Z((self.proposals, C), "float64")
+            self.rec_acc = Z((self.proposals, C), "float64")
+        else:
+            self.rec_eps = self.rec_acc = None
+        # injected streams
+        self._stream_chunk = None
+        self.stream_z = self.stream_f = self.stream_u = None
+        if self.rng_streams is not None:
+            self.stream_z = E((k, d, C))
+            self.stream_f = E((k, C))
+            self.stream_u = E((k, C), "float64")
+            if isinstance(self.rng_streams, str):
+                if self.rng_streams != "numpy":
+                    raise ValueError("rng_streams must be None, 'numpy' or a (z, f, u) tuple")
+                base = 0 if self.seed is None else int(self.seed)
+                self._numpy_rngs = [_numpy.random.default_rng(base + c) for c in range(C)]
+            else:
+                z, f, u = self.rng_streams
+                z = _numpy.asarray(z, _numpy.float64).reshape(-1, d, C)
+                f = _numpy.asarray(f, _numpy.float64).reshape(-1, C)
+                u = _numpy.asarray(u, _numpy.float64).reshape(-1, C)
+                assert z.shape[0] >= self.proposals and u.shape[0] >= self.proposals, "streams too short"
+                self._explicit_streams = (z, f, u)
+        st = _lib.HmcChains()
+        st.dtype = _dev.dtype_code(dt)
+        st.mass_kind = self.mass_matrix.kind
+        st.dims, st.chains = d, C
+        for name in ("q_cur", "q", "p", "g", "v", "eps", "eps_local", "x_cur", "x_prop", "k_cur", "k_prop",
+                     "accepted", "flags"):
+            setattr(st, name, _dev.ptr(getattr(self, name)))
+        st.proposal = self.control.data_ptr()
+        st.mass_diag = _dev.ptr(mp.get("diag"))
+        st.mass_inv_diag = _dev.ptr(mp.get("inv_diag"))
+        st.mass_chol = _dev.ptr(mp.get("chol"))
+        st.mass_inv = _dev.ptr(mp.get("inv"))
+        st.lower, st.upper = _dev.ptr(self.lower), _dev.ptr(self.upper)
+        st.seed = self.philox_seed
+        st.randomize_stepsize = int(self.randomize_stepsize)
+        st.autotune = int(self.autotuning)
+        st.target_acceptance = self.target_acceptance_rate
+        st.learning_rate = self.learning_rate
+        st.minimal_stepsize = self.minimal_stepsize
+        st.stream_z, st.stream_eps, st.stream_u = _dev.ptr(self.stream_z), _dev.ptr(self.stream_f), _dev.ptr(self.stream_u)
+        st.stream_len = k if self.rng_streams is not None else 0
+        st.ring_q, st.ring_x = self.ring_q.data_ptr(), self.ring_x.data_ptr()
+        st.ring_slots, st.thinning = slots, self.online_thinning
+        st.rec_stepsize, st.rec_acceptance = _dev.ptr(self.rec_eps), _dev.ptr(self.rec_acc)
+        st.rec_len = self.proposals if self.autotuning else 0
+        self._state = st
+        self._state_ref = _ct.byref(st)
+        # Initial misfit (reference asserts it is finite, Samplers.py:419-426).
+        self.stream.wait_stream(_torch.cuda.current_stream(dev))
+        h = self.stream.cuda_stream
+        self.distribution._device_misfit(self.q_cur, self.x_cur, False, dt, h)
+        # Allocate every scratch buffer of the target before any capture.
+        self.distribution._device_gradient(self.q_cur, self.g, False, dt, h)
+        self.distribution._device_misfit(self.q_cur, self.x_prop, False, dt, h)
+        self.stream.synchronize()
+        x0 = self.x_cur.cpu().numpy()
+        assert not _numpy.any(_numpy.isnan(x0)), "Initial position in model space gives NaN probability"
+        assert not _numpy.any(_numpy.isinf(x0)), "Initial position in model space gives inf/-inf probability"
+        self.current_x = x0[0] if C == 1 else x0
+        self._graph = None
+
+    # ------------------------------------------------------------------
+    def _issue_proposal(self, h):
+        """Enqueue one proposal for every chain on stream handle h."""
+        st, dist, dt = self._state_ref, self.distribution, self.dtype
+        first, steps = self._schedule
+        _lib.call("hmc_begin_trajectory", st, first, h)
+        for needs_grad, kick, drift in steps:
+            if needs_grad:
+                dist._device_gradient(self.q, self.g, False, dt, h)
+            _lib.call("hmc_kick_drift", st, kick, drift, h)
+        dist._device_misfit(self.q, self.x_prop, False, dt, h)
+        _lib.call("hmc_end_trajectory", st, h)
+
+    def _issue_block(self, n_props, h):
+        for _ in range(n_props):
+            self._issue_proposal(h)
+
+    def _load_streams(self, n0, n):
+        """Copy the injected random streams of proposals [n0, n0+n) to the device."""
+        if self.rng_streams is None:
+            return
+        d, C = self.dimensions, self.chains
+        if isinstance(self.rng_streams, str):
+            z = _numpy.empty((n, d, C))
+            f = _numpy.ones((n, C))
+            u = _numpy.empty((n, C))
+            for c, rng in enumerate(self._numpy_rngs):
+                for j in range(n):
+                    z[j, :, c] = rng.normal(size=(d, 1))[:, 0]
+                    if self.randomize_stepsize:
+                        f[j, c] = rng.uniform(0.5, 1.5)
+                    u[j, c] = rng.uniform(0, 1)
+        else:
+            zz, ff, uu = self._explicit_streams
+            z, f, u = zz[n0 : n0 + n], ff[n0 : n0 + n], uu[n0 : n0 + n]
+        with _torch.cuda.stream(self.stream):
+            self.stream_z[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(z)).to(self.stream_z.dtype), non_blocking=False)
+            self.stream_f[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(f)).to(self.stream_f.dtype), non_blocking=False)
+            self.stream_u[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(u)), non_blocking=False)
+
+    def _drain(self, n0, n):
+        """Move the thinned samples of proposals [n0, n0+n) to the files."""
+        if self._writers is None or self.keep_samples:
+            return
+        m = n // self.online_thinning
+        if m == 0:
+            return
+        with _torch.cuda.stream(self.stream):
+            q = self.ring_q[:m].to(_torch.float64).cpu().numpy()  # m, d, C
+            x = self.ring_x[:m].cpu().numpy()  # m, C
+        for c, w in enumerate(self._writers):
+            w.append_columns(_numpy.vstack([q[:, :, c].T, x[None, :, c]]))
+
+    def _run(self):
+        h = self.stream.cuda_stream
+        k = self.proposals_per_graph
+        P = self.proposals
+        self._start_time = _datetime.now()
+        t0 = _time.time()
+        deadline = t0 + self.max_time if self.max_time is not None else None
+        done = 0
+        n_blocks_timed = 0
+        launches0 = _lib.launch_count()
+        try:
+            while done < P:
+                n = min(k, P - done)
+                self._load_streams(done, n)
+                if self.use_graph and n == k:
+                    if self._graph is None:
+                        _lib.call("hmc_graph_begin", h)
+                        try:
+                            self._issue_block(k, h)
+                        finally:
+                            exec_ptr = _ct.c_void_p()
+                            rc = _lib.load().hmc_graph_end(h, _ct.byref(exec_ptr))
+                        _lib.check(rc, "hmc_graph_end")
+                        self._graph = exec_ptr
+                    _lib.call("hmc_graph_launch", self._graph, h)
+                else:
+                    self._issue_block(n, h)
+                self._drain(done, n)
+                done += n
+                n_blocks_timed += 1
+                if deadline is not None and _time.time() > deadline:
+                    self.stream.synchronize()
+                    raise TimeoutError
+        except TimeoutError:
+            pass
+        except KeyboardInterrupt:
+            pass
+        finally:
+            self.stream.synchronize()
+            self._end_time = _datetime.now()
+            self.runtime_seconds = _time.time() - t0
+            self.kernel_launches = _lib.launch_count() - launches0
+            self.proposals_done = done
+            if self._graph is not None:
+                _lib.call("hmc_graph_destroy", self._graph)
+                self._graph = None
+            self._finalise(done)
+
+    def _finalise(self, done):
+        C = self.chains
+        self.current_proposal = max(done - 1, 0)
+        acc = self.accepted.cpu().numpy()
+        self.accepted_proposals = int(acc[0]) if C == 1 else acc
+        q = self.q_cur.to(_torch.float64).cpu().numpy()
+        self.current_model = q
+        x = self.x_cur.cpu().numpy()
+        self.current_x = float(x[0]) if C == 1 else x
+        eps = self.eps.to(_torch.float64).cpu().numpy()
+        if self.autotuning:
+            self.stepsize = float(eps[0]) if C == 1 else eps
+            n = self.current_proposal  # the reference keeps [:current_proposal]
+            se = self.rec_eps[:n].cpu().numpy()
+            ra = self.rec_acc[:n].cpu().numpy()
+            self.stepsizes = se if C > 1 else se[:, :1]
+            self.acceptance_rates = ra if C > 1 else ra[:, :1]
+        rate = acc / max(done, 1)
+        self.acceptance_rate = rate
+        if self._writers is not None:
+            for c, w in enumerate(self._writers):
+                w.write_attribute("acceptance_rate", float(rate[c]))
+                w.write_attribute("end_time", self._end_time.strftime("%d-%b-%Y (%H:%M:%S.%f)"))
+                w.write_attribute("runtime", str(self._end_time - self._start_time))
+                w.write_attribute("runtime_seconds", (self._end_time - self._start_time).total_seconds())
+                if self.autotuning:
+                    w.write_attribute("acceptance_rates", self.acceptance_rates[:, c : c + 1])
+                    w.write_attribute("stepsizes", self.stepsizes[:, c : c + 1])
+                w.close()
+            self._writers = None
+        if self.keep_samples:
+            m = done // self.online_thinning
+            self.samples_device = (self.ring_q[:m], self.ring_x[:m])
+
+    # ------------------------------------------------------------------
+    def samples_numpy(self, chain=None):
+        """Samples kept on the device as (d+1, N) per chain (reference layout);
+        (C, d+1, N) for all chains when `chain` is None."""
+        assert self.samples_device is not None, "sample(..., keep_samples=True) keeps samples on the device"
+        q, x = self.samples_device
+        q = q.to(_torch.float64).cpu().numpy()  # N, d, C
+        x = x.cpu().numpy()  # N, C
+        full = _numpy.concatenate([_numpy.transpose(q, (2, 1, 0)), x.T[:, None, :]], axis=1)
+        return full if chain is None else full[chain]
+
+    def load_results(self, burn_in: int = 0, chain: int = 0):
+        assert burn_in >= 0
+        names = self._filenames()
+        assert names is not None, "no samples file was written"
+        with _Samples(names[chain], burn_in=burn_in) as s:
+            return _numpy.array(s.numpy)

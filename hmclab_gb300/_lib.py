@@ -1,0 +1,186 @@
+"""ctypes binding of the C ABI declared in include/hmclab_gb300.h.
+
+The shared library is built in-tree (`hmclab_gb300/libhmclab_gb300.so`, see
+`build.py`).  There is no CPU fallback: every device operation raises
+`DeviceUnavailableError` when the library or a CUDA device is missing.
+"""
+import ctypes as _ct
+import os as _os
+import threading as _threading
+
+from hmclab_gb300.Helpers.CustomExceptions import DeviceUnavailableError, DeviceTimeoutError
+
+_HERE = _os.path.dirname(_os.path.abspath(__file__))
+LIB_PATH = _os.path.join(_HERE, "libhmclab_gb300.so")
+
+HMC_OK = 0
+HMC_ERR_INVALID_ARG = 1
+HMC_ERR_CUDA = 2
+HMC_ERR_TIMEOUT = 3
+HMC_ERR_NONFINITE = 4
+HMC_ERR_UNSUPPORTED = 5
+
+HMC_F32 = 0
+HMC_F64 = 1
+
+HMC_MASS_UNIT = 0
+HMC_MASS_DIAG = 1
+HMC_MASS_FULL = 2
+
+HMC_FLAG_OUT_OF_BOUNDS = 1
+
+c_void_p = _ct.c_void_p
+c_int = _ct.c_int
+c_int32 = _ct.c_int32
+c_int64 = _ct.c_int64
+c_uint32 = _ct.c_uint32
+c_uint64 = _ct.c_uint64
+c_double = _ct.c_double
+c_char_p = _ct.c_char_p
+
+
+class HmcChains(_ct.Structure):
+    """Mirror of `hmc_chains` in include/hmclab_gb300.h (field order matters)."""
+
+    _fields_ = [
+        ("dtype", c_int32),
+        ("mass_kind", c_int32),
+        ("dims", c_int64),
+        ("chains", c_int64),
+        ("q_cur", c_void_p),
+        ("q", c_void_p),
+        ("p", c_void_p),
+        ("g", c_void_p),
+        ("v", c_void_p),
+        ("mass_diag", c_void_p),
+        ("mass_inv_diag", c_void_p),
+        ("mass_chol", c_void_p),
+        ("mass_inv", c_void_p),
+        ("lower", c_void_p),
+        ("upper", c_void_p),
+        ("eps", c_void_p),
+        ("eps_local", c_void_p),
+        ("x_cur", c_void_p),
+        ("x_prop", c_void_p),
+        ("k_cur", c_void_p),
+        ("k_prop", c_void_p),
+        ("accepted", c_void_p),
+        ("flags", c_void_p),
+        ("proposal", c_void_p),
+        ("seed", c_uint64),
+        ("randomize_stepsize", c_int32),
+        ("autotune", c_int32),
+        ("target_acceptance", c_double),
+        ("learning_rate", c_double),
+        ("minimal_stepsize", c_double),
+        ("stream_z", c_void_p),
+        ("stream_eps", c_void_p),
+        ("stream_u", c_void_p),
+        ("stream_len", c_int64),
+        ("ring_q", c_void_p),
+        ("ring_x", c_void_p),
+        ("ring_slots", c_int64),
+        ("thinning", c_int64),
+        ("rec_stepsize", c_void_p),
+        ("rec_acceptance", c_void_p),
+        ("rec_len", c_int64),
+    ]
+
+
+P = c_void_p
+I = c_int
+I64 = c_int64
+D = c_double
+S = c_void_p  # stream
+
+# name -> argtypes (restype is int unless listed in _RESTYPES)
+SIGNATURES = {
+    "hmc_version": [],
+    "hmc_last_error": [],
+    "hmc_launch_count": [],
+    "hmc_philox_normal": [I, I64, I64, c_uint64, c_uint64, c_uint32, P, S],
+    "hmc_philox_raw": [I64, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, P, S],
+    "hmc_begin_trajectory": [P, D, S],
+    "hmc_kick_drift": [P, D, D, S],
+    "hmc_end_trajectory": [P, S],
+    "hmc_kinetic_energy": [P, P, P, S],
+    "hmc_kinetic_energy_gradient": [P, P, P, S],
+    "hmc_normal_diag_misfit": [I, I64, I64, P, P, P, P, I, S],
+    "hmc_normal_diag_gradient": [I, I64, I64, P, P, P, P, I, S],
+    "hmc_normal_full_misfit": [I, I64, I64, P, P, P, P, P, I, S],
+    "hmc_normal_full_gradient": [I, I64, I64, P, P, P, P, P, I, S],
+    "hmc_laplace_misfit": [I, I64, I64, P, P, P, P, I, S],
+    "hmc_laplace_gradient": [I, I64, I64, P, P, P, P, I, S],
+    "hmc_dense_premul_gradient": [I, I64, I64, P, P, P, P, I, S],
+    "hmc_dense_premul_misfit": [I, I64, I64, P, P, P, D, P, P, I, S],
+    "hmc_dense_resid_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, S],
+    "hmc_dense_resid_gradient": [I, I64, I64, I64, P, P, P, P, P, P, P, I, S],
+    "hmc_csr_misfit": [I, I64, I64, I64, P, P, P, P, P, P, P, P, I, S],
+    "hmc_csr_gradient": [I, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, I, S],
+    "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
+    "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
+    "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
+    "hmc_graph_begin": [S],
+    "hmc_graph_end": [S, _ct.POINTER(c_void_p)],
+    "hmc_graph_launch": [P, S],
+    "hmc_graph_destroy": [P],
+}
+_RESTYPES = {"hmc_last_error": c_char_p, "hmc_launch_count": c_int64}
+
+_lock = _threading.Lock()
+_lib = None
+
+
+def library_available():
+    return _os.path.exists(LIB_PATH)
+
+
+def load():
+    """Load the shared library once; raise DeviceUnavailableError if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not _os.path.exists(LIB_PATH):
+            raise DeviceUnavailableError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(hmclab_gb300 has no CPU fallback)"
+            )
+        lib = _ct.CDLL(LIB_PATH)
+        for name, argtypes in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = argtypes
+            fn.restype = _RESTYPES.get(name, c_int)
+        _lib = lib
+    return _lib
+
+
+def last_error():
+    return load().hmc_last_error().decode(errors="replace")
+
+
+def check(rc, name):
+    """Map a C status code to the exception class the reference raises."""
+    if rc == HMC_OK:
+        return
+    msg = f"{name}: {last_error()}"
+    if rc == HMC_ERR_INVALID_ARG:
+        raise ValueError(msg)
+    if rc == HMC_ERR_TIMEOUT:
+        raise DeviceTimeoutError(msg)
+    if rc == HMC_ERR_NONFINITE:
+        raise FloatingPointError(msg)
+    if rc == HMC_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise RuntimeError(msg)
+
+
+def call(name, *args):
+    rc = getattr(load(), name)(*args)
+    check(rc, name)
+
+
+def launch_count():
+    return int(load().hmc_launch_count())

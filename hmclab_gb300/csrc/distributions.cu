@@ -1,0 +1,472 @@
+// Batched misfit / gradient kernels of the target distributions on the HMC
+// path.  Every misfit is an FP64 per-chain sum; every gradient is written (or
+// accumulated, for BayesRule sums) into a [d][C] array of the state dtype.
+//
+//   Normal (diag / full)   Distributions/base.py:539-574
+//   Laplace                Distributions/base.py:689-710
+//   LinearMatrix dense     Distributions/LinearMatrix.py:139-222
+//   LinearMatrix sparse    Distributions/LinearMatrix.py:309-440
+//   SourceLocation3D       Distributions/SourceLocation.py:482-540,697-713
+#include <math.h>
+
+#include "common.cuh"
+
+namespace hmc {
+int gemm_ex(int dtype, int64_t m, int64_t n, int64_t k, double alpha, const void* A, const void* B, const void* bias,
+            double bias_scale, const void* row_scale, void* out, int accumulate, cudaStream_t stream);
+}
+
+namespace hmc {
+namespace {
+
+inline unsigned ew_grid(int64_t n) {
+  const unsigned b = blocks_for(n, 256);
+  return b > 152u * 32u ? 152u * 32u : b;
+}
+
+// out[i][c] = M[i][c] - mean[i]
+template <typename T>
+__global__ void centre_kernel(int64_t d, int64_t C, const T* __restrict__ M, const T* __restrict__ mean, T* out) {
+  const int64_t total = d * C;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    out[idx] = M[idx] - mean[idx / C];
+}
+
+// ---- elementwise priors -----------------------------------------------------
+enum PriorKind { PRIOR_NORMAL_DIAG = 0, PRIOR_LAPLACE = 1 };
+
+template <typename T, int KIND>
+__global__ void prior_misfit_kernel(int64_t d, int64_t C, const T* __restrict__ M, const T* __restrict__ mean,
+                                    const T* __restrict__ w, double* out, int accumulate) {
+  __shared__ double sh[RED_Y][RED_X + 1];
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  double acc = 0.0;
+  if (c < C) {
+    for (int64_t i = threadIdx.y; i < d; i += RED_Y) {
+      const T m = M[i * C + c];
+      if (KIND == PRIOR_NORMAL_DIAG) {
+        const T r = mean[i] - m;  // (means - coordinates)
+        acc += (double)r * (double)(w[i] * r);
+      } else {
+        const T r = m - mean[i];
+        acc += (double)(fabs(r) * w[i]);
+      }
+    }
+  }
+  const double s = block_chain_sum(acc, sh);
+  if (c < C && threadIdx.y == 0) {
+    const double v = KIND == PRIOR_NORMAL_DIAG ? 0.5 * s : s;
+    out[c] = accumulate ? out[c] + v : v;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T sgn(T x) {
+  return x > (T)0 ? (T)1 : (x < (T)0 ? (T)-1 : (T)0);
+}
+
+template <typename T, int KIND>
+__global__ void prior_gradient_kernel(int64_t d, int64_t C, const T* __restrict__ M, const T* __restrict__ mean,
+                                      const T* __restrict__ w, T* out, int accumulate) {
+  const int64_t total = d * C;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / C;
+    const T m = M[idx];
+    T g;
+    if (KIND == PRIOR_NORMAL_DIAG)
+      g = -(w[i] * (mean[i] - m));
+    else
+      g = sgn(m - mean[i]) * w[i];
+    out[idx] = accumulate ? out[idx] + g : g;
+  }
+}
+
+template <typename T, int KIND>
+int prior_misfit(int64_t d, int64_t C, const void* M, const void* mean, const void* w, double* out, int accumulate,
+                 cudaStream_t st, const char* who) {
+  HMC_REQUIRE(d > 0 && C >= 0, "%s: bad sizes", who);
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && mean && w && out, "%s: null argument", who);
+  prior_misfit_kernel<T, KIND><<<red_grid(C), red_block(), 0, st>>>(d, C, (const T*)M, (const T*)mean,
+                                                                    (const T*)w, out, accumulate);
+  return check_launch(who);
+}
+
+template <typename T, int KIND>
+int prior_gradient(int64_t d, int64_t C, const void* M, const void* mean, const void* w, void* out, int accumulate,
+                   cudaStream_t st, const char* who) {
+  HMC_REQUIRE(d > 0 && C >= 0, "%s: bad sizes", who);
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && mean && w && out, "%s: null argument", who);
+  prior_gradient_kernel<T, KIND><<<ew_grid(d * C), 256, 0, st>>>(d, C, (const T*)M, (const T*)mean, (const T*)w,
+                                                                 (T*)out, accumulate);
+  return check_launch(who);
+}
+
+// ---- per-chain quadratic forms ---------------------------------------------
+// out[c] (+)= scale * (sum_i a[i][c] * (b[i][c] + sb * bvec[i]) + add)
+template <typename T>
+__global__ void dot_columns_kernel(int64_t d, int64_t C, const T* __restrict__ a, const T* __restrict__ b,
+                                   const T* __restrict__ bvec, double sb, double add, double scale, double* out,
+                                   int accumulate) {
+  __shared__ double sh[RED_Y][RED_X + 1];
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  double acc = 0.0;
+  if (c < C) {
+    for (int64_t i = threadIdx.y; i < d; i += RED_Y) {
+      double bv = (double)b[i * C + c];
+      if (bvec) bv += sb * (double)bvec[i];
+      acc += (double)a[i * C + c] * bv;
+    }
+  }
+  const double s = block_chain_sum(acc, sh);
+  if (c < C && threadIdx.y == 0) {
+    const double v = scale * (s + add);
+    out[c] = accumulate ? out[c] + v : v;
+  }
+}
+
+// out[c] (+)= 0.5 * sum_j r[j][c]^2 * w[j]
+template <typename T>
+__global__ void weighted_sq_kernel(int64_t n, int64_t C, const T* __restrict__ r, const T* __restrict__ w,
+                                   double* out, int accumulate) {
+  __shared__ double sh[RED_Y][RED_X + 1];
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  double acc = 0.0;
+  if (c < C) {
+    for (int64_t j = threadIdx.y; j < n; j += RED_Y) {
+      const double rv = (double)r[j * C + c];
+      acc += rv * rv * (double)w[j];
+    }
+  }
+  const double s = block_chain_sum(acc, sh);
+  if (c < C && threadIdx.y == 0) {
+    const double v = 0.5 * s;
+    out[c] = accumulate ? out[c] + v : v;
+  }
+}
+
+// ---- CSR sparse-times-dense (chains fastest) -------------------------------
+// out[j][c] = (sum_k val[k] X[col[k]][c] - (bias ? bias[j] : 0)) * (rs ? rs[j] : 1) (+ out)
+template <typename T>
+__global__ void csr_spmm_kernel(int64_t rows, int64_t C, const int32_t* __restrict__ rp,
+                                const int32_t* __restrict__ col, const T* __restrict__ val, const T* __restrict__ X,
+                                const T* __restrict__ bias, const T* __restrict__ rs, T* out, int accumulate) {
+  const int64_t j = blockIdx.y;
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= rows || c >= C) return;
+  T acc = (T)0;
+  const int32_t b = rp[j], e = rp[j + 1];
+  for (int32_t k = b; k < e; ++k) acc += val[k] * X[(int64_t)col[k] * C + c];
+  if (bias) acc -= bias[j];
+  if (rs) acc *= rs[j];
+  const int64_t o = j * C + c;
+  out[o] = accumulate ? out[o] + acc : acc;
+}
+
+template <typename T>
+int csr_spmm(int64_t rows, int64_t C, const int32_t* rp, const int32_t* col, const void* val, const void* X,
+             const void* bias, const void* rs, void* out, int accumulate, cudaStream_t st) {
+  HMC_REQUIRE(rows <= 65535 * 1024ll, "csr: too many rows");
+  const int threads = C >= 256 ? 256 : (C >= 128 ? 128 : (C >= 64 ? 64 : 32));
+  dim3 grid((unsigned)((C + threads - 1) / threads), 1);
+  // grid.y is limited to 65535: split tall matrices into row batches.
+  for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
+    const int64_t nr = rows - r0 < 65535 ? rows - r0 : 65535;
+    grid.y = (unsigned)nr;
+    csr_spmm_kernel<T><<<grid, threads, 0, st>>>(nr, C, rp + r0, col, (const T*)val, (const T*)X,
+                                                 bias ? (const T*)bias + r0 : nullptr,
+                                                 rs ? (const T*)rs + r0 : nullptr, (T*)out + r0 * C, accumulate);
+    HMC_TRY(check_launch("csr_spmm_kernel"));
+  }
+  return HMC_OK;
+}
+
+// ---- 3-D source location ----------------------------------------------------
+// One thread per (chain, event); stations are staged in shared memory.  The
+// per-pair terms mirror SourceLocation.py:495-540, including nansum's skipping
+// of NaN terms (missing observations, zero distances).
+constexpr int SL_EY = 8;  // event lanes per block (threadIdx.y)
+
+template <typename T, bool GRAD>
+__global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restrict__ M, const T* __restrict__ rx,
+                              const T* __restrict__ ry, const T* __restrict__ rz, const T* __restrict__ obs,
+                              const T* __restrict__ iv, int infer_v, T v_fixed, double* out_x, T* out_g,
+                              int accumulate) {
+  extern __shared__ unsigned char smem_raw[];
+  T* srx = (T*)smem_raw;
+  T* sry = srx + S;
+  T* srz = sry + S;
+  __shared__ double red[SL_EY][RED_X + 1];
+  for (int64_t s = threadIdx.y * blockDim.x + threadIdx.x; s < S; s += blockDim.x * blockDim.y) {
+    srx[s] = rx[s];
+    sry[s] = ry[s];
+    srz[s] = rz[s];
+  }
+  __syncthreads();
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  const bool live = c < C;
+  const T v = live ? (infer_v ? M[(4 * E) * C + c] : v_fixed) : (T)1;
+  double mis = 0.0;
+  T gv = (T)0;
+  if (live) {
+    for (int64_t e = threadIdx.y; e < E; e += SL_EY) {
+      const T x = M[(4 * e + 0) * C + c], y = M[(4 * e + 1) * C + c], z = M[(4 * e + 2) * C + c],
+              t0 = M[(4 * e + 3) * C + c];
+      T gx = 0, gy = 0, gz = 0, gT = 0;
+      double me = 0.0;
+      for (int64_t s = 0; s < S; ++s) {
+        const T dx = x - srx[s], dy = y - sry[s], dz = z - srz[s];
+        const T dist = sqrt(dx * dx + dy * dy + dz * dz);
+        const T tc = t0 + dist / v;
+        const T o = obs[e * S + s], w = iv[e * S + s];
+        if (!GRAD) {
+          const T r = o - tc;
+          const T term = r * r * w;
+          if (!isnan(term)) me += (double)term;
+        } else {
+          const T mg = (tc - o) * w;  // (t_calc - obs) / std^2
+          const T vd = v * dist;
+          T t;
+          t = mg * (dx / vd);
+          if (!isnan(t)) gx += t;
+          t = mg * (dy / vd);
+          if (!isnan(t)) gy += t;
+          t = mg * (dz / vd);
+          if (!isnan(t)) gz += t;
+          if (!isnan(mg)) gT += mg;
+          t = mg * (-dist / (v * v));
+          if (!isnan(t)) gv += t;
+        }
+      }
+      if (GRAD) {
+        const int64_t o0 = (4 * e) * C + c;
+        if (accumulate) {
+          out_g[o0] += gx;
+          out_g[o0 + C] += gy;
+          out_g[o0 + 2 * C] += gz;
+          out_g[o0 + 3 * C] += gT;
+        } else {
+          out_g[o0] = gx;
+          out_g[o0 + C] = gy;
+          out_g[o0 + 2 * C] = gz;
+          out_g[o0 + 3 * C] = gT;
+        }
+      } else {
+        mis += me;
+      }
+    }
+  }
+  // Reduce the velocity gradient (or the misfit) over the event lanes.
+  red[threadIdx.y][threadIdx.x] = GRAD ? (double)gv : mis;
+  __syncthreads();
+  if (threadIdx.y == 0 && live) {
+    double s = 0.0;
+    for (int y = 0; y < SL_EY; ++y) s += red[y][threadIdx.x];
+    if (GRAD) {
+      if (infer_v) {
+        const int64_t o = (4 * E) * C + c;
+        out_g[o] = accumulate ? out_g[o] + (T)s : (T)s;
+      }
+    } else {
+      const double val = 0.5 * s;
+      out_x[c] = accumulate ? out_x[c] + val : val;
+    }
+  }
+}
+
+template <typename T>
+int srcloc(bool grad, int64_t E, int64_t S, int64_t C, const void* M, const void* rx, const void* ry, const void* rz,
+           const void* obs, const void* iv, int infer_v, double v_fixed, double* out_x, void* out_g, int accumulate,
+           cudaStream_t st) {
+  const char* who = grad ? "hmc_srcloc3d_gradient" : "hmc_srcloc3d_misfit";
+  HMC_REQUIRE(E > 0 && S > 0 && C >= 0, "%s: bad sizes", who);
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && rx && ry && rz && obs && iv, "%s: null argument", who);
+  HMC_REQUIRE(grad ? out_g != nullptr : out_x != nullptr, "%s: null output", who);
+  const size_t smem = 3 * (size_t)S * sizeof(T);
+  HMC_REQUIRE(smem <= 160 * 1024, "%s: too many stations (%lld)", who, (long long)S);
+  auto kern = grad ? srcloc_kernel<T, true> : srcloc_kernel<T, false>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(srcloc)");
+  }
+  kern<<<red_grid(C), dim3(RED_X, SL_EY), smem, st>>>(E, S, C, (const T*)M, (const T*)rx, (const T*)ry,
+                                                       (const T*)rz, (const T*)obs, (const T*)iv, infer_v,
+                                                       (T)v_fixed, out_x, (T*)out_g, accumulate);
+  return check_launch(who);
+}
+
+}  // namespace
+}  // namespace hmc
+
+using namespace hmc;
+
+extern "C" {
+
+int hmc_normal_diag_misfit(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_var,
+                           double* out_x, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return prior_misfit<T, PRIOR_NORMAL_DIAG>(d, C, M, mean, inv_var, out_x, accumulate, as_stream(stream),
+                                              "hmc_normal_diag_misfit");
+  });
+}
+
+int hmc_normal_diag_gradient(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_var,
+                             void* out_g, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return prior_gradient<T, PRIOR_NORMAL_DIAG>(d, C, M, mean, inv_var, out_g, accumulate, as_stream(stream),
+                                                "hmc_normal_diag_gradient");
+  });
+}
+
+int hmc_laplace_misfit(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_disp,
+                       double* out_x, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return prior_misfit<T, PRIOR_LAPLACE>(d, C, M, mean, inv_disp, out_x, accumulate, as_stream(stream),
+                                          "hmc_laplace_misfit");
+  });
+}
+
+int hmc_laplace_gradient(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_disp,
+                         void* out_g, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return prior_gradient<T, PRIOR_LAPLACE>(d, C, M, mean, inv_disp, out_g, accumulate, as_stream(stream),
+                                            "hmc_laplace_gradient");
+  });
+}
+
+// Normal with full covariance (base.py:553-574): with D = m - mu,
+// misfit 0.5 D^T S^-1 D and gradient -S^-1 (mu - m) = S^-1 D.
+// work holds 2*d*C elements of the state dtype (gradient uses the first d*C).
+int hmc_normal_full_misfit(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_cov,
+                           void* work, double* out_x, int accumulate, void* stream) {
+  HMC_REQUIRE(d > 0 && C >= 0, "hmc_normal_full_misfit: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && mean && inv_cov && work && out_x, "hmc_normal_full_misfit: null argument");
+  cudaStream_t st = as_stream(stream);
+  return HMC_DISPATCH(dtype, T, [&] {
+    T* D = (T*)work;
+    T* SD = D + d * C;
+    centre_kernel<T><<<ew_grid(d * C), 256, 0, st>>>(d, C, (const T*)M, (const T*)mean, D);
+    HMC_TRY(check_launch("centre_kernel"));
+    HMC_TRY(gemm_ex(dtype, d, C, d, 1.0, inv_cov, D, nullptr, 0.0, nullptr, SD, 0, st));
+    dot_columns_kernel<T><<<red_grid(C), red_block(), 0, st>>>(d, C, D, SD, nullptr, 0.0, 0.0, 0.5, out_x,
+                                                               accumulate);
+    return check_launch("dot_columns_kernel");
+  });
+}
+
+int hmc_normal_full_gradient(int dtype, int64_t d, int64_t C, const void* M, const void* mean, const void* inv_cov,
+                             void* work, void* out_g, int accumulate, void* stream) {
+  HMC_REQUIRE(d > 0 && C >= 0, "hmc_normal_full_gradient: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && mean && inv_cov && work && out_g, "hmc_normal_full_gradient: null argument");
+  cudaStream_t st = as_stream(stream);
+  return HMC_DISPATCH(dtype, T, [&] {
+    centre_kernel<T><<<ew_grid(d * C), 256, 0, st>>>(d, C, (const T*)M, (const T*)mean, (T*)work);
+    HMC_TRY(check_launch("centre_kernel"));
+    return gemm_ex(dtype, d, C, d, 1.0, inv_cov, work, nullptr, 0.0, nullptr, out_g, accumulate, st);
+  });
+}
+
+int hmc_dense_premul_gradient(int dtype, int64_t d, int64_t C, const void* M, const void* GtG, const void* Gtd0,
+                              void* out_g, int accumulate, void* stream) {
+  HMC_REQUIRE(d > 0 && C >= 0, "hmc_dense_premul_gradient: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && GtG && Gtd0 && out_g, "hmc_dense_premul_gradient: null argument");
+  return gemm_ex(dtype, d, C, d, 1.0, GtG, M, Gtd0, -1.0, nullptr, out_g, accumulate, as_stream(stream));
+}
+
+int hmc_dense_premul_misfit(int dtype, int64_t d, int64_t C, const void* M, const void* GtG, const void* Gtd0,
+                            double dtd, void* work, double* out_x, int accumulate, void* stream) {
+  HMC_REQUIRE(d > 0 && C >= 0, "hmc_dense_premul_misfit: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && GtG && Gtd0 && work && out_x, "hmc_dense_premul_misfit: null argument");
+  cudaStream_t st = as_stream(stream);
+  // work = GtG m - 2 Gtd0; x = 0.5 * (m^T work + dtd)   (LinearMatrix.py:184-191)
+  HMC_TRY(gemm_ex(dtype, d, C, d, 1.0, GtG, M, Gtd0, -2.0, nullptr, work, 0, st));
+  return HMC_DISPATCH(dtype, T, [&] {
+    dot_columns_kernel<T><<<red_grid(C), red_block(), 0, st>>>(d, C, (const T*)M, (const T*)work, nullptr, 0.0, dtd,
+                                                               0.5, out_x, accumulate);
+    return check_launch("dot_columns_kernel");
+  });
+}
+
+int hmc_dense_resid_misfit(int dtype, int64_t n, int64_t d, int64_t C, const void* M, const void* G,
+                           const void* data, const void* inv_var, void* resid, double* out_x, int accumulate,
+                           void* stream) {
+  HMC_REQUIRE(n > 0 && d > 0 && C >= 0, "hmc_dense_resid_misfit: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && G && data && inv_var && resid && out_x, "hmc_dense_resid_misfit: null argument");
+  cudaStream_t st = as_stream(stream);
+  HMC_TRY(gemm_ex(dtype, n, C, d, 1.0, G, M, data, -1.0, nullptr, resid, 0, st));
+  return HMC_DISPATCH(dtype, T, [&] {
+    weighted_sq_kernel<T><<<red_grid(C), red_block(), 0, st>>>(n, C, (const T*)resid, (const T*)inv_var, out_x,
+                                                               accumulate);
+    return check_launch("weighted_sq_kernel");
+  });
+}
+
+int hmc_dense_resid_gradient(int dtype, int64_t n, int64_t d, int64_t C, const void* M, const void* G,
+                             const void* Gt, const void* data, const void* inv_var, void* resid, void* out_g,
+                             int accumulate, void* stream) {
+  HMC_REQUIRE(n > 0 && d > 0 && C >= 0, "hmc_dense_resid_gradient: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && G && Gt && data && inv_var && resid && out_g, "hmc_dense_resid_gradient: null argument");
+  cudaStream_t st = as_stream(stream);
+  HMC_TRY(gemm_ex(dtype, n, C, d, 1.0, G, M, data, -1.0, inv_var, resid, 0, st));
+  return gemm_ex(dtype, d, C, n, 1.0, Gt, resid, nullptr, 0.0, nullptr, out_g, accumulate, st);
+}
+
+int hmc_csr_misfit(int dtype, int64_t n, int64_t d, int64_t C, const void* M, const int32_t* row_ptr,
+                   const int32_t* col, const void* val, const void* data, const void* inv_var, void* resid,
+                   double* out_x, int accumulate, void* stream) {
+  HMC_REQUIRE(n > 0 && d > 0 && C >= 0, "hmc_csr_misfit: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && row_ptr && col && val && data && inv_var && resid && out_x, "hmc_csr_misfit: null argument");
+  cudaStream_t st = as_stream(stream);
+  return HMC_DISPATCH(dtype, T, [&] {
+    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, nullptr, resid, 0, st));
+    weighted_sq_kernel<T><<<red_grid(C), red_block(), 0, st>>>(n, C, (const T*)resid, (const T*)inv_var, out_x,
+                                                               accumulate);
+    return check_launch("weighted_sq_kernel");
+  });
+}
+
+int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C, const void* M, const int32_t* row_ptr,
+                     const int32_t* col, const void* val, const int32_t* t_row_ptr, const int32_t* t_col,
+                     const void* t_val, const void* data, const void* inv_var, void* resid, void* out_g,
+                     int accumulate, void* stream) {
+  HMC_REQUIRE(n > 0 && d > 0 && C >= 0, "hmc_csr_gradient: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && row_ptr && col && val && t_row_ptr && t_col && t_val && data && inv_var && resid && out_g,
+              "hmc_csr_gradient: null argument");
+  cudaStream_t st = as_stream(stream);
+  return HMC_DISPATCH(dtype, T, [&] {
+    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
+    return csr_spmm<T>(d, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
+  });
+}
+
+int hmc_srcloc3d_misfit(int dtype, int64_t E, int64_t S, int64_t C, const void* M, const void* rx, const void* ry,
+                        const void* rz, const void* obs, const void* inv_var, int infer_velocity,
+                        double medium_velocity, double* out_x, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return srcloc<T>(false, E, S, C, M, rx, ry, rz, obs, inv_var, infer_velocity, medium_velocity, out_x, nullptr,
+                     accumulate, as_stream(stream));
+  });
+}
+
+int hmc_srcloc3d_gradient(int dtype, int64_t E, int64_t S, int64_t C, const void* M, const void* rx, const void* ry,
+                          const void* rz, const void* obs, const void* inv_var, int infer_velocity,
+                          double medium_velocity, void* out_g, int accumulate, void* stream) {
+  return HMC_DISPATCH(dtype, T, [&] {
+    return srcloc<T>(true, E, S, C, M, rx, ry, rz, obs, inv_var, infer_velocity, medium_velocity, nullptr, out_g,
+                     accumulate, as_stream(stream));
+  });
+}
+
+}  // extern "C"

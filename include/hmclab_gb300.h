@@ -1,0 +1,272 @@
+/*
+ * hmclab_gb300 — C ABI of the GB300 Hamiltonian Monte Carlo hot path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as `void*`, NULL = legacy default stream) and returns an int status
+ * (HMC_OK = 0).  No C++ exceptions and no framework types cross this boundary;
+ * the library never frees or retains caller memory.  `hmc_last_error()` returns
+ * a human-readable message for the last failing call on the calling thread.
+ *
+ * Layout convention: a batch of C chains of a d-dimensional model is stored
+ * dimension-major, chain-fastest: element (i, c) of a [d][C] array lives at
+ * offset i*C + c.  A single reference-style column vector (d,1) is the C = 1
+ * case.  Per-chain scalars (misfits, energies, step sizes) are [C] arrays.
+ *
+ * dtype codes select the arithmetic type of positions, momenta and gradients:
+ * HMC_F32 (production) or HMC_F64 (verification).  Hamiltonian sums, misfits
+ * and the accept test are always FP64.
+ *
+ * Reference interfaces each group replaces are cited per declaration as
+ * file:line in the reference project (larsgeb/hmclab).
+ */
+#ifndef HMCLAB_GB300_H
+#define HMCLAB_GB300_H
+
+#include <stdint.h>
+
+#if defined(HMC_BUILDING_LIBRARY) && defined(__GNUC__)
+#define HMC_API __attribute__((visibility("default")))
+#else
+#define HMC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define HMC_OK 0
+#define HMC_ERR_INVALID_ARG 1 /* maps to AssertionError/ValueError host-side */
+#define HMC_ERR_CUDA 2        /* CUDA runtime error (launch or execution)    */
+#define HMC_ERR_TIMEOUT 3     /* a bounded device wait ran out               */
+#define HMC_ERR_NONFINITE 4   /* non-finite state where it is not allowed    */
+#define HMC_ERR_UNSUPPORTED 5 /* valid request this build does not provide   */
+
+#define HMC_F32 0
+#define HMC_F64 1
+
+#define HMC_MASS_UNIT 0
+#define HMC_MASS_DIAG 1
+#define HMC_MASS_FULL 2
+
+/* per-chain flag bits in hmc_chains.flags */
+#define HMC_FLAG_OUT_OF_BOUNDS 1 /* trajectory left the bounds: misfit = +inf */
+
+/* ---- library ------------------------------------------------------------- */
+HMC_API int hmc_version(void);
+HMC_API const char* hmc_last_error(void);
+/* Number of kernels this library has launched since load (host-side counter). */
+HMC_API int64_t hmc_launch_count(void);
+
+/* ---- counter-based RNG (Philox4x32-10, Salmon et al. 2011) ---------------
+ * Replaces the numpy Generator draws of MassMatrices.py:142,227,314 and
+ * Samplers.py:1534,1486 in production mode.  out[i][c] = standard normal for
+ * counter (i/4, c, proposal, purpose) under key = seed.                      */
+HMC_API int hmc_philox_normal(int dtype, int64_t rows, int64_t chains, uint64_t seed,
+                      uint64_t proposal, uint32_t purpose, void* out,
+                      void* stream);
+/* Raw Philox4x32-10 blocks for known-answer tests: n blocks, block k uses
+ * counter (ctr0 + k, ctr1, ctr2, ctr3) and key (key0, key1); out is uint32[4n]
+ * in device memory. */
+HMC_API int hmc_philox_raw(int64_t n, uint32_t ctr0, uint32_t ctr1, uint32_t ctr2,
+                   uint32_t ctr3, uint32_t key0, uint32_t key1, uint32_t* out,
+                   void* stream);
+
+/* ---- batched chain state of the sampler ----------------------------------
+ * Mirrors the per-chain state HMC keeps in Samplers.py:1105-1180
+ * (current_model, current_x, current_momentum, stepsize, accepted_proposals)
+ * for C chains at once.  All pointers are device memory unless noted.       */
+typedef struct hmc_chains {
+  int32_t dtype;     /* HMC_F32 / HMC_F64: type of q_cur, q, p, g, v, eps, ring_q */
+  int32_t mass_kind; /* HMC_MASS_* */
+  int64_t dims;      /* d */
+  int64_t chains;    /* C */
+  void* q_cur;       /* [d][C] current model of every chain            */
+  void* q;           /* [d][C] position along the trajectory           */
+  void* p;           /* [d][C] momentum                                */
+  void* g;           /* [d][C] gradient of the misfit at q (scratch)   */
+  void* v;           /* [d][C] scratch for full-mass products (FULL)   */
+  const void* mass_diag;     /* [d] diagonal of M (DIAG)               */
+  const void* mass_inv_diag; /* [d] 1/diagonal (DIAG)                  */
+  const void* mass_chol;     /* [d][d] lower Cholesky factor of M (FULL) */
+  const void* mass_inv;      /* [d][d] M^-1 (FULL)                     */
+  const void* lower;         /* [d] lower bounds or NULL               */
+  const void* upper;         /* [d] upper bounds or NULL               */
+  void* eps;                 /* [C] base step size per chain           */
+  void* eps_local;           /* [C] step size of this trajectory       */
+  double* x_cur;             /* [C] misfit of q_cur                    */
+  double* x_prop;            /* [C] misfit at the trajectory end       */
+  double* k_cur;             /* [C] kinetic energy at the start        */
+  double* k_prop;            /* [C] kinetic energy at the end          */
+  int64_t* accepted;         /* [C] accepted proposals                 */
+  int32_t* flags;            /* [C] HMC_FLAG_* of the current trajectory */
+  int64_t* proposal;         /* [1] proposals completed (device counter) */
+  uint64_t seed;             /* Philox key                             */
+  int32_t randomize_stepsize;/* eps_local = U(0.5,1.5) * eps if nonzero */
+  int32_t autotune;          /* per-chain Robbins-Monro step adaptation */
+  double target_acceptance;  /* autotune target (Samplers.py:1494-1522) */
+  double learning_rate;      /* autotune exponent kappa                */
+  double minimal_stepsize;   /* autotune floor                         */
+  /* Injected random streams (parity mode); NULL selects Philox.
+   * stream_z [S][d][C] standard normals, stream_eps [S][C] step factors
+   * (already in [0.5,1.5)), stream_u [S][C] accept uniforms; proposal n uses
+   * slice n % S.                                                            */
+  const void* stream_z;
+  const void* stream_eps;
+  const double* stream_u;
+  int64_t stream_len;
+  /* Thinned sample ring: proposal n with n % thinning == 0 is written to slot
+   * (n / thinning) % ring_slots as ring_q[slot][d][C], ring_x[slot][C].
+   * ring_q may be NULL to disable recording.                               */
+  void* ring_q;
+  double* ring_x;
+  int64_t ring_slots;
+  int64_t thinning;
+  /* Optional per-proposal records for autotuning: [S][C] step sizes and
+   * acceptance rates min(1, exp(H0-H1)); NULL to skip.                     */
+  double* rec_stepsize;
+  double* rec_acceptance;
+  int64_t rec_len;
+} hmc_chains;
+
+/* Samplers.py:1463-1469 + 1524-1545 (and MassMatrices.py:100-314):
+ * draw momenta p ~ N(0, M), step factors, kinetic energy K(p) in FP64,
+ * copy q_cur -> q and make the first drift q += drift * eps_local * M^-1 p,
+ * then apply the bound reflection of base.py:239-270.  drift is 0.5 for the
+ * leapfrog integrator and a1 for the 3-/4-stage integrators (Samplers.py:
+ * 1586-1726).                                                               */
+HMC_API int hmc_begin_trajectory(const hmc_chains* s, double drift, void* stream);
+
+/* Samplers.py:1561-1569: p -= kick * eps_local * g, then
+ * q += drift * eps_local * M^-1 p, then reflect at the bounds.  drift = 0
+ * skips the position update.                                               */
+HMC_API int hmc_kick_drift(const hmc_chains* s, double kick, double drift,
+                   void* stream);
+
+/* Samplers.py:1471-1492 (+ autotune 1494-1522 and the thinned append of
+ * 529-704 lines 675-678): K(p) at the end, H = x + K for both states, accept
+ * iff exp(H0 - H1) > u with FP64 arithmetic (NaN rejects), copy q -> q_cur
+ * on accept, count, optionally adapt eps, record the thinned sample and
+ * advance the proposal counter.  x_prop must hold misfit(q).               */
+HMC_API int hmc_end_trajectory(const hmc_chains* s, void* stream);
+
+/* MassMatrices.py:100-113,185-198,270-285: out[c] = 0.5 p_c^T M^-1 p_c (FP64).
+ * For FULL, s->v is used as scratch.                                       */
+HMC_API int hmc_kinetic_energy(const hmc_chains* s, const void* p, double* out,
+                       void* stream);
+/* MassMatrices.py:115-133,200-218,287-305: out = M^-1 p.                   */
+HMC_API int hmc_kinetic_energy_gradient(const hmc_chains* s, const void* p, void* out,
+                                void* stream);
+
+/* ---- target distributions: batched misfit / gradient ---------------------
+ * misfit: out_x[c] (+)= chi(M[:,c]) in FP64 (accumulate != 0 adds).
+ * gradient: out_g[i][c] (+)= d chi / d m_i at M[:,c].                       */
+
+/* base.py:539-574 (Normal, diagonal covariance):
+ * chi = 0.5 sum (m - mean)^2 * inv_var, grad = (m - mean) * inv_var.        */
+HMC_API int hmc_normal_diag_misfit(int dtype, int64_t d, int64_t C, const void* M,
+                           const void* mean, const void* inv_var,
+                           double* out_x, int accumulate, void* stream);
+HMC_API int hmc_normal_diag_gradient(int dtype, int64_t d, int64_t C, const void* M,
+                             const void* mean, const void* inv_var,
+                             void* out_g, int accumulate, void* stream);
+
+/* base.py:553-574 (Normal, full covariance): inv_cov is [d][d].  With
+ * D = m - mean: chi = 0.5 D^T inv_cov D, grad = inv_cov D.  work is a scratch
+ * buffer of 2*d*C elements (misfit) or d*C elements (gradient).             */
+HMC_API int hmc_normal_full_misfit(int dtype, int64_t d, int64_t C, const void* M,
+                           const void* mean, const void* inv_cov, void* work,
+                           double* out_x, int accumulate, void* stream);
+HMC_API int hmc_normal_full_gradient(int dtype, int64_t d, int64_t C, const void* M,
+                             const void* mean, const void* inv_cov,
+                             void* work, void* out_g, int accumulate,
+                             void* stream);
+
+/* base.py:689-710 (Laplace): chi = sum |m - mean| * inv_disp,
+ * grad = sign(m - mean) * inv_disp, sign(0) = 0.                            */
+HMC_API int hmc_laplace_misfit(int dtype, int64_t d, int64_t C, const void* M,
+                       const void* mean, const void* inv_disp, double* out_x,
+                       int accumulate, void* stream);
+HMC_API int hmc_laplace_gradient(int dtype, int64_t d, int64_t C, const void* M,
+                         const void* mean, const void* inv_disp, void* out_g,
+                         int accumulate, void* stream);
+
+/* LinearMatrix.py:184-208, premultiplied dense form (n > d):
+ * grad = GtG m - Gtd0; chi = 0.5 (m^T (GtG m - 2 Gtd0) + dtd).
+ * GtG is [d][d] row-major, Gtd0 is [d]; work is a [d][C] scratch.  This is
+ * the FP64 verification form; FP32 chains use the residual form below (the
+ * premultiplied misfit cancels catastrophically in FP32).                   */
+HMC_API int hmc_dense_premul_gradient(int dtype, int64_t d, int64_t C, const void* M,
+                              const void* GtG, const void* Gtd0, void* out_g,
+                              int accumulate, void* stream);
+HMC_API int hmc_dense_premul_misfit(int dtype, int64_t d, int64_t C, const void* M,
+                            const void* GtG, const void* Gtd0, double dtd,
+                            void* work, double* out_x, int accumulate,
+                            void* stream);
+
+/* LinearMatrix.py:193-208, residual dense form:
+ * r = (G m - data) * inv_var (n x C), chi = 0.5 sum (G m - data)^2 inv_var,
+ * grad = G^T r.  G is [n][d], Gt is [d][n] (both row-major); resid is an
+ * [n][C] scratch of the state dtype.                                        */
+HMC_API int hmc_dense_resid_misfit(int dtype, int64_t n, int64_t d, int64_t C,
+                           const void* M, const void* G, const void* data,
+                           const void* inv_var, void* resid, double* out_x,
+                           int accumulate, void* stream);
+HMC_API int hmc_dense_resid_gradient(int dtype, int64_t n, int64_t d, int64_t C,
+                             const void* M, const void* G, const void* Gt,
+                             const void* data, const void* inv_var,
+                             void* resid, void* out_g, int accumulate,
+                             void* stream);
+
+/* LinearMatrix.py:389-426 (sparse G, CSR, simple covariance):
+ * G rows (n) in CSR (row_ptr[n+1], col[nnz], val[nnz] of the state dtype);
+ * Gt is G^T in CSR (d rows).  resid is an [n][C] scratch.                   */
+HMC_API int hmc_csr_misfit(int dtype, int64_t n, int64_t d, int64_t C, const void* M,
+                   const int32_t* row_ptr, const int32_t* col, const void* val,
+                   const void* data, const void* inv_var, void* resid,
+                   double* out_x, int accumulate, void* stream);
+HMC_API int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C,
+                     const void* M, const int32_t* row_ptr,
+                     const int32_t* col, const void* val,
+                     const int32_t* t_row_ptr, const int32_t* t_col,
+                     const void* t_val, const void* data,
+                     const void* inv_var, void* resid, void* out_g,
+                     int accumulate, void* stream);
+
+/* SourceLocation.py:482-540 (SourceLocation3D, homogeneous velocity).
+ * Parameters are interleaved [x,y,z,T] per event followed by v when
+ * infer_velocity != 0, else v = medium_velocity (SourceLocation.py:697-713).
+ * rx/ry/rz are [S] station coordinates; obs and inv_var are [E][S];
+ * NaN observations are skipped (nansum).                                   */
+HMC_API int hmc_srcloc3d_misfit(int dtype, int64_t E, int64_t S, int64_t C,
+                        const void* M, const void* rx, const void* ry,
+                        const void* rz, const void* obs, const void* inv_var,
+                        int infer_velocity, double medium_velocity,
+                        double* out_x, int accumulate, void* stream);
+HMC_API int hmc_srcloc3d_gradient(int dtype, int64_t E, int64_t S, int64_t C,
+                          const void* M, const void* rx, const void* ry,
+                          const void* rz, const void* obs,
+                          const void* inv_var, int infer_velocity,
+                          double medium_velocity, void* out_g, int accumulate,
+                          void* stream);
+
+/* ---- dense matrix product used by the ops above -------------------------
+ * out[m][n] = alpha * A[m][k] B[k][n] + (bias ? bias[m] : 0)
+ *             + (accumulate ? out[m][n] : 0), all row-major.                */
+HMC_API int hmc_gemm(int dtype, int64_t m, int64_t n, int64_t k, double alpha,
+             const void* A, const void* B, const void* bias, void* out,
+             int accumulate, void* stream);
+
+/* ---- CUDA graphs of whole proposals --------------------------------------
+ * Capture the work issued on `stream` between begin and end into an
+ * executable graph; launch it any number of times.                          */
+HMC_API int hmc_graph_begin(void* stream);
+HMC_API int hmc_graph_end(void* stream, void** graph_exec);
+HMC_API int hmc_graph_launch(void* graph_exec, void* stream);
+HMC_API int hmc_graph_destroy(void* graph_exec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMCLAB_GB300_H */

@@ -1,0 +1,84 @@
+"""CPU-side checks of the C ABI: the library loads, exports every function
+include/hmclab_gb300.h declares, and the ctypes mirror of `hmc_chains` has the
+C layout.  No compute call is made (no GPU here)."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from hmclab_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hmclab_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"HMC_API\s+[\w\s\*]+?\b(hmc_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not _lib.library_available():
+        from hmclab_gb300 import build
+
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "hmc_begin_trajectory" in names and "hmc_end_trajectory" in names
+    assert len(names) >= 25
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} is declared in the header but not exported"
+
+
+def test_python_signatures_cover_header():
+    assert set(declared_functions()) == set(_lib.SIGNATURES), (
+        "ctypes signatures and header declarations differ: "
+        f"{set(declared_functions()) ^ set(_lib.SIGNATURES)}"
+    )
+
+
+def test_version_and_error_string_without_gpu(lib):
+    assert lib.hmc_version() == 1
+    assert isinstance(lib.hmc_last_error(), bytes)
+
+
+def test_invalid_arguments_fail_before_any_launch(lib):
+    # Null state: rejected on the host, no CUDA call is made.
+    rc = lib.hmc_begin_trajectory(None, 0.5, None)
+    assert rc == _lib.HMC_ERR_INVALID_ARG
+    assert b"null state" in lib.hmc_last_error()
+    with pytest.raises(ValueError):
+        _lib.check(rc, "hmc_begin_trajectory")
+    st = _lib.HmcChains()
+    st.dtype = 7
+    rc = lib.hmc_end_trajectory(ctypes.byref(st), None)
+    assert rc == _lib.HMC_ERR_INVALID_ARG
+
+
+def test_chains_struct_layout_matches_c(tmp_path):
+    """Compile a probe with gcc that prints sizeof/offsetof of hmc_chains and
+    compare with the ctypes Structure."""
+    fields = [f for f, _ in _lib.HmcChains._fields_]
+    src = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){",
+           'printf("%zu\\n", sizeof(hmc_chains));']
+    for f in fields:
+        src.append(f'printf("%zu\\n", offsetof(hmc_chains, {f}));')
+    src.append("return 0;}")
+    c = tmp_path / "probe.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-o", str(exe), str(c)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(_lib.HmcChains)
+    for f, off in zip(fields, out[1:]):
+        assert getattr(_lib.HmcChains, f).offset == off, f

@@ -1,0 +1,150 @@
+"""Host-side logic that needs no GPU: argument validation with the reference's
+exception classes, integrator schedules, samples files, synthetic problems,
+and the loud failure when no device is present."""
+import os
+
+import numpy as np
+import pytest
+
+import hmclab_gb300 as H
+from hmclab_gb300 import Samplers, problems
+from hmclab_gb300.Helpers.CustomExceptions import DeviceUnavailableError
+from oracle import hmc_oracle as O
+
+torch = pytest.importorskip("torch")
+NO_GPU = not torch.cuda.is_available()
+
+
+@pytest.mark.parametrize("integrator", ["lf", "3s", "4s"])
+@pytest.mark.parametrize("L", [1, 3, 10])
+def test_integrator_ops_match_oracle(integrator, L):
+    assert Samplers.integrator_ops(integrator, L) == O.integrator_schedule(integrator, L)
+
+
+def test_schedule_compiles_to_fused_kick_drift():
+    first, steps = Samplers.compile_schedule(Samplers.integrator_ops("lf", 4))
+    assert first == 0.5
+    assert steps == [(True, 1.0, 1.0)] * 3 + [(True, 1.0, 0.5)]
+    first, steps = Samplers.compile_schedule(Samplers.integrator_ops("3s", 2))
+    # 3 kicks per stage, a bare drift where two stages meet
+    assert sum(s[0] for s in steps) == 6
+    assert sum(1 for s in steps if not s[0]) == 1
+
+
+def test_unknown_integrator_raises_value_error():
+    with pytest.raises(ValueError):
+        Samplers.integrator_ops("rk4", 3)
+
+
+def _normal(d=3):
+    return H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1)))
+
+
+@pytest.mark.parametrize(
+    "kwargs,exc",
+    [
+        (dict(proposals=0), AssertionError),
+        (dict(proposals=10, online_thinning=3), AssertionError),
+        (dict(stepsize=-1.0), AssertionError),
+        (dict(amount_of_steps=2.5), AssertionError),
+        (dict(integrator="xx"), ValueError),
+        (dict(mass_matrix=H.MassMatrices.Unit(5)), AssertionError),
+        (dict(autotuning=True, learning_rate=0.3), AssertionError),
+        (dict(initial_model=np.zeros((4, 1))), AssertionError),
+        (dict(max_time=-1.0), AssertionError),
+    ],
+)
+def test_sampler_argument_validation(kwargs, exc):
+    """Invalid arguments are rejected before any device work, with the
+    reference's exception types (Samplers.py:347-441, 1335-1384)."""
+    base = dict(proposals=10)
+    base.update(kwargs)
+    with pytest.raises(exc):
+        Samplers.HMC(seed=1)._parse(
+            None, _normal(), base.get("stepsize", 0.1), True, base.get("amount_of_steps", 10),
+            base.get("mass_matrix"), base.get("integrator", "lf"), base.get("initial_model"), base["proposals"],
+            base.get("online_thinning", 1), False, False, base.get("max_time"), base.get("autotuning", False),
+            0.65, base.get("learning_rate", 0.75), None, None, None, True, None, False,
+        )
+
+
+@pytest.mark.skipif(not NO_GPU, reason="checks the no-device behaviour")
+def test_device_calls_fail_loudly_without_gpu():
+    with pytest.raises(DeviceUnavailableError):
+        _normal().misfit(np.zeros((3, 1)))
+    with pytest.raises(DeviceUnavailableError):
+        H.Samplers.HMC(seed=0).sample(None, _normal(), proposals=2)
+
+
+def test_distribution_bounds_validation():
+    d = _normal(2)
+    with pytest.raises(ValueError):
+        d.update_bounds(lower=np.zeros((3, 1)))
+    with pytest.raises(ValueError):
+        d.update_bounds(lower=np.ones((2, 1)), upper=np.zeros((2, 1)))
+    d.update_bounds(lower=-np.ones((2, 1)), upper=np.ones((2, 1)))
+    assert d.misfit_bounds(np.zeros((2, 1))) == 0.0
+    assert d.misfit_bounds(np.full((2, 1), 2.0)) == np.inf
+    q, p = np.array([[-1.5], [0.5]]), np.ones((2, 1))
+    d.corrector(q, p)
+    assert np.allclose(q, [[-0.5], [0.5]]) and np.allclose(p, [[-1.0], [1.0]])
+
+
+def test_bayes_rule_collapses_bounds():
+    a = H.Distributions.Normal(np.zeros((2, 1)), np.ones((2, 1)), lower_bounds=np.array([[-1.0], [-2.0]]))
+    b = H.Distributions.Laplace(np.zeros((2, 1)), np.ones((2, 1)), lower_bounds=np.array([[-3.0], [-1.0]]),
+                                upper_bounds=np.array([[4.0], [5.0]]))
+    post = H.Distributions.BayesRule([a, b])
+    assert np.array_equal(post.lower_bounds, [[-1.0], [-1.0]])
+    assert np.array_equal(post.upper_bounds, [[4.0], [5.0]])
+
+
+def test_linear_matrix_reproduces_reference_quirks(golden):
+    g = golden("linearmatrix_public.npz")
+    lik = H.Distributions.LinearMatrix(g["G"].copy(), g["d"].copy(), float(g["var"]))
+    assert lik.premultiplication
+    M = g["probe_m"]
+    mis = 0.5 * (np.sum(M * (lik.GtG @ M - 2 * lik.Gtd0), axis=0) + lik.dtd)
+    np.testing.assert_allclose(mis, g["probe_misfit"], rtol=1e-12)
+    np.testing.assert_allclose(lik.GtG @ M - lik.Gtd0, g["probe_grad"], rtol=1e-12, atol=1e-9)
+
+
+def test_samples_file_roundtrip(tmp_path):
+    fn = str(tmp_path / "s.npy")
+    w = H.Samples(fn, mode="w")
+    a = np.arange(12.0).reshape(4, 3)
+    w.append_columns(a)
+    w.append_columns(a + 100)
+    w.write_attribute("proposals", 6)
+    w.close()
+    arr = np.load(fn)
+    assert arr.shape == (6, 4)  # rows are samples, like the reference's file
+    with H.Samples(fn) as r:
+        assert r.numpy.shape == (4, 6)
+        np.testing.assert_array_equal(r.numpy[:, :3], a)
+        assert r.read_attribute("write_index") == 6
+    with pytest.raises(FileExistsError):
+        H.Samples(fn, mode="w")
+    H.Samples(fn, mode="w", overwrite=True).close()
+
+
+def test_siddon_lengths_sum_to_segment_length():
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        x0, y0, x1, y1 = rng.uniform(0, 16, size=4)
+        idx, lens = problems.ray_cell_lengths(x0, y0, x1, y1, 16, 16, 1.0)
+        assert np.isclose(lens.sum(), np.hypot(x1 - x0, y1 - y0), rtol=1e-12)
+        assert len(np.unique(idx)) == len(idx)
+    # axis-aligned ray along a grid line interior
+    idx, lens = problems.ray_cell_lengths(0.0, 2.5, 16.0, 2.5, 16, 16, 1.0)
+    assert len(idx) == 16 and np.allclose(lens, 1.0)
+
+
+def test_tomography_problem_shape():
+    t = problems.tomography(nx=32, ny=32, n_rays=200, seed=1)
+    G = t["G"]
+    assert G.shape == (200, 1024)
+    nnz = np.diff(G.indptr)
+    assert nnz.min() > 0 and 20 < nnz.mean() < 64 * 2
+    bg = t["background"]
+    assert bg.min() >= 0.2 - 1e-12 and bg.max() <= 0.5 + 1e-12
