@@ -141,13 +141,15 @@ class HMC:
         Raises AssertionError / ValueError / TypeError / FileExistsError for
         invalid arguments like the reference."""
         self.disable_progressbar = disable_progressbar
-        self._parse(
-            samples_filename, distribution, stepsize, randomize_stepsize, amount_of_steps, mass_matrix, integrator,
-            initial_model, proposals, online_thinning, diagnostic_mode, overwrite_existing_file, max_time, autotuning,
-            target_acceptance_rate, learning_rate, chains, dtype, rng_streams, graph, proposals_per_graph, keep_samples,
+        self.prepare(
+            samples_filename, distribution, stepsize=stepsize, randomize_stepsize=randomize_stepsize,
+            amount_of_steps=amount_of_steps, mass_matrix=mass_matrix, integrator=integrator,
+            initial_model=initial_model, proposals=proposals, online_thinning=online_thinning,
+            diagnostic_mode=diagnostic_mode, overwrite_existing_file=overwrite_existing_file, max_time=max_time,
+            autotuning=autotuning, target_acceptance_rate=target_acceptance_rate, learning_rate=learning_rate,
+            chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
+            keep_samples=keep_samples,
         )
-        self._setup_device()
-        self._open_files()
         self._run()
         return self
 
@@ -438,36 +440,83 @@ class HMC:
         for c, w in enumerate(self._writers):
             w.append_columns(_numpy.vstack([q[:, :, c].T, x[None, :, c]]))
 
-    def _run(self):
+    # ---- lower-level driving API (used by sample() and by benchmarks) ------
+    def prepare(self, samples_filename, distribution, **kwargs):
+        """Validate arguments, allocate the device state and open the files
+        without running any proposal.  Takes the keyword arguments of sample()."""
+        defaults = dict(
+            stepsize=0.1, randomize_stepsize=True, amount_of_steps=10, mass_matrix=None, integrator="lf",
+            initial_model=None, proposals=100, online_thinning=1, diagnostic_mode=False, overwrite_existing_file=False,
+            max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
+            dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
+        )
+        unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
+        if unknown:
+            raise TypeError(f"Unidentified argument(s) not applicable to sampler: {unknown}")
+        defaults.update({k: v for k, v in kwargs.items() if k in defaults})
+        a = defaults
+        self._parse(
+            samples_filename, distribution, a["stepsize"], a["randomize_stepsize"], a["amount_of_steps"],
+            a["mass_matrix"], a["integrator"], a["initial_model"], a["proposals"], a["online_thinning"],
+            a["diagnostic_mode"], a["overwrite_existing_file"], a["max_time"], a["autotuning"],
+            a["target_acceptance_rate"], a["learning_rate"], a["chains"], a["dtype"], a["rng_streams"], a["graph"],
+            a["proposals_per_graph"], a["keep_samples"],
+        )
+        self._setup_device()
+        self._open_files()
+        self._done = 0
+        self._t0 = _time.time()
+        self._start_time = _datetime.now()
+        self._launches0 = _lib.launch_count()
+        return self
+
+    def run(self, n_proposals):
+        """Enqueue the next `n_proposals` proposals (whole graph blocks where
+        possible) on the sampler's stream; returns the number issued.  Does not
+        synchronise unless samples are drained to files."""
         h = self.stream.cuda_stream
         k = self.proposals_per_graph
-        P = self.proposals
-        self._start_time = _datetime.now()
-        t0 = _time.time()
-        deadline = t0 + self.max_time if self.max_time is not None else None
-        done = 0
-        n_blocks_timed = 0
-        launches0 = _lib.launch_count()
+        target = min(self.proposals, self._done + int(n_proposals))
+        issued = 0
+        while self._done < target:
+            n = min(k, target - self._done)
+            self._load_streams(self._done, n)
+            if self.use_graph and n == k:
+                if self._graph is None:
+                    _lib.call("hmc_graph_begin", h)
+                    try:
+                        self._issue_block(k, h)
+                    finally:
+                        exec_ptr = _ct.c_void_p()
+                        rc = _lib.load().hmc_graph_end(h, _ct.byref(exec_ptr))
+                    _lib.check(rc, "hmc_graph_end")
+                    self._graph = exec_ptr
+                _lib.call("hmc_graph_launch", self._graph, h)
+            else:
+                self._issue_block(n, h)
+            self._drain(self._done, n)
+            self._done += n
+            issued += n
+        return issued
+
+    def finish(self):
+        """Synchronise, release the graph, write attributes and close files."""
+        self.stream.synchronize()
+        self._end_time = _datetime.now()
+        self.runtime_seconds = _time.time() - self._t0
+        self.kernel_launches = _lib.launch_count() - self._launches0
+        self.proposals_done = self._done
+        if self._graph is not None:
+            _lib.call("hmc_graph_destroy", self._graph)
+            self._graph = None
+        self._finalise(self._done)
+        return self
+
+    def _run(self):
+        deadline = self._t0 + self.max_time if self.max_time is not None else None
         try:
-            while done < P:
-                n = min(k, P - done)
-                self._load_streams(done, n)
-                if self.use_graph and n == k:
-                    if self._graph is None:
-                        _lib.call("hmc_graph_begin", h)
-                        try:
-                            self._issue_block(k, h)
-                        finally:
-                            exec_ptr = _ct.c_void_p()
-                            rc = _lib.load().hmc_graph_end(h, _ct.byref(exec_ptr))
-                        _lib.check(rc, "hmc_graph_end")
-                        self._graph = exec_ptr
-                    _lib.call("hmc_graph_launch", self._graph, h)
-                else:
-                    self._issue_block(n, h)
-                self._drain(done, n)
-                done += n
-                n_blocks_timed += 1
+            while self._done < self.proposals:
+                self.run(self.proposals_per_graph)
                 if deadline is not None and _time.time() > deadline:
                     self.stream.synchronize()
                     raise TimeoutError
@@ -476,15 +525,7 @@ class HMC:
         except KeyboardInterrupt:
             pass
         finally:
-            self.stream.synchronize()
-            self._end_time = _datetime.now()
-            self.runtime_seconds = _time.time() - t0
-            self.kernel_launches = _lib.launch_count() - launches0
-            self.proposals_done = done
-            if self._graph is not None:
-                _lib.call("hmc_graph_destroy", self._graph)
-                self._graph = None
-            self._finalise(done)
+            self.finish()
 
     def _finalise(self, done):
         C = self.chains
@@ -530,6 +571,19 @@ class HMC:
         x = x.cpu().numpy()  # N, C
         full = _numpy.concatenate([_numpy.transpose(q, (2, 1, 0)), x.T[:, None, :]], axis=1)
         return full if chain is None else full[chain]
+
+    def samples_host(self):
+        """Samples kept on the device, copied to host memory in the device
+        layout: q [N][d][C] (state dtype) and misfits x [N][C] (float64)."""
+        assert self.samples_device is not None, "sample(..., keep_samples=True) keeps samples on the device"
+        q, x = self.samples_device
+        hq = _torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
+        hx = _torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+        with _torch.cuda.stream(self.stream):
+            hq.copy_(q, non_blocking=True)
+            hx.copy_(x, non_blocking=True)
+        self.stream.synchronize()
+        return hq.numpy(), hx.numpy()
 
     def load_results(self, burn_in: int = 0, chain: int = 0):
         assert burn_in >= 0

@@ -46,7 +46,7 @@ def normalise_dtype(dtype):
 def upload(array, dtype, device=None):
     """Copy a numpy array (any float type) to a contiguous device tensor."""
     device = device or require_cuda()
-    a = _np.ascontiguousarray(_np.asarray(array, dtype=_np.float64))
+    a = _np.array(array, dtype=_np.float64, order="C", copy=True)
     return _torch.from_numpy(a).to(device=device, dtype=torch_dtype(dtype)).contiguous()
 
 

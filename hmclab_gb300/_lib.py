@@ -120,12 +120,15 @@ SIGNATURES = {
     "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
+    "hmc_ess": [I, I64, I64, I64, P, I, P, P, P, S],
+    "hmc_ess_work_size": [I64, I64, I],
+    "hmc_moments": [I, I64, I64, I64, P, P, P, S],
     "hmc_graph_begin": [S],
     "hmc_graph_end": [S, _ct.POINTER(c_void_p)],
     "hmc_graph_launch": [P, S],
     "hmc_graph_destroy": [P],
 }
-_RESTYPES = {"hmc_last_error": c_char_p, "hmc_launch_count": c_int64}
+_RESTYPES = {"hmc_last_error": c_char_p, "hmc_launch_count": c_int64, "hmc_ess_work_size": c_int64}
 
 _lock = _threading.Lock()
 _lib = None

@@ -257,6 +257,23 @@ HMC_API int hmc_gemm(int dtype, int64_t m, int64_t n, int64_t k, double alpha,
              const void* A, const void* B, const void* bias, void* out,
              int accumulate, void* stream);
 
+/* ---- effective sample size (no counterpart in the reference, whose only
+ * mixing diagnostic is Helpers/Processing.py:6-13) --------------------------
+ * Split-chain multi-chain ESS per parameter with Geyer's initial monotone
+ * sequence (Gelman et al., BDA3 section 11.5): samples are [N][d][C] (the
+ * sampler's thinned ring), lags bounds the autocorrelation window; ess[d]
+ * is negated where the window was too short to truncate; rhat[d] (nullable)
+ * receives split-R-hat.  work holds hmc_ess_work_size(d, C, lags) doubles.  */
+HMC_API int hmc_ess(int dtype, int64_t N, int64_t d, int64_t C,
+                    const void* samples, int lags, double* work, double* ess,
+                    double* rhat, void* stream);
+HMC_API int64_t hmc_ess_work_size(int64_t d, int64_t C, int lags);
+/* Mean and (population) variance over all draws and chains of every
+ * parameter of an [N][d][C] sample array, in FP64.                          */
+HMC_API int hmc_moments(int dtype, int64_t N, int64_t d, int64_t C,
+                        const void* samples, double* mean, double* var,
+                        void* stream);
+
 /* ---- CUDA graphs of whole proposals --------------------------------------
  * Capture the work issued on `stream` between begin and end into an
  * executable graph; launch it any number of times.                          */

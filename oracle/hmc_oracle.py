@@ -450,3 +450,48 @@ def run_chains(
         res["stepsizes"] = np.array(stepsizes)
         res["acceptance_rates"] = np.array(rates)
     return res
+
+
+# ---------------------------------------------------------------------------
+# Effective sample size (the reference has none; BDA3 section 11.5 split-chain
+# multi-chain estimator with Geyer's initial monotone sequence).
+# ---------------------------------------------------------------------------
+def ess_split(x, lags):
+    """x: [N][d][C] samples.  Returns (ess[d], rhat[d]); ess is negated where
+    the lag window was too short to truncate (same convention as hmc_ess)."""
+    N, d, C = x.shape
+    n = N // 2
+    h = np.concatenate([x[:n], x[n : 2 * n]], axis=2)  # n, d, M
+    M = 2 * C
+    mu_m = h.mean(axis=0)  # d, M
+    var_m = h.var(axis=0, ddof=1)
+    W = var_m.mean(axis=1)
+    mu = mu_m.mean(axis=1)
+    B = n / (M - 1) * np.sum((mu_m - mu[:, None]) ** 2, axis=1)
+    varp = (n - 1) / n * W + B / n
+    hc = h - mu_m[None]
+    out = np.empty(d)
+    for i in range(d):
+        def rho(t):
+            g = np.sum(hc[: n - t, i] * hc[t:, i], axis=0) / n  # M
+            return 1.0 - (W[i] - g.mean()) / varp[i]
+
+        s, prev, trunc = 0.0, np.inf, False
+        t = 0
+        while t + 1 < lags:
+            P = rho(t) + rho(t + 1)
+            if P < 0:
+                trunc = True
+                break
+            P = min(P, prev)
+            prev = P
+            s += P
+            t += 2
+        e = M * n / (-1.0 + 2.0 * s)
+        out[i] = e if trunc else -e
+    return out, np.sqrt(varp / W)
+
+
+def ar1_ess(phi, n_total):
+    """Asymptotic ESS of a stationary AR(1) chain: N (1 - phi) / (1 + phi)."""
+    return n_total * (1 - phi) / (1 + phi)
