@@ -22,7 +22,7 @@ def test_oracle_ess_matches_ar1_theory():
     e, rhat = O.ess_split(x, 100)
     ref = O.ar1_ess(np.array(phi), 400 * 64)
     np.testing.assert_allclose(np.abs(e), ref, rtol=0.15)
-    assert np.all(np.abs(rhat - 1) < 0.02)
+    assert np.all(np.abs(rhat - 1) < 0.06)
 
 
 def test_oracle_ess_detects_unmixed_chains():
