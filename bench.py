@@ -330,8 +330,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="dense", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-chains", type=int, default=32)
-    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--cpu-chains", type=int, default=64)
+    ap.add_argument("--cpu-steps", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     assert args.warmup >= 3, "at least 3 warm-up steps"

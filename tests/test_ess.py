@@ -40,7 +40,8 @@ def test_device_ess_and_moments_match_oracle():
     from hmclab_gb300 import diagnostics
 
     x = ar1(300, 5, 96, [0.0, 0.3, 0.6, 0.9, -0.4], seed=3)
-    for dtype, tol in ((torch.float64, 1e-9), (torch.float32, 1e-4)):
+    # the kernel stages draws in FP32 shared memory: 1e-6 relative for FP64 input
+    for dtype, tol in ((torch.float64, 1e-6), (torch.float32, 1e-4)):
         t = torch.from_numpy(x).to("cuda", dtype)
         e, rh = diagnostics.ess(t, lags=80, return_rhat=True)
         xr = t.double().cpu().numpy()
