@@ -115,6 +115,7 @@ SIGNATURES = {
     "hmc_dense_premul_misfit": [I, I64, I64, P, P, P, D, P, P, I, S],
     "hmc_dense_resid_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, S],
     "hmc_dense_resid_gradient": [I, I64, I64, I64, P, P, P, P, P, P, P, I, S],
+    "hmc_dense_resid_misfit_noalloc": [I, I64, I64, I64, P, P, P, P, P, I, S],
     "hmc_csr_misfit": [I, I64, I64, I64, P, P, P, P, P, P, P, P, I, S],
     "hmc_csr_gradient": [I, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, I, S],
     "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],

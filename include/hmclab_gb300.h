@@ -218,6 +218,22 @@ HMC_API int hmc_dense_resid_gradient(int dtype, int64_t n, int64_t d, int64_t C,
                              void* resid, void* out_g, int accumulate,
                              void* stream);
 
+/* No counterpart in the reference.  hmc_dense_resid_misfit for callers that
+ * cannot allocate device memory (their host framework owns every device
+ * allocation, or cudaMalloc would stall a latency-critical path): the [n][C]
+ * residual lives in a library-owned device array of
+ * HMC_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library until
+ * exit.  Larger n*C is rejected with HMC_ERR_INVALID_ARG.  No allocation is
+ * made; the array's address is looked up on each device's first call (make
+ * that call before any stream capture).  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised.                           */
+#define HMC_NOALLOC_SCRATCH_BYTES (16u << 20)
+HMC_API int hmc_dense_resid_misfit_noalloc(int dtype, int64_t n, int64_t d,
+                                           int64_t C, const void* M,
+                                           const void* G, const void* data,
+                                           const void* inv_var, double* out_x,
+                                           int accumulate, void* stream);
+
 /* LinearMatrix.py:389-426 (sparse G, CSR, simple covariance):
  * G rows (n) in CSR (row_ptr[n+1], col[nnz], val[nnz] of the state dtype);
  * Gt is G^T in CSR (d rows).  resid is an [n][C] scratch.                   */
