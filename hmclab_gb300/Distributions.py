@@ -490,10 +490,28 @@ class LinearMatrix(_AbstractDistribution):
             p["Gtd0"] = _dev.upload(self.Gtd0[:, 0], dtype)
         return p
 
+    def _tc_operands(self, C, device):
+        """BF16 hi/lo operands of the tensor-core path for a batch of C chains."""
+        from hmclab_gb300 import _dense_tc
+
+        cache = self.__dict__.setdefault("_scratch_cache", {})
+        key = ("tc", int(C))
+        if key not in cache:
+            cache[key] = _dense_tc.DenseOperands(self, C, device)
+        return cache[key]
+
+    def _use_tc(self, dtype, C):
+        from hmclab_gb300 import _dense_tc
+
+        return dtype == "float32" and _dense_tc.usable(self, C)
+
     def _device_misfit(self, M, out, accumulate, dtype, stream):
         p = self._params(dtype)
         d, C = M.shape
         code = _dev.dtype_code(dtype)
+        if self._use_tc(dtype, C):
+            self._tc_operands(C, M.device).misfit(M, out, accumulate, stream)
+            return
         if self.premultiplication and dtype == "float64":
             work = self._scratch("work", (d, C), dtype, M.device)
             _lib.call("hmc_dense_premul_misfit", code, d, C, M.data_ptr(), p["GtG"].data_ptr(), p["Gtd0"].data_ptr(),
@@ -512,6 +530,9 @@ class LinearMatrix(_AbstractDistribution):
         p = self._params(dtype)
         d, C = M.shape
         code = _dev.dtype_code(dtype)
+        if self.premultiplication and self._use_tc(dtype, C):
+            self._tc_operands(C, M.device).gradient(M, out, accumulate, stream)
+            return
         if self.premultiplication:
             _lib.call("hmc_dense_premul_gradient", code, d, C, M.data_ptr(), p["GtG"].data_ptr(),
                       p["Gtd0"].data_ptr(), out.data_ptr(), int(accumulate), stream)

@@ -386,6 +386,9 @@ class HMC:
         assert not _numpy.any(_numpy.isinf(x0)), "Initial position in model space gives inf/-inf probability"
         self.current_x = x0[0] if C == 1 else x0
         self._graph = None
+        from hmclab_gb300._dense_tc import FusedDenseStep
+
+        self._fused = FusedDenseStep.applies(self)
 
     # ------------------------------------------------------------------
     def _issue_proposal(self, h):
@@ -393,6 +396,18 @@ class HMC:
         st, dist, dt = self._state_ref, self.distribution, self.dtype
         first, steps = self._schedule
         _lib.call("hmc_begin_trajectory", st, first, h)
+        fused = self._fused
+        if fused is not None:
+            # gradient + prior + kick + drift in the tensor-core epilogue
+            fused.after_begin(h)
+            for needs_grad, kick, drift in steps:
+                if needs_grad:
+                    fused.kick_drift(kick, drift, h)
+                else:
+                    fused.drift_only(drift, h)
+            fused.misfit(h)
+            _lib.call("hmc_end_trajectory", st, h)
+            return
         for needs_grad, kick, drift in steps:
             if needs_grad:
                 dist._device_gradient(self.q, self.g, False, dt, h)
@@ -509,6 +524,8 @@ class HMC:
         if self._graph is not None:
             _lib.call("hmc_graph_destroy", self._graph)
             self._graph = None
+        if self._fused is not None:
+            self._fused.ops.check_status()
         self._finalise(self._done)
         return self
 

@@ -121,6 +121,12 @@ SIGNATURES = {
     "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
+    "hmc_split_bf16": [I64, I64, P, I64, P, P, S],
+    "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],
+    "hmc_tc_gradient": [I64, I64, I64, P, P, I64, P, P, I64, P, P, I, P, S],
+    "hmc_tc_step": [P, P, P, I64, P, P, P, P, I64, P, P, I, P, P, D, D, P, S],
+    "hmc_tc_resid_misfit": [I64, I64, I64, P, P, I64, P, P, I64, P, P, P, P, I, P, S],
+    "hmc_tc_partials_size": [I64, I64],
     "hmc_ess": [I, I64, I64, I64, P, I, P, P, P, S],
     "hmc_ess_work_size": [I64, I64, I],
     "hmc_moments": [I, I64, I64, I64, P, P, P, S],
@@ -129,7 +135,12 @@ SIGNATURES = {
     "hmc_graph_launch": [P, S],
     "hmc_graph_destroy": [P],
 }
-_RESTYPES = {"hmc_last_error": c_char_p, "hmc_launch_count": c_int64, "hmc_ess_work_size": c_int64}
+_RESTYPES = {
+    "hmc_last_error": c_char_p,
+    "hmc_launch_count": c_int64,
+    "hmc_ess_work_size": c_int64,
+    "hmc_tc_partials_size": c_int64,
+}
 
 _lock = _threading.Lock()
 _lib = None

@@ -1,0 +1,596 @@
+// Tensor-core (tcgen05) contraction of a dense matrix with all chains at once,
+// with the HMC step fused into the epilogue.
+//
+//   D[c][r] = sum_k Q[c][k] A[r][k]          (c: chain, r: matrix row, k: model index)
+//
+// computed as BF16 hi/lo split products with FP32 accumulation in TMEM:
+//   Q A ~ Qhi Ahi + Qhi Alo + Qlo Ahi,  x_hi = bf16(x), x_lo = bf16(x - x_hi).
+// A is GtG (gradient of the premultiplied dense LinearMatrix,
+// LinearMatrix.py:204-208) or G (residual misfit, LinearMatrix.py:193-202);
+// Q holds the chains' positions transposed to chain-major [C][ld] (K-major
+// operand), re-split by the epilogue of every fused step.
+//
+// Kernel structure (one 128-chain x 256-row output tile per CTA, 192 threads):
+//   warp 0  TMEM allocation; one lane issues TMA tile loads (128B swizzle)
+//   warp 1  one lane issues tcgen05.mma (M=128, N=256, K=16) and commits
+//   warps 2-5  epilogue: tcgen05.ld of the accumulator (lane = chain),
+//           then one of:
+//             EPI_GRAD       g[r][c] (+)= D - bias[r]
+//             EPI_STEP       g = D - bias + prior'(q); p -= kick*eps*g;
+//                            q += drift*eps*M^-1 p; reflect; write p, q and
+//                            the next step's Q hi/lo operand
+//             EPI_MISFIT     partial[tile][c] = sum_r (D - data[r])^2 inv_var[r]
+// Every mbarrier wait is bounded (2 s of %globaltimer); on expiry the CTA sets
+// *status = HMC_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
+// copies and MMAs, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+
+namespace hmc {
+namespace tc {
+
+constexpr int BM = 128;                   // chains per tile (UMMA M)
+constexpr int BN = 256;                   // matrix rows per tile (UMMA N)
+constexpr int BK = 64;                    // k per stage = one 128-byte swizzle row of bf16
+constexpr int UK = 16;                    // k per tcgen05.mma (kind::f16)
+constexpr int STAGES = 2;
+constexpr int A_BYTES = BM * BK * 2;      // 16 KiB per operand half (chains)
+constexpr int B_BYTES = BN * BK * 2;      // 32 KiB per operand half (rows)
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 192;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
+
+enum Epi { EPI_GRAD = 0, EPI_STEP = 1, EPI_MISFIT = 2 };
+enum Prior { PRIOR_NONE = 0, PRIOR_NORMAL = 1, PRIOR_LAPLACE = 2 };
+
+struct EpiParams {
+  int64_t C;        // chains
+  int64_t rows;     // rows of A (d for GtG, n for G)
+  const float* bias;   // Gtd0 (gradient) or data (misfit), [rows]
+  // EPI_GRAD
+  float* g;            // [rows][C]
+  int accumulate;
+  // EPI_STEP
+  int prior;
+  const float* prior_mean;
+  const float* prior_w;  // inverse variance (normal) or inverse dispersion (laplace)
+  float* p;              // [d][C]
+  float* q;              // [d][C]
+  const float* eps_local;  // [C]
+  float kick, drift;
+  const float* minv;       // [d] inverse mass diagonal or null (unit)
+  const float* lo;
+  const float* hi;
+  const float* center;     // [d] or null: the next operand holds q - center
+  int32_t* flags;          // [C]
+  __nv_bfloat16* qn_hi;    // next operand [C][ldq]
+  __nv_bfloat16* qn_lo;
+  int64_t ldq;
+  // EPI_MISFIT
+  const float* inv_var;    // [rows]
+  double* partial;         // [n_tiles][C]
+  int* status;
+};
+
+// ---- PTX helpers ------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, P;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; false when the 2 s limit expired or another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > WAIT_NS) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, rows of
+// 128 B, 8-row groups 1024 B apart (tcgen05 descriptor format, version 1).
+__device__ __forceinline__ uint64_t sdesc_k_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major.
+constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "setp.ne.b32 P, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, P;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// ---- the kernel -------------------------------------------------------------
+template <int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    chain_gemm_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__ CUtensorMap tq_lo,
+                      const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                      int num_kb, EpiParams ep) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int m0 = blockIdx.x * BM;  // first chain of the tile
+  const int n0 = blockIdx.y * BN;  // first matrix row of the tile
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int tma_issued_stage_uses = 0;  // producer bookkeeping for the abort drain
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer ----------------
+    for (int kb = 0; kb < num_kb; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES) {
+        if (!mbar_wait(&empty[s], ((kb / STAGES) & 1) ^ 1, abort_flag)) {
+          *abort_flag = 1;
+          break;
+        }
+      }
+      unsigned char* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      const int kx = kb * BK;
+      tma_load_2d(st, &tq_hi, &full[s], kx, m0);
+      tma_load_2d(st + A_BYTES, &tq_lo, &full[s], kx, m0);
+      tma_load_2d(st + 2 * A_BYTES, &ta_hi, &full[s], kx, n0);
+      tma_load_2d(st + 2 * A_BYTES + B_BYTES, &ta_lo, &full[s], kx, n0);
+      ++tma_issued_stage_uses;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    bool ok = true;
+    for (int kb = 0; kb < num_kb; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag)) {
+        *abort_flag = 1;
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sa_hi = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t sa_lo = sa_hi + A_BYTES;
+      const uint32_t sb_hi = sa_hi + 2 * A_BYTES;
+      const uint32_t sb_lo = sb_hi + B_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / UK; ++kk) {
+        const uint32_t off = kk * UK * 2;  // bytes along the 128-byte row
+        const uint64_t qh = sdesc_k_sw128(sa_hi + off), ql = sdesc_k_sw128(sa_lo + off);
+        const uint64_t ah = sdesc_k_sw128(sb_hi + off), al = sdesc_k_sw128(sb_lo + off);
+        umma_bf16(tmem, qh, ah, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+        umma_bf16(tmem, qh, al, idesc, 1u);
+        umma_bf16(tmem, ql, ah, idesc, 1u);
+      }
+      umma_commit(&empty[s]);  // frees the stage once these MMAs complete
+    }
+    umma_commit(accum);  // arrives when every MMA issued above completed
+    (void)ok;
+  } else if (warp >= 2) {
+    // ---------------- epilogue ----------------
+    // warp-uniform: the TMEM loads below are warp-collective
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort_flag) ? 1 : 0) != 0;
+    tc_fence_after();
+    const int lane_base = 32 * (warp % 4);
+    const int64_t c = (int64_t)m0 + lane_base + lane;  // this thread's chain
+    const bool live_c = ready && c < ep.C;
+    const uint32_t tbase = tmem + ((uint32_t)lane_base << 16);
+    float eps_k = 0.f, eps_d = 0.f;
+    if (EPI == EPI_STEP && live_c) {
+      const float e = ep.eps_local[c];
+      eps_k = ep.kick * e;
+      eps_d = ep.drift * e;
+    }
+    double misfit_part = 0.0;
+    bool oob = false;
+    for (int cb = 0; cb < BN / 16; ++cb) {
+      float acc[16];
+      if (ready) tmem_ld16(tbase + cb * 16, acc);  // warp-collective: every lane takes part
+      if (!live_c) continue;
+      const int64_t r0 = (int64_t)n0 + cb * 16;
+      if (EPI == EPI_MISFIT) {
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t r = r0 + j;
+          if (r < ep.rows) {
+            const float res = acc[j] - ep.bias[r];
+            s = fmaf(res * res, ep.inv_var[r], s);
+          }
+        }
+        misfit_part += (double)s;
+      } else if (EPI == EPI_GRAD) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t r = r0 + j;
+          if (r < ep.rows) {
+            float gv = acc[j] - ep.bias[r];
+            const int64_t o = r * ep.C + c;
+            if (ep.accumulate) gv += ep.g[o];
+            ep.g[o] = gv;
+          }
+        }
+      } else {  // EPI_STEP
+        __align__(16) __nv_bfloat16 hi16[16];
+        __align__(16) __nv_bfloat16 lo16[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t r = r0 + j;
+          float qv = 0.f;
+          if (r < ep.rows) {
+            const int64_t o = r * ep.C + c;
+            qv = ep.q[o];
+            float gv = acc[j] - ep.bias[r];
+            if (ep.prior == PRIOR_NORMAL) {
+              gv += ep.prior_w[r] * (qv - ep.prior_mean[r]);
+            } else if (ep.prior == PRIOR_LAPLACE) {
+              const float dq = qv - ep.prior_mean[r];
+              gv += (dq > 0.f ? 1.f : (dq < 0.f ? -1.f : 0.f)) * ep.prior_w[r];
+            }
+            float pv = ep.p[o] - eps_k * gv;
+            if (eps_d != 0.f) {
+              const float mp = ep.minv ? ep.minv[r] * pv : pv;
+              qv = qv + eps_d * mp;
+              if (ep.lo && qv < ep.lo[r]) {
+                qv += 2.f * (ep.lo[r] - qv);
+                pv = -pv;
+              }
+              if (ep.hi && qv > ep.hi[r]) {
+                qv += 2.f * (ep.hi[r] - qv);
+                pv = -pv;
+              }
+              if ((ep.lo && qv < ep.lo[r]) || (ep.hi && qv > ep.hi[r])) oob = true;
+              ep.q[o] = qv;
+            }
+            ep.p[o] = pv;
+          }
+          const float qs = (ep.center != nullptr && r < ep.rows) ? qv - ep.center[r] : qv;
+          const __nv_bfloat16 h = __float2bfloat16_rn(qs);
+          hi16[j] = h;
+          lo16[j] = __float2bfloat16_rn(qs - __bfloat162float(h));
+        }
+        if (ep.qn_hi != nullptr && r0 < ep.ldq) {
+          uint4* dh = (uint4*)(ep.qn_hi + c * ep.ldq + r0);
+          uint4* dl = (uint4*)(ep.qn_lo + c * ep.ldq + r0);
+          dh[0] = ((const uint4*)hi16)[0];
+          dh[1] = ((const uint4*)hi16)[1];
+          dl[0] = ((const uint4*)lo16)[0];
+          dl[1] = ((const uint4*)lo16)[1];
+        }
+      }
+    }
+    if (EPI == EPI_MISFIT && live_c) ep.partial[(int64_t)blockIdx.y * ep.C + c] = misfit_part;
+    if (EPI == EPI_STEP && oob) atomicOr(&ep.flags[c], HMC_FLAG_OUT_OF_BOUNDS);
+    if (!ready && threadIdx.x == 64) {
+      atomicExch(ep.status, HMC_ERR_TIMEOUT);
+      *abort_flag = 1;
+    }
+  }
+  // ---------------- teardown ----------------
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_flag) {
+    // Drain what this CTA put in flight before releasing TMEM and smem.
+    if (warp == 1 && lane == 0) {
+      const uint64_t t0 = globaltimer();
+      while (!mbar_try_wait(accum, 0) && globaltimer() - t0 < WAIT_NS) {
+      }
+    }
+    if (warp == 0 && lane == 0) {
+      for (int u = 0; u < tma_issued_stage_uses && u < num_kb; ++u) {
+        const int s = u % STAGES;
+        const uint64_t t0 = globaltimer();
+        while (!mbar_try_wait(&full[s], (u / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+        }
+      }
+      atomicExch(ep.status, HMC_ERR_TIMEOUT);
+    }
+    __syncthreads();
+  }
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// ---- helpers for the operands ------------------------------------------------
+// hi/lo split of a row-major FP32 matrix into padded [rows][ld] BF16 arrays
+// (columns cols..ld-1 are zero).
+__global__ void split_rows_kernel(int64_t rows, int64_t cols, const float* __restrict__ src, int64_t ld,
+                                  __nv_bfloat16* hi, __nv_bfloat16* lo) {
+  const int64_t total = rows * ld;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / ld, k = t % ld;
+    const float v = k < cols ? src[r * cols + k] : 0.f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi[t] = h;
+    lo[t] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
+// Chain state q [d][C] -> chain-major hi/lo [C][ld] (zero pad), 32x32 tiles.
+__global__ void split_transpose_kernel(int64_t d, int64_t C, const float* __restrict__ q,
+                                       const float* __restrict__ center, int64_t ld, __nv_bfloat16* hi,
+                                       __nv_bfloat16* lo) {
+  __shared__ float tile[32][33];
+  const int64_t i0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t i = i0 + y, c = c0 + threadIdx.x;
+    tile[y][threadIdx.x] = (i < d && c < C) ? (center ? q[i * C + c] - center[i] : q[i * C + c]) : 0.f;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t c = c0 + y, i = i0 + threadIdx.x;
+    if (c < C && i < ld) {
+      const float v = tile[threadIdx.x][y];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[c * ld + i] = h;
+      lo[c * ld + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+  }
+}
+
+// x[c] (+)= 0.5 * sum_t partial[t][c]
+__global__ void reduce_partials_kernel(int64_t C, int tiles, const double* __restrict__ partial, double* x,
+                                       int accumulate) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  double s = 0.0;
+  for (int t = 0; t < tiles; ++t) s += partial[(int64_t)t * C + c];
+  x[c] = accumulate ? x[c] + 0.5 * s : 0.5 * s;
+}
+
+// ---- host side -----------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+// 2-D BF16 tensor map over a [rows][ld] array whose first `cols` columns are
+// valid (columns >= cols read as zero), box = box_rows x 64.
+int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return fail(HMC_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  HMC_REQUIRE(((uintptr_t)base & 15) == 0, "tensor-core operand must be 16-byte aligned");
+  HMC_REQUIRE((ld * 2) % 16 == 0 && ld >= cols, "tensor-core operand pitch must be a multiple of 8 elements");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HMC_ERR_INVALID_ARG, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return HMC_OK;
+}
+
+template <int EPI>
+int launch(int64_t C, int64_t rows, int64_t K, const void* q_hi, const void* q_lo, int64_t ldq, const void* a_hi,
+           const void* a_lo, int64_t lda, const EpiParams& ep, cudaStream_t st) {
+  HMC_REQUIRE(C > 0 && rows > 0 && K > 0, "tensor-core contraction: bad sizes");
+  HMC_REQUIRE(C < (1ll << 31) && rows < (1ll << 31) && K < (1ll << 31), "tensor-core contraction: too large");
+  HMC_REQUIRE(ep.status != nullptr, "tensor-core contraction: null status word");
+  CUtensorMap mq_hi, mq_lo, ma_hi, ma_lo;
+  HMC_TRY(make_map(&mq_hi, q_hi, C, K, ldq, BM));
+  HMC_TRY(make_map(&mq_lo, q_lo, C, K, ldq, BM));
+  HMC_TRY(make_map(&ma_hi, a_hi, rows, K, lda, BN));
+  HMC_TRY(make_map(&ma_lo, a_lo, rows, K, lda, BN));
+  static bool attr_set[3] = {false, false, false};
+  if (!attr_set[EPI]) {
+    cudaError_t e = cudaFuncSetAttribute(chain_gemm_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM_BYTES);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(chain_gemm_kernel)");
+    attr_set[EPI] = true;
+  }
+  const int num_kb = (int)((K + BK - 1) / BK);
+  const dim3 grid((unsigned)((C + BM - 1) / BM), (unsigned)((rows + BN - 1) / BN));
+  HMC_REQUIRE(grid.y <= 65535, "tensor-core contraction: too many rows");
+  chain_gemm_kernel<EPI><<<grid, THREADS, SMEM_BYTES, st>>>(mq_hi, mq_lo, ma_hi, ma_lo, num_kb, ep);
+  return check_launch("chain_gemm_kernel");
+}
+
+}  // namespace tc
+}  // namespace hmc
+
+using namespace hmc;
+using namespace hmc::tc;
+
+extern "C" {
+
+HMC_API int hmc_split_bf16(int64_t rows, int64_t cols, const float* src, int64_t ld, void* hi, void* lo,
+                           void* stream) {
+  HMC_REQUIRE(rows >= 0 && cols >= 0 && ld >= cols && ld % 8 == 0, "hmc_split_bf16: bad sizes");
+  if (rows == 0) return HMC_OK;
+  HMC_REQUIRE(src && hi && lo, "hmc_split_bf16: null argument");
+  const unsigned g = blocks_for(rows * ld, 256) > 152u * 16 ? 152u * 16 : blocks_for(rows * ld, 256);
+  split_rows_kernel<<<g, 256, 0, as_stream(stream)>>>(rows, cols, src, ld, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+  return check_launch("split_rows_kernel");
+}
+
+HMC_API int hmc_split_bf16_transpose(int64_t d, int64_t C, const float* q, const float* center, int64_t ld,
+                                     void* hi, void* lo, void* stream) {
+  HMC_REQUIRE(d > 0 && C >= 0 && ld >= d && ld % 8 == 0, "hmc_split_bf16_transpose: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(q && hi && lo, "hmc_split_bf16_transpose: null argument");
+  HMC_REQUIRE((ld + 31) / 32 <= 65535, "hmc_split_bf16_transpose: too many rows");
+  const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((ld + 31) / 32));
+  split_transpose_kernel<<<grid, dim3(32, 8), 0, as_stream(stream)>>>(d, C, q, center, ld, (__nv_bfloat16*)hi,
+                                                                     (__nv_bfloat16*)lo);
+  return check_launch("split_transpose_kernel");
+}
+
+HMC_API int hmc_tc_gradient(int64_t rows, int64_t K, int64_t C, const void* a_hi, const void* a_lo, int64_t lda,
+                            const void* q_hi, const void* q_lo, int64_t ldq, const float* bias, float* g,
+                            int accumulate, int* status, void* stream) {
+  HMC_REQUIRE(bias && g, "hmc_tc_gradient: null argument");
+  EpiParams ep = {};
+  ep.C = C;
+  ep.rows = rows;
+  ep.bias = bias;
+  ep.g = g;
+  ep.accumulate = accumulate;
+  ep.status = status;
+  return launch<EPI_GRAD>(C, rows, K, q_hi, q_lo, ldq, a_hi, a_lo, lda, ep, as_stream(stream));
+}
+
+HMC_API int hmc_tc_step(const hmc_chains* s, const void* a_hi, const void* a_lo, int64_t lda, const void* q_hi,
+                        const void* q_lo, void* qn_hi, void* qn_lo, int64_t ldq, const float* center,
+                        const float* bias, int prior, const float* prior_mean, const float* prior_w, double kick,
+                        double drift, int* status, void* stream) {
+  HMC_REQUIRE(s != nullptr && s->dtype == HMC_F32, "hmc_tc_step: needs an FP32 chain state");
+  HMC_REQUIRE(s->mass_kind == HMC_MASS_UNIT || s->mass_kind == HMC_MASS_DIAG,
+              "hmc_tc_step: unit or diagonal mass only");
+  HMC_REQUIRE(bias && s->p && s->q && s->eps_local && s->flags, "hmc_tc_step: missing buffer");
+  HMC_REQUIRE(prior == PRIOR_NONE || (prior_mean && prior_w), "hmc_tc_step: prior needs mean and weights");
+  HMC_REQUIRE(prior >= PRIOR_NONE && prior <= PRIOR_LAPLACE, "hmc_tc_step: unknown prior kind");
+  HMC_REQUIRE(ldq % 16 == 0, "hmc_tc_step: operand pitch must be a multiple of 16");
+  EpiParams ep = {};
+  ep.C = s->chains;
+  ep.rows = s->dims;
+  ep.bias = bias;
+  ep.prior = prior;
+  ep.prior_mean = prior_mean;
+  ep.prior_w = prior_w;
+  ep.p = (float*)s->p;
+  ep.q = (float*)s->q;
+  ep.eps_local = (const float*)s->eps_local;
+  ep.kick = (float)kick;
+  ep.drift = (float)drift;
+  ep.minv = s->mass_kind == HMC_MASS_DIAG ? (const float*)s->mass_inv_diag : nullptr;
+  ep.lo = (const float*)s->lower;
+  ep.hi = (const float*)s->upper;
+  ep.flags = s->flags;
+  ep.center = center;
+  HMC_REQUIRE(qn_hi != q_hi && qn_lo != q_lo, "hmc_tc_step: the next operand must not alias the current one");
+  ep.qn_hi = (__nv_bfloat16*)qn_hi;
+  ep.qn_lo = (__nv_bfloat16*)qn_lo;
+  ep.ldq = ldq;
+  ep.status = status;
+  return launch<EPI_STEP>(s->chains, s->dims, s->dims, q_hi, q_lo, ldq, a_hi, a_lo, lda, ep, as_stream(stream));
+}
+
+HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C, const void* g_hi, const void* g_lo, int64_t ldg,
+                                const void* q_hi, const void* q_lo, int64_t ldq, const float* data,
+                                const float* inv_var, double* partial, double* out_x, int accumulate, int* status,
+                                void* stream) {
+  HMC_REQUIRE(data && inv_var && partial && out_x, "hmc_tc_resid_misfit: null argument");
+  EpiParams ep = {};
+  ep.C = C;
+  ep.rows = n;
+  ep.bias = data;
+  ep.inv_var = inv_var;
+  ep.partial = partial;
+  ep.status = status;
+  HMC_TRY(launch<EPI_MISFIT>(C, n, d, q_hi, q_lo, ldq, g_hi, g_lo, ldg, ep, as_stream(stream)));
+  const int tiles = (int)((n + BN - 1) / BN);
+  reduce_partials_kernel<<<blocks_for(C, 256), 256, 0, as_stream(stream)>>>(C, tiles, partial, out_x, accumulate);
+  return check_launch("reduce_partials_kernel");
+}
+
+HMC_API int64_t hmc_tc_partials_size(int64_t n, int64_t C) { return (n + BN - 1) / BN * C; }
+
+}  // extern "C"

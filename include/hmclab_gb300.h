@@ -266,6 +266,52 @@ HMC_API int hmc_srcloc3d_gradient(int dtype, int64_t E, int64_t S, int64_t C,
                           double medium_velocity, void* out_g, int accumulate,
                           void* stream);
 
+/* ---- tensor-core (tcgen05) contraction of a dense matrix with all chains --
+ * FP32 path of LinearMatrix.py:184-208: BF16 hi/lo split operands
+ * (x = hi + lo, 3 products hi*hi + hi*lo + lo*hi, FP32 accumulation in
+ * TMEM).  A dense matrix A [rows][K] is stored split as a_hi/a_lo with row
+ * pitch lda (multiple of 64); the chain positions are stored transposed,
+ * chain-major, as q_hi/q_lo [C][ldq].  status is a device int that receives
+ * HMC_ERR_TIMEOUT if a bounded wait inside the kernel expired.             */
+HMC_API int hmc_split_bf16(int64_t rows, int64_t cols, const float* src,
+                           int64_t ld, void* hi, void* lo, void* stream);
+/* hi/lo split of (q - center) (center [d] nullable) transposed to [C][ld]. */
+HMC_API int hmc_split_bf16_transpose(int64_t d, int64_t C, const float* q,
+                                     const float* center, int64_t ld,
+                                     void* hi, void* lo, void* stream);
+/* g[r][c] (+)= sum_k A[r][k] Q[c][k] - bias[r]   (GtG m - Gtd0)            */
+HMC_API int hmc_tc_gradient(int64_t rows, int64_t K, int64_t C,
+                            const void* a_hi, const void* a_lo, int64_t lda,
+                            const void* q_hi, const void* q_lo, int64_t ldq,
+                            const float* bias, float* g, int accumulate,
+                            int* status, void* stream);
+/* One fused leapfrog kick(+drift) for FP32 chains (Samplers.py:1561-1581)
+ * with the posterior gradient GtG q - Gtd0 + prior'(q) (prior: 0 none,
+ * 1 Normal diagonal with prior_w = 1/variance, 2 Laplace with prior_w =
+ * 1/dispersion; base.py:564-574, 702-710) formed in the epilogue; writes p,
+ * q (reflected at the bounds) and the next operand qn_hi/qn_lo = split of
+ * (q - center) (must not alias q_hi/q_lo).  With a center c the operands
+ * hold q - c and bias must be Gtd0 - GtG c, which keeps the split products
+ * accurate near the data-consistent region.  Unit or diagonal mass.         */
+HMC_API int hmc_tc_step(const hmc_chains* s, const void* a_hi,
+                        const void* a_lo, int64_t lda, const void* q_hi,
+                        const void* q_lo, void* qn_hi, void* qn_lo,
+                        int64_t ldq, const float* center,
+                        const float* bias, int prior,
+                        const float* prior_mean, const float* prior_w,
+                        double kick, double drift, int* status, void* stream);
+/* Residual misfit 0.5 sum_r (G m - data)_r^2 inv_var_r per chain
+ * (LinearMatrix.py:193-202) with FP64 per-chain sums; partial holds
+ * hmc_tc_partials_size(n, C) doubles.                                       */
+HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C,
+                                const void* g_hi, const void* g_lo,
+                                int64_t ldg, const void* q_hi,
+                                const void* q_lo, int64_t ldq,
+                                const float* data, const float* inv_var,
+                                double* partial, double* out_x, int accumulate,
+                                int* status, void* stream);
+HMC_API int64_t hmc_tc_partials_size(int64_t n, int64_t C);
+
 /* ---- dense matrix product used by the ops above -------------------------
  * out[m][n] = alpha * A[m][k] B[k][n] + (bias ? bias[m] : 0)
  *             + (accumulate ? out[m][n] : 0), all row-major.                */
