@@ -205,20 +205,30 @@ def run_reference_arm(args, wl):
 
 # ---------------------------------------------------------------------------
 def dominant_kernel_timing(post, smp, n_iter=20):
-    """Average duration of the dense gradient launch (GtG @ Q - Gtd0 + prior)
-    with CUDA events on the sampler stream, inputs = the live chain state."""
+    """Average duration of the dominant kernel with CUDA events on the sampler
+    stream, on the live chain state: the fused tensor-core leapfrog step
+    (GtG @ Q - Gtd0 + prior, kick, drift, operand re-split) when the sampler
+    uses it, else the gradient launch of the likelihood."""
     import torch
 
     st = smp.stream
     h = st.cuda_stream
     lik = post.separate_distributions[1]
+    if smp._fused is not None:
+        smp._fused.after_begin(h)
+
+        def launch():
+            smp._fused.kick_drift(1.0, 1.0, h)
+    else:
+        def launch():
+            lik._device_gradient(smp.q, smp.g, False, smp.dtype, h)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(st):
         for _ in range(3):
-            lik._device_gradient(smp.q, smp.g, False, smp.dtype, h)
+            launch()
         ev0.record(st)
         for _ in range(n_iter):
-            lik._device_gradient(smp.q, smp.g, False, smp.dtype, h)
+            launch()
         ev1.record(st)
     st.synchronize()
     return ev0.elapsed_time(ev1) / 1e3 / n_iter
@@ -307,9 +317,12 @@ def run_gpu_arm(args, wl):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds": t_e2e},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "dense gradient GtG@Q (prior fused)", "bound": "tensor", "achieved": achieved,
-                     "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
-                     "peak_source": src, "launch_s": t_gemm},
+        "roofline": {"kernel": ("chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
+                                if smp._fused is not None else "dense gradient GEMM"),
+                     "bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": achieved / bf16, "traffic": None, "peak_source": src, "launch_s": t_gemm,
+                     "algorithmic_flop_per_launch": wl.gemm_flops(),
+                     "executed_flop_per_launch": 3 * wl.gemm_flops() if smp._fused is not None else wl.gemm_flops()},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
