@@ -10,10 +10,10 @@
 // Q holds the chains' positions transposed to chain-major [C][ld] (K-major
 // operand), re-split by the epilogue of every fused step.
 //
-// Kernel structure (one 128-chain x 256-row output tile per CTA, 192 threads):
+// Kernel structure (one 128-chain x 256-row output tile per CTA, 320 threads):
 //   warp 0  TMEM allocation; one lane issues TMA tile loads (128B swizzle)
 //   warp 1  one lane issues tcgen05.mma (M=128, N=256, K=16) and commits
-//   warps 2-5  epilogue: tcgen05.ld of the accumulator (lane = chain),
+//   warps 2-9  epilogue: tcgen05.ld of the accumulator (lane = chain),
 //           then one of:
 //             EPI_GRAD       g[r][c] (+)= D - bias[r]
 //             EPI_STEP       g = D - bias + prior'(q); p -= kick*eps*g;
@@ -43,7 +43,7 @@ constexpr int A_BYTES = BM * BK * 2;      // 16 KiB per operand half (chains)
 constexpr int B_BYTES = BN * BK * 2;      // 32 KiB per operand half (rows)
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int THREADS = 192;
+constexpr int THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t TMEM_COLS = 256;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
 
@@ -263,12 +263,31 @@ __global__ void __launch_bounds__(THREADS, 1)
     (void)ok;
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
+    // Eight warps: warp w reads TMEM lanes 32*(w%4)..+31 (its chains) and
+    // handles every other 16-column chunk of the tile (half = 0 or 1).
+    const int quarter = warp % 4;
+    const int half = (warp - 2) / 4;
+    const int lane_base = 32 * quarter;
+    const int64_t c = (int64_t)m0 + lane_base + lane;  // this thread's chain
+    float* __restrict__ pp = ep.p;
+    float* __restrict__ qq = ep.q;
+    const int64_t C = ep.C;
+    // While the MMAs run, pull this tile's rows of p and q into L2.
+    if (EPI == EPI_STEP) {
+      const int et = threadIdx.x - 64;  // 0..255
+      const int64_t row = (int64_t)n0 + et;
+      if (row < ep.rows && m0 < C) {
+        const int64_t cnt = (C - m0) < BM ? (C - m0) : BM;
+        for (int64_t off = 0; off < cnt; off += 32) {
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pp + row * C + m0 + off));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(qq + row * C + m0 + off));
+        }
+      }
+    }
     // warp-uniform: the TMEM loads below are warp-collective
     const bool ready = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort_flag) ? 1 : 0) != 0;
     tc_fence_after();
-    const int lane_base = 32 * (warp % 4);
-    const int64_t c = (int64_t)m0 + lane_base + lane;  // this thread's chain
-    const bool live_c = ready && c < ep.C;
+    const bool live_c = ready && c < C;
     const uint32_t tbase = tmem + ((uint32_t)lane_base << 16);
     float eps_k = 0.f, eps_d = 0.f;
     if (EPI == EPI_STEP && live_c) {
@@ -278,71 +297,78 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     double misfit_part = 0.0;
     bool oob = false;
-    for (int cb = 0; cb < BN / 16; ++cb) {
+    for (int cb = half; cb < BN / 16; cb += 2) {
       float acc[16];
       if (ready) tmem_ld16(tbase + cb * 16, acc);  // warp-collective: every lane takes part
       if (!live_c) continue;
       const int64_t r0 = (int64_t)n0 + cb * 16;
+      const int nr = (int)((ep.rows - r0) < 16 ? (ep.rows - r0) : 16);  // valid rows in this chunk
       if (EPI == EPI_MISFIT) {
         float s = 0.f;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int64_t r = r0 + j;
-          if (r < ep.rows) {
-            const float res = acc[j] - ep.bias[r];
-            s = fmaf(res * res, ep.inv_var[r], s);
+          if (j < nr) {
+            const float res = acc[j] - ep.bias[r0 + j];
+            s = fmaf(res * res, ep.inv_var[r0 + j], s);
           }
         }
         misfit_part += (double)s;
       } else if (EPI == EPI_GRAD) {
+        float gold[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) gold[j] = (ep.accumulate && j < nr) ? ep.g[(r0 + j) * C + c] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (j < nr) ep.g[(r0 + j) * C + c] = acc[j] - ep.bias[r0 + j] + gold[j];
+      } else {  // EPI_STEP
+        // all loads of the chunk first (independent, in flight together)
+        float qv[16], pv[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int64_t r = r0 + j;
-          if (r < ep.rows) {
-            float gv = acc[j] - ep.bias[r];
-            const int64_t o = r * ep.C + c;
-            if (ep.accumulate) gv += ep.g[o];
-            ep.g[o] = gv;
-          }
+          qv[j] = j < nr ? qq[(r0 + j) * C + c] : 0.f;
+          pv[j] = j < nr ? pp[(r0 + j) * C + c] : 0.f;
         }
-      } else {  // EPI_STEP
         __align__(16) __nv_bfloat16 hi16[16];
         __align__(16) __nv_bfloat16 lo16[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int64_t r = r0 + j;
-          float qv = 0.f;
-          if (r < ep.rows) {
-            const int64_t o = r * ep.C + c;
-            qv = ep.q[o];
+          float qs = 0.f;
+          if (j < nr) {
             float gv = acc[j] - ep.bias[r];
             if (ep.prior == PRIOR_NORMAL) {
-              gv += ep.prior_w[r] * (qv - ep.prior_mean[r]);
+              gv += ep.prior_w[r] * (qv[j] - ep.prior_mean[r]);
             } else if (ep.prior == PRIOR_LAPLACE) {
-              const float dq = qv - ep.prior_mean[r];
+              const float dq = qv[j] - ep.prior_mean[r];
               gv += (dq > 0.f ? 1.f : (dq < 0.f ? -1.f : 0.f)) * ep.prior_w[r];
             }
-            float pv = ep.p[o] - eps_k * gv;
+            pv[j] = pv[j] - eps_k * gv;
             if (eps_d != 0.f) {
-              const float mp = ep.minv ? ep.minv[r] * pv : pv;
-              qv = qv + eps_d * mp;
-              if (ep.lo && qv < ep.lo[r]) {
-                qv += 2.f * (ep.lo[r] - qv);
-                pv = -pv;
+              const float mp = ep.minv ? ep.minv[r] * pv[j] : pv[j];
+              float qn = qv[j] + eps_d * mp;
+              if (ep.lo && qn < ep.lo[r]) {
+                qn += 2.f * (ep.lo[r] - qn);
+                pv[j] = -pv[j];
               }
-              if (ep.hi && qv > ep.hi[r]) {
-                qv += 2.f * (ep.hi[r] - qv);
-                pv = -pv;
+              if (ep.hi && qn > ep.hi[r]) {
+                qn += 2.f * (ep.hi[r] - qn);
+                pv[j] = -pv[j];
               }
-              if ((ep.lo && qv < ep.lo[r]) || (ep.hi && qv > ep.hi[r])) oob = true;
-              ep.q[o] = qv;
+              if ((ep.lo && qn < ep.lo[r]) || (ep.hi && qn > ep.hi[r])) oob = true;
+              qv[j] = qn;
             }
-            ep.p[o] = pv;
+            qs = ep.center != nullptr ? qv[j] - ep.center[r] : qv[j];
           }
-          const float qs = (ep.center != nullptr && r < ep.rows) ? qv - ep.center[r] : qv;
           const __nv_bfloat16 h = __float2bfloat16_rn(qs);
           hi16[j] = h;
           lo16[j] = __float2bfloat16_rn(qs - __bfloat162float(h));
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (j < nr) {
+            pp[(r0 + j) * C + c] = pv[j];
+            if (eps_d != 0.f) qq[(r0 + j) * C + c] = qv[j];
+          }
         }
         if (ep.qn_hi != nullptr && r0 < ep.ldq) {
           uint4* dh = (uint4*)(ep.qn_hi + c * ep.ldq + r0);
@@ -354,11 +380,22 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
     }
-    if (EPI == EPI_MISFIT && live_c) ep.partial[(int64_t)blockIdx.y * ep.C + c] = misfit_part;
+    if (EPI == EPI_MISFIT && live_c) {
+      // two warps share each chain: combine their halves through shared memory
+      double* red = (double*)(smem);  // operand stages are idle once the accumulator is ready
+      if (half == 1) red[lane_base + lane] = misfit_part;
+    }
     if (EPI == EPI_STEP && oob) atomicOr(&ep.flags[c], HMC_FLAG_OUT_OF_BOUNDS);
     if (!ready && threadIdx.x == 64) {
       atomicExch(ep.status, HMC_ERR_TIMEOUT);
       *abort_flag = 1;
+    }
+    if (EPI == EPI_MISFIT) {
+      asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps only
+      if (half == 0 && live_c) {
+        const double* red = (const double*)(smem);
+        ep.partial[(int64_t)blockIdx.y * C + c] = misfit_part + red[lane_base + lane];
+      }
     }
   }
   // ---------------- teardown ----------------
