@@ -36,11 +36,12 @@ namespace tc {
 
 constexpr int BM = 128;                   // chains per tile (UMMA M)
 constexpr int BN = 256;                   // matrix rows per tile (UMMA N)
-constexpr int BK = 64;                    // k per stage = one 128-byte swizzle row of bf16
+constexpr int SWZ = 64;                   // swizzle span in bytes (64 or 128)
+constexpr int BK = SWZ / 2;               // k per stage = one swizzle row of bf16
 constexpr int UK = 16;                    // k per tcgen05.mma (kind::f16)
-constexpr int STAGES = 2;
-constexpr int A_BYTES = BM * BK * 2;      // 16 KiB per operand half (chains)
-constexpr int B_BYTES = BN * BK * 2;      // 32 KiB per operand half (rows)
+constexpr int STAGES = SWZ == 64 ? 4 : 2;
+constexpr int A_BYTES = BM * BK * 2;      // per operand half (chains)
+constexpr int B_BYTES = BN * BK * 2;      // per operand half (rows)
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
@@ -130,15 +131,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, rows of
-// 128 B, 8-row groups 1024 B apart (tcgen05 descriptor format, version 1).
-__device__ __forceinline__ uint64_t sdesc_k_sw128(uint32_t saddr) {
+// Shared-memory matrix descriptor: K-major tile, SWZ-byte swizzle, rows of
+// SWZ bytes, 8-row groups 8*SWZ bytes apart (tcgen05 descriptor, version 1).
+__device__ __forceinline__ uint64_t sdesc_k_sw(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
   d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)((8 * SWZ) >> 4) << 32;  // stride byte offset
   d |= (uint64_t)1 << 46;              // descriptor version
-  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  d |= (uint64_t)(SWZ == 128 ? 2 : 4) << 61;  // SWIZZLE_128B / SWIZZLE_64B
   return d;
 }
 
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   int tma_issued_stage_uses = 0;  // producer bookkeeping for the abort drain
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer ----------------
+    const int kb_rot = (int)((blockIdx.x + 7u * blockIdx.y) % (unsigned)num_kb);
     for (int kb = 0; kb < num_kb; ++kb) {
       const int s = kb % STAGES;
       if (kb >= STAGES) {
@@ -225,7 +227,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       unsigned char* st = smem + s * STAGE_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      const int kx = kb * BK;
+      // CTAs that share an operand tile start at different k-blocks, so
+      // they do not all fetch the same lines from the same L2 slices at once.
+      const int kx = ((kb + kb_rot) % num_kb) * BK;
       tma_load_2d(st, &tq_hi, &full[s], kx, m0);
       tma_load_2d(st + A_BYTES, &tq_lo, &full[s], kx, m0);
       tma_load_2d(st + 2 * A_BYTES, &ta_hi, &full[s], kx, n0);
@@ -251,8 +255,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int kk = 0; kk < BK / UK; ++kk) {
         const uint32_t off = kk * UK * 2;  // bytes along the 128-byte row
-        const uint64_t qh = sdesc_k_sw128(sa_hi + off), ql = sdesc_k_sw128(sa_lo + off);
-        const uint64_t ah = sdesc_k_sw128(sb_hi + off), al = sdesc_k_sw128(sb_lo + off);
+        const uint64_t qh = sdesc_k_sw(sa_hi + off), ql = sdesc_k_sw(sa_lo + off);
+        const uint64_t ah = sdesc_k_sw(sb_hi + off), al = sdesc_k_sw(sb_lo + off);
         umma_bf16(tmem, qh, ah, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
         umma_bf16(tmem, qh, al, idesc, 1u);
         umma_bf16(tmem, ql, ah, idesc, 1u);
@@ -499,7 +503,8 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int
   cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, SWZ == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(HMC_ERR_INVALID_ARG, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return HMC_OK;
