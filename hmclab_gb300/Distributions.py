@@ -625,3 +625,217 @@ class SourceLocation3D(_AbstractDistribution):
     @staticmethod
     def forward(x, y, z, T, v, receiver_array_x, receiver_array_y, receiver_array_z):
         return T + ((x - receiver_array_x) ** 2 + (y - receiver_array_y) ** 2 + (z - receiver_array_z) ** 2) ** 0.5 / v
+
+
+# ---------------------------------------------------------------------------
+class ElasticFullWaveform2D(_AbstractDistribution):
+    """2-D elastic P-SV full-waveform misfit (reference
+    `ElasticFullWaveform2D.py:12-226`), computed by the project's own FP32
+    finite-difference kernels instead of psvWave, for C chains at once.
+
+    `_input` is an `hmclab_gb300.fwi.ElasticConfig` (the reference takes a
+    psvWave .ini file) or another ElasticFullWaveform2D to copy.  Observed
+    records `ux_obs`, `uz_obs` are [shots][nt][receivers].  The misfit is
+    0.5 * sum (u - u_obs)^2 / data_std^2 / temperature.  The model is
+    parametrised by Gaussian blobs (`free_parameter_grid=[nx, nz]`,
+    `make_blob`), m = [vp blobs | vs blobs | rho blobs], fine fields =
+    basis @ m + background.  The gradient is the exact derivative of the
+    discrete misfit (chain rule through the basis); `gradient_projection=
+    "least_squares"` instead applies the reference's (C^T C)^-1 C^T map
+    (ElasticFullWaveform2D.py:159, 329-330)."""
+
+    temperature: float = 1.0
+
+    def __init__(self, _input, ux_obs=None, uz_obs=None, temperature=None, omp_threads_override=None,
+                 free_parameter_grid=None, data_std=1.0, background=None, gradient_projection="chain_rule"):
+        from hmclab_gb300 import fwi as _fwi
+
+        if isinstance(_input, ElasticFullWaveform2D):
+            src = _input
+            self.config = src.config
+            self.background = src.background
+            ux_obs = src.ux_obs if ux_obs is None else ux_obs
+            uz_obs = src.uz_obs if uz_obs is None else uz_obs
+            temperature = src.temperature if temperature is None else temperature
+            data_std = src.data_std
+            free_parameter_grid = free_parameter_grid or ([src.blob.nbx, src.blob.nbz] if src.blob else None)
+            gradient_projection = src.gradient_projection
+        elif isinstance(_input, _fwi.ElasticConfig):
+            self.config = _input
+            self.background = background if background is not None else _fwi.layered_model(_input, anomalies=False)
+        else:
+            raise ValueError(f"Incorrect initialization. Passed argument `{_input}` can not create an FWI object.")
+        if ux_obs is None or uz_obs is None:
+            raise ValueError("No passed observed data. Could not construct an inverse problem.")
+        cfg = self.config
+        self.ux_obs = _numpy.asarray(ux_obs, dtype=_numpy.float64).reshape(cfg.n_shots, cfg.nt, cfg.n_rec)
+        self.uz_obs = _numpy.asarray(uz_obs, dtype=_numpy.float64).reshape(cfg.n_shots, cfg.nt, cfg.n_rec)
+        self.temperature = 1.0 if temperature is None else float(temperature)
+        self.data_std = float(data_std)
+        self.gradient_projection = gradient_projection
+        self.blob = None
+        self.dimensions = 3 * cfg.nx * cfg.nz
+        if free_parameter_grid is not None:
+            self.make_blob(*free_parameter_grid)
+
+    def make_blob(self, nx, nz):
+        from hmclab_gb300 import fwi as _fwi
+
+        self.blob = _fwi.BlobBasis(self.config, nx, nz)
+        self.dimensions = self.blob.free_parameters
+        self.__dict__.pop("_param_cache", None)
+        self.__dict__.pop("_scratch_cache", None)
+
+    @property
+    def weight(self):
+        return 1.0 / (self.data_std**2 * self.temperature)
+
+    def fine_model(self, m):
+        """Physical (vp, vs, rho) fields [nz][nx] of a blob model vector (host)."""
+        m = _numpy.asarray(m, dtype=_numpy.float64).reshape(3, -1)
+        cfg = self.config
+        return tuple((self.blob.B @ m[f]).reshape(cfg.nz, cfg.nx) + self.background[f] for f in range(3))
+
+    # ---- device parameters ------------------------------------------------
+    def _make_params(self, dtype):
+        if self.blob is None:
+            raise NotImplementedError("the device path needs the blob parametrisation (make_blob)")
+        cfg = self.config
+        Bs = self.blob.simulation_basis()  # [cells][blobs]
+        bg = [cfg.extend(self.background[f]).reshape(-1) for f in range(3)]  # vp, vs, rho
+        obs = _numpy.stack([self.ux_obs, self.uz_obs], axis=-1)  # shots, nt, rec, 2
+        rec_map = -_numpy.ones((cfg.nzc, cfg.nxc), _numpy.int32)
+        for r, (x, z) in enumerate(zip(cfg.rec_x, cfg.rec_z)):
+            rec_map[z, x] = r
+        p = {
+            "B": _dev.upload(Bs, "float32"),
+            "Bt": _dev.upload(_numpy.ascontiguousarray(Bs.T), "float32"),
+            "bg": [_dev.upload(b, "float32") for b in bg],
+            "taper": _dev.upload(cfg.taper(), "float32"),
+            "rec_map": _dev.upload_int32(rec_map),
+            "obs": _dev.upload(obs, "float32"),
+            "stf_host": _numpy.ascontiguousarray(cfg.ricker(), dtype=_numpy.float32),
+        }
+        if self.gradient_projection == "least_squares":
+            B = self.blob.B
+            p["proj"] = _dev.upload(_numpy.linalg.inv(B.T @ B), "float32")
+        return p
+
+    def _workspace(self, C, device, with_gradient):
+        import torch
+
+        cache = self.__dict__.setdefault("_scratch_cache", {})
+        key = ("fwi", int(C))
+        ws = cache.get(key)
+        cfg = self.config
+        cells = cfg.nzc * cfg.nxc
+        if ws is None:
+            z = lambda *shape: torch.zeros(shape, dtype=torch.float32, device=device)  # noqa: E731
+            ws = {name: z(cells, C) for name in ("vp", "vs", "rho", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz",
+                                                 "sxx", "szz", "sxz")}
+            ws["rec"] = z(cfg.n_shots * cfg.nt * cfg.n_rec * 2 * C)
+            cache[key] = ws
+        if with_gradient and "store" not in ws:
+            z = lambda *shape: torch.zeros(shape, dtype=torch.float32, device=device)  # noqa: E731
+            for name in ("avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam", "g_muxz", "g_vp",
+                         "g_vs", "g_rho"):
+                ws[name] = z(cells, C)
+            ws["store"] = z(cfg.nt * 2 * cells * C)
+            ws["resid"] = z(cfg.nt * cfg.n_rec * 2 * C)
+            ws["gtmp"] = z(self.blob.n_blobs, C)
+        return ws
+
+    def _descriptor(self, ws, C):
+        from hmclab_gb300 import _lib as L
+
+        cfg, p = self.config, self._params("float32")
+        d = L.HmcFwi()
+        d.nx, d.nz, d.nt, d.nrec, d.chains = cfg.nxc, cfg.nzc, cfg.nt, cfg.n_rec, C
+        d.h, d.dt, d.w = cfg.h, cfg.dt, self.weight
+        d.taper, d.rec_map, d.obs = p["taper"].data_ptr(), p["rec_map"].data_ptr(), p["obs"].data_ptr()
+        d.stf_host = p["stf_host"].ctypes.data
+        for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec"):
+            setattr(d, name, ws[name].data_ptr())
+        for name in ("store", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam",
+                     "g_muxz"):
+            if name in ws:
+                setattr(d, name, ws[name].data_ptr())
+        return d
+
+    def _set_model(self, M, ws, stream):
+        """Blob amplitudes (3*nb, C) FP32 -> simulation-grid fields."""
+        p = self._params("float32")
+        nb, C = self.blob.n_blobs, M.shape[1]
+        cells = self.config.nzc * self.config.nxc
+        for f, name in enumerate(("vp", "vs", "rho")):
+            _lib.call("hmc_gemm", _lib.HMC_F32, cells, C, nb, 1.0, p["B"].data_ptr(), M[f * nb:(f + 1) * nb].data_ptr(),
+                      p["bg"][f].data_ptr(), ws[name].data_ptr(), 0, stream)
+
+    def _forward_all(self, M, ws, stream, store_and_adjoint):
+        import ctypes
+
+        cfg = self.config
+        C = M.shape[1]
+        d = self._descriptor(ws, C)
+        ref = ctypes.byref(d)
+        self._set_model(M, ws, stream)
+        _lib.call("hmc_fwi_prepare", ref, stream)
+        if store_and_adjoint:
+            _lib.call("hmc_fwi_zero_gradients", ref, stream)
+        for k, (sx, sz) in enumerate(cfg.src):
+            _lib.call("hmc_fwi_forward_shot", ref, k, sx, sz, int(store_and_adjoint), stream)
+            if store_and_adjoint:
+                _lib.call("hmc_fwi_adjoint_shot", ref, k, stream)
+        return d
+
+    def _check_dtype(self, dtype):
+        if dtype != "float32":
+            raise NotImplementedError("the elastic finite-difference kernels run in FP32 (float32 chains)")
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        import ctypes
+
+        self._check_dtype(dtype)
+        ws = self._workspace(M.shape[1], M.device, False)
+        d = self._forward_all(M, ws, stream, False)
+        _lib.call("hmc_fwi_misfit", ctypes.byref(d), self.config.n_shots, out.data_ptr(), int(accumulate), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        import ctypes
+
+        self._check_dtype(dtype)
+        C = M.shape[1]
+        ws = self._workspace(C, M.device, True)
+        d = self._forward_all(M, ws, stream, True)
+        _lib.call("hmc_fwi_param_gradient", ctypes.byref(d), ws["g_rho"].data_ptr(), ws["g_vp"].data_ptr(),
+                  ws["g_vs"].data_ptr(), 0, stream)
+        p = self._params("float32")
+        nb = self.blob.n_blobs
+        cells = self.config.nzc * self.config.nxc
+        for f, name in enumerate(("g_vp", "g_vs", "g_rho")):
+            dst = out[f * nb:(f + 1) * nb]
+            if self.gradient_projection == "least_squares":
+                _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(), None,
+                          ws["gtmp"].data_ptr(), 0, stream)
+                _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, nb, 1.0, p["proj"].data_ptr(), ws["gtmp"].data_ptr(),
+                          None, dst.data_ptr(), int(accumulate), stream)
+            else:
+                _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(), None,
+                          dst.data_ptr(), int(accumulate), stream)
+
+    def last_misfit(self, C, out, stream=None):
+        """Misfit of the model of the last gradient call (its forward records
+        are still in the workspace)."""
+        import ctypes
+
+        ws = self._workspace(C, out.device, False)
+        d = self._descriptor(ws, C)
+        _lib.call("hmc_fwi_misfit", ctypes.byref(d), self.config.n_shots, out.data_ptr(), 0,
+                  _dev.stream_handle(stream))
+
+    def get_model_vector(self):
+        return _numpy.zeros((self.dimensions, 1))
+
+    @staticmethod
+    def create_default(dimensions: int, ini_file=None, omp_threads_override: int = 0):
+        raise _InvalidCaseError("construct ElasticFullWaveform2D from an hmclab_gb300.fwi.ElasticConfig")

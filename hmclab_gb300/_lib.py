@@ -87,6 +87,24 @@ class HmcChains(_ct.Structure):
     ]
 
 
+class HmcFwi(_ct.Structure):
+    """Mirror of `hmc_fwi` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("nx", c_int32),
+        ("nz", c_int32),
+        ("nt", c_int32),
+        ("nrec", c_int32),
+        ("chains", c_int64),
+        ("h", _ct.c_float),
+        ("dt", _ct.c_float),
+        ("w", _ct.c_float),
+    ] + [(n, c_void_p) for n in (
+        "taper", "stf_host", "rec_map", "rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx",
+        "szz", "sxz", "store", "rec", "obs", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz",
+        "g_l2m", "g_lam", "g_muxz")]
+
+
 P = c_void_p
 I = c_int
 I64 = c_int64
@@ -127,6 +145,12 @@ SIGNATURES = {
     "hmc_tc_step": [P, P, P, I64, P, P, P, P, I64, P, P, I, P, P, D, D, P, S],
     "hmc_tc_resid_misfit": [I64, I64, I64, P, P, I64, P, P, I64, P, P, P, P, I, P, S],
     "hmc_tc_partials_size": [I64, I64],
+    "hmc_fwi_prepare": [P, S],
+    "hmc_fwi_forward_shot": [P, I, I, I, I, S],
+    "hmc_fwi_misfit": [P, I, P, I, S],
+    "hmc_fwi_zero_gradients": [P, S],
+    "hmc_fwi_adjoint_shot": [P, I, S],
+    "hmc_fwi_param_gradient": [P, P, P, P, I, S],
     "hmc_ess": [I, I64, I64, I64, P, I, P, P, P, S],
     "hmc_ess_work_size": [I64, I64, I],
     "hmc_moments": [I, I64, I64, I64, P, P, P, S],

@@ -1,0 +1,417 @@
+// 2-D elastic P-SV finite differences for many chains at once, FP32: forward
+// simulation, L2 waveform misfit, exact discrete adjoint and parameter
+// gradients.  Replaces the psvWave calls of the reference
+// (hmclab/Distributions/ElasticFullWaveform2D.py:138-184: forward_simulate,
+// calculate_l2_misfit, calculate_l2_adjoint_sources, adjoint_simulate,
+// map_kernels_to_velocity), restated from Virieux (1986) / Levander (1988)
+// with a Cerjan et al. (1985) sponge.
+//
+// Layout: every field is [nz][nx][C] (chain fastest), so each warp reads 32
+// chains of one cell in one 128-byte transaction and the stencil neighbours
+// of a block stay in L1/L2; one shot is simulated at a time so that the
+// fields and parameters of all chains (about 86 MB at 240 x 140 x 64) stay in
+// L2 for the 2 x nt half-step launches.
+//
+// Scheme (identical to the FP64 oracle): on the cells 2 <= i < nx-2,
+// 2 <= j < nz-2 of a zero-padded grid,
+//   velocity:  vx += dt bx (Dx+ sxx + Dz- sxz),  vz += dt bz (Dx- sxz + Dz+ szz),
+//              then taper, record receivers, store (vx, vz) for the adjoint;
+//   stress:    sxx += dt ((l+2m) Dx- vx + l Dz- vz), szz += dt (l Dx- vx + (l+2m) Dz- vz),
+//              sxz += dt muxz (Dz+ vx + Dx+ vz), source into sxx and szz, taper.
+// The adjoint runs the transpose of these maps backwards in time
+// ((Dx+)^T = -Dx-, (Dx-)^T = -Dx+, same in z), accumulating gradients with
+// respect to bx, bz, l+2m, l, muxz, which are then mapped to rho, vp, vs.
+#include "common.cuh"
+
+namespace hmc {
+namespace fwi {
+
+constexpr float C1 = 9.0f / 8.0f;
+constexpr float C2 = -1.0f / 24.0f;
+
+struct Grid {
+  int nx, nz;
+  int64_t C;
+  float inv_h;
+  float dt;
+  __device__ __forceinline__ int64_t at(int j, int i) const { return ((int64_t)j * nx + i) * C; }
+  __device__ __forceinline__ bool valid(int i, int j) const { return i >= 2 && i < nx - 2 && j >= 2 && j < nz - 2; }
+};
+
+// Fourth-order staggered differences of field f at cell (j, i) for chain c
+// (offsets in units of cells; sx = C, sz = nx*C).
+__device__ __forceinline__ float dxp(const float* f, int64_t k, int64_t sx, float ih) {
+  return (C1 * (f[k + sx] - f[k]) + C2 * (f[k + 2 * sx] - f[k - sx])) * ih;
+}
+__device__ __forceinline__ float dxm(const float* f, int64_t k, int64_t sx, float ih) {
+  return (C1 * (f[k] - f[k - sx]) + C2 * (f[k + sx] - f[k - 2 * sx])) * ih;
+}
+
+template <typename F>
+__device__ __forceinline__ void for_cells(const Grid& g, F&& fn) {
+  const int64_t total = (int64_t)g.nx * g.nz * g.C;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t % g.C, cell = t / g.C;
+    const int i = (int)(cell % g.nx), j = (int)(cell / g.nx);
+    fn(i, j, c, t);
+  }
+}
+
+__global__ void derive_params_kernel(Grid g, const float* __restrict__ rho, const float* __restrict__ vp,
+                                     const float* __restrict__ vs, float* bx, float* bz, float* l2m, float* lam,
+                                     float* muxz) {
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    const int i1 = i + 1 < g.nx ? i + 1 : i, j1 = j + 1 < g.nz ? j + 1 : j;
+    const int64_t kx = g.at(j, i1) + c, kz = g.at(j1, i) + c, kxz = g.at(j1, i1) + c;
+    const float r = rho[k], p = vp[k], s = vs[k];
+    const float mu = r * s * s;
+    lam[k] = r * (p * p - 2.f * s * s);
+    l2m[k] = lam[k] + 2.f * mu;
+    bx[k] = 0.5f * (1.f / r + 1.f / rho[kx]);
+    bz[k] = 0.5f * (1.f / r + 1.f / rho[kz]);
+    muxz[k] = 0.25f * (mu + rho[kx] * vs[kx] * vs[kx] + rho[kz] * vs[kz] * vs[kz] + rho[kxz] * vs[kxz] * vs[kxz]);
+  });
+}
+
+struct Fields {
+  float *vx, *vz, *sxx, *szz, *sxz;
+};
+struct Params {
+  const float *bx, *bz, *l2m, *lam, *muxz;
+};
+
+__global__ void velocity_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
+                                const int32_t* __restrict__ rec_map, int nrec, float* rec_n, float* store_n) {
+  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C;
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    float vx = f.vx[k], vz = f.vz[k];
+    if (g.valid(i, j)) {
+      vx += g.dt * p.bx[k] * (dxp(f.sxx, k, sx, g.inv_h) + dxm(f.sxz, k, sz, g.inv_h));
+      vz += g.dt * p.bz[k] * (dxm(f.sxz, k, sx, g.inv_h) + dxp(f.szz, k, sz, g.inv_h));
+    }
+    const float t = taper[(int64_t)j * g.nx + i];
+    vx *= t;
+    vz *= t;
+    f.vx[k] = vx;
+    f.vz[k] = vz;
+    const int r = rec_map[(int64_t)j * g.nx + i];
+    if (r >= 0) {
+      rec_n[((int64_t)r * 2 + 0) * g.C + c] = vx;
+      rec_n[((int64_t)r * 2 + 1) * g.C + c] = vz;
+    }
+    if (store_n) {
+      store_n[k] = vx;
+      store_n[(int64_t)g.nx * g.nz * g.C + k] = vz;
+    }
+  });
+}
+
+__global__ void stress_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper, int src_i, int src_j,
+                              float src_value) {
+  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C;
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    float sxx = f.sxx[k], szz = f.szz[k], sxz = f.sxz[k];
+    if (g.valid(i, j)) {
+      const float exx = dxm(f.vx, k, sx, g.inv_h), ezz = dxm(f.vz, k, sz, g.inv_h);
+      sxx += g.dt * (p.l2m[k] * exx + p.lam[k] * ezz);
+      szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
+      sxz += g.dt * p.muxz[k] * (dxp(f.vx, k, sz, g.inv_h) + dxp(f.vz, k, sx, g.inv_h));
+    }
+    if (i == src_i && j == src_j) {
+      sxx += src_value;
+      szz += src_value;
+    }
+    const float t = taper[(int64_t)j * g.nx + i];
+    f.sxx[k] = sxx * t;
+    f.szz[k] = szz * t;
+    f.sxz[k] = sxz * t;
+  });
+}
+
+// ---- adjoint ---------------------------------------------------------------
+struct Grads {
+  float *bx, *bz, *l2m, *lam, *muxz;
+};
+
+// Adjoint velocity pass of step n (reverse of stress step 4, receivers 3,
+// taper 2, and the buoyancy gradient of velocity step 1).  The adjoint
+// stresses are already multiplied by the taper of step n.
+__global__ void adj_velocity_kernel(Grid g, Fields a, Params p, Grads gr, const float* __restrict__ taper,
+                                    const int32_t* __restrict__ rec_map, const float* __restrict__ resid_n,
+                                    const float* __restrict__ vn, const float* __restrict__ vprev) {
+  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C, plane = (int64_t)g.nx * g.nz * g.C;
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    if (!g.valid(i, j)) return;
+    // t1 = dt (l2m asxx + lam aszz), t2 = dt (lam asxx + l2m aszz), t3 = dt muxz asxz,
+    // zero outside the valid cells.
+    auto t1 = [&](int ii, int jj) {
+      if (!g.valid(ii, jj)) return 0.f;
+      const int64_t q = g.at(jj, ii) + c;
+      return g.dt * (p.l2m[q] * a.sxx[q] + p.lam[q] * a.szz[q]);
+    };
+    auto t2 = [&](int ii, int jj) {
+      if (!g.valid(ii, jj)) return 0.f;
+      const int64_t q = g.at(jj, ii) + c;
+      return g.dt * (p.lam[q] * a.sxx[q] + p.l2m[q] * a.szz[q]);
+    };
+    auto t3 = [&](int ii, int jj) {
+      if (!g.valid(ii, jj)) return 0.f;
+      const int64_t q = g.at(jj, ii) + c;
+      return g.dt * p.muxz[q] * a.sxz[q];
+    };
+    const float ih = g.inv_h;
+    // -Dx+ t1 - Dz- t3  and  -Dz+ t2 - Dx- t3
+    const float dxp_t1 = (C1 * (t1(i + 1, j) - t1(i, j)) + C2 * (t1(i + 2, j) - t1(i - 1, j))) * ih;
+    const float dzm_t3 = (C1 * (t3(i, j) - t3(i, j - 1)) + C2 * (t3(i, j + 1) - t3(i, j - 2))) * ih;
+    const float dzp_t2 = (C1 * (t2(i, j + 1) - t2(i, j)) + C2 * (t2(i, j + 2) - t2(i, j - 1))) * ih;
+    const float dxm_t3 = (C1 * (t3(i, j) - t3(i - 1, j)) + C2 * (t3(i + 1, j) - t3(i - 2, j))) * ih;
+    float ax = a.vx[k] - dxp_t1 - dzm_t3;
+    float az = a.vz[k] - dzp_t2 - dxm_t3;
+    // stiffness gradients: strains of the stored forward velocities at step n
+    const float* vxn = vn;
+    const float* vzn = vn + plane;
+    const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
+    const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
+    const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
+    gr.l2m[k] += g.dt * (exx * asxx + ezz * aszz);
+    gr.lam[k] += g.dt * (ezz * asxx + exx * aszz);
+    gr.muxz[k] += g.dt * exz * asxz;
+    // adjoint sources (residuals already weighted)
+    const int r = rec_map[(int64_t)j * g.nx + i];
+    if (r >= 0) {
+      ax += resid_n[((int64_t)r * 2 + 0) * g.C + c];
+      az += resid_n[((int64_t)r * 2 + 1) * g.C + c];
+    }
+    const float tp = taper[(int64_t)j * g.nx + i];
+    ax *= tp;
+    az *= tp;
+    a.vx[k] = ax;
+    a.vz[k] = az;
+    // buoyancy gradients: dt * (divergence of stress) = (v' - v_prev) / b
+    const float dvx = vxn[k] / tp - (vprev ? vprev[k] : 0.f);
+    const float dvz = vzn[k] / tp - (vprev ? vprev[plane + k] : 0.f);
+    gr.bx[k] += dvx / p.bx[k] * ax;
+    gr.bz[k] += dvz / p.bz[k] * az;
+  });
+}
+
+// Adjoint stress pass of step n (reverse of velocity step 1), followed by the
+// taper of step n-1 (reverse of its stress taper).
+__global__ void adj_stress_kernel(Grid g, Fields a, Params p, const float* __restrict__ taper) {
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    if (!g.valid(i, j)) return;
+    auto t4 = [&](int ii, int jj) {
+      if (!g.valid(ii, jj)) return 0.f;
+      const int64_t q = g.at(jj, ii) + c;
+      return g.dt * p.bx[q] * a.vx[q];
+    };
+    auto t5 = [&](int ii, int jj) {
+      if (!g.valid(ii, jj)) return 0.f;
+      const int64_t q = g.at(jj, ii) + c;
+      return g.dt * p.bz[q] * a.vz[q];
+    };
+    const float ih = g.inv_h;
+    const float dxm_t4 = (C1 * (t4(i, j) - t4(i - 1, j)) + C2 * (t4(i + 1, j) - t4(i - 2, j))) * ih;
+    const float dzp_t4 = (C1 * (t4(i, j + 1) - t4(i, j)) + C2 * (t4(i, j + 2) - t4(i, j - 1))) * ih;
+    const float dxp_t5 = (C1 * (t5(i + 1, j) - t5(i, j)) + C2 * (t5(i + 2, j) - t5(i - 1, j))) * ih;
+    const float dzm_t5 = (C1 * (t5(i, j) - t5(i, j - 1)) + C2 * (t5(i, j + 1) - t5(i, j - 2))) * ih;
+    const float tp = taper[(int64_t)j * g.nx + i];
+    a.sxx[k] = (a.sxx[k] - dxm_t4) * tp;
+    a.sxz[k] = (a.sxz[k] - dzp_t4 - dxp_t5) * tp;
+    a.szz[k] = (a.szz[k] - dzm_t5) * tp;
+  });
+}
+
+// Weighted residuals w (rec - obs) of one shot, all steps: [nt][nrec][2][C];
+// obs is shared by all chains: [nt][nrec][2].  Also the FP64 misfit partials.
+__global__ void residual_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec,
+                                const float* __restrict__ obs, float w, float* resid) {
+  const int64_t total = n_rows * C;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+    resid[t] = w * (rec[t] - obs[t / C]);
+}
+
+__global__ void misfit_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec, const float* __restrict__ obs,
+                              double w, double* out, int accumulate) {
+  __shared__ double sh[RED_Y][RED_X + 1];
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  double acc = 0.0;
+  if (c < C) {
+    for (int64_t r = threadIdx.y; r < n_rows; r += RED_Y) {
+      const double d = (double)rec[r * C + c] - (double)obs[r];
+      acc += d * d;
+    }
+  }
+  const double s = block_chain_sum(acc, sh);
+  if (c < C && threadIdx.y == 0) {
+    const double v = 0.5 * w * s;
+    out[c] = accumulate ? out[c] + v : v;
+  }
+}
+
+// (bx, bz, l+2m, l, muxz) gradients -> (rho, vp, vs) gradients, all cells.
+__global__ void param_gradient_kernel(Grid g, Grads gr, const float* __restrict__ rho, const float* __restrict__ vp,
+                                      const float* __restrict__ vs, float* g_rho, float* g_vp, float* g_vs,
+                                      int accumulate) {
+  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
+    float gl = gr.lam[k] + gr.l2m[k];
+    float gm = 2.f * gr.l2m[k];
+    float gb = 0.5f * gr.bx[k] + 0.5f * gr.bz[k];
+    if (i > 0) gb += 0.5f * gr.bx[g.at(j, i - 1) + c];
+    if (j > 0) gb += 0.5f * gr.bz[g.at(j - 1, i) + c];
+    float gmu = 0.25f * gr.muxz[k];
+    if (i > 0) gmu += 0.25f * gr.muxz[g.at(j, i - 1) + c];
+    if (j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i) + c];
+    if (i > 0 && j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i - 1) + c];
+    gm += gmu;
+    const float r = rho[k], p = vp[k], s = vs[k];
+    const float vgp = gl * 2.f * r * p;
+    const float vgs = gl * (-4.f * r * s) + gm * 2.f * r * s;
+    const float vgr = gl * (p * p - 2.f * s * s) + gm * s * s - gb / (r * r);
+    if (accumulate) {
+      g_vp[k] += vgp;
+      g_vs[k] += vgs;
+      g_rho[k] += vgr;
+    } else {
+      g_vp[k] = vgp;
+      g_vs[k] = vgs;
+      g_rho[k] = vgr;
+    }
+  });
+}
+
+inline unsigned grid_for(int64_t n) {
+  const unsigned b = blocks_for(n, 256);
+  return b > 152u * 64u ? 152u * 64u : b;
+}
+
+}  // namespace fwi
+}  // namespace hmc
+
+using namespace hmc;
+using namespace hmc::fwi;
+
+static int check_fwi(const hmc_fwi* s, const char* who) {
+  HMC_REQUIRE(s != nullptr, "%s: null descriptor", who);
+  HMC_REQUIRE(s->nx >= 5 && s->nz >= 5 && s->nt > 0 && s->chains > 0 && s->nrec > 0, "%s: bad sizes", who);
+  HMC_REQUIRE(s->taper && s->stf_host && s->rec_map && s->rho && s->vp && s->vs, "%s: missing model buffer", who);
+  HMC_REQUIRE(s->bx && s->bz && s->l2m && s->lam && s->muxz, "%s: missing parameter work buffer", who);
+  HMC_REQUIRE(s->vx && s->vz && s->sxx && s->szz && s->sxz && s->rec, "%s: missing wavefield buffer", who);
+  return HMC_OK;
+}
+
+static Grid grid_of(const hmc_fwi* s) {
+  Grid g;
+  g.nx = s->nx;
+  g.nz = s->nz;
+  g.C = s->chains;
+  g.inv_h = 1.f / s->h;
+  g.dt = s->dt;
+  return g;
+}
+
+extern "C" {
+
+HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_prepare"));
+  const Grid g = grid_of(s);
+  derive_params_kernel<<<grid_for((int64_t)s->nx * s->nz * s->chains), 256, 0, as_stream(stream)>>>(
+      g, s->rho, s->vp, s->vs, s->bx, s->bz, s->l2m, s->lam, s->muxz);
+  return check_launch("derive_params_kernel");
+}
+
+HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_z, int store, void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_forward_shot"));
+  HMC_REQUIRE(src_x >= 0 && src_x < s->nx && src_z >= 0 && src_z < s->nz, "hmc_fwi_forward_shot: source off grid");
+  HMC_REQUIRE(!store || s->store, "hmc_fwi_forward_shot: storing needs the store buffer");
+  cudaStream_t st = as_stream(stream);
+  const Grid g = grid_of(s);
+  const int64_t cells = (int64_t)s->nx * s->nz * s->chains;
+  const size_t fb = (size_t)cells * sizeof(float);
+  // zero the wavefields
+  for (float* f : {s->vx, s->vz, s->sxx, s->szz, s->sxz}) {
+    cudaError_t e = cudaMemsetAsync(f, 0, fb, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fwi fields)");
+  }
+  Fields f{s->vx, s->vz, s->sxx, s->szz, s->sxz};
+  Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
+  const unsigned grid = grid_for(cells);
+  const float src_scale = s->dt / (s->h * s->h);
+  float* rec_shot = s->rec + (int64_t)shot * s->nt * s->nrec * 2 * s->chains;
+  // the source wavelet is read on the host: it is a handful of floats per step
+  for (int n = 0; n < s->nt; ++n) {
+    float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
+    float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
+    velocity_kernel<<<grid, 256, 0, st>>>(g, f, p, s->taper, s->rec_map, s->nrec, rec_n, store_n);
+    HMC_TRY(check_launch("velocity_kernel"));
+    stress_kernel<<<grid, 256, 0, st>>>(g, f, p, s->taper, src_x, src_z, s->stf_host[n] * src_scale);
+    HMC_TRY(check_launch("stress_kernel"));
+  }
+  return HMC_OK;
+}
+
+HMC_API int hmc_fwi_misfit(const hmc_fwi* s, int nshots, double* out_x, int accumulate, void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_misfit"));
+  HMC_REQUIRE(s->obs && out_x, "hmc_fwi_misfit: missing observations or output");
+  const int64_t rows = (int64_t)nshots * s->nt * s->nrec * 2;
+  misfit_kernel<<<red_grid(s->chains), red_block(), 0, as_stream(stream)>>>(rows, s->chains, s->rec, s->obs,
+                                                                           (double)s->w, out_x, accumulate);
+  return check_launch("fwi misfit_kernel");
+}
+
+HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_adjoint_shot"));
+  HMC_REQUIRE(s->store && s->obs && s->resid && s->avx && s->avz && s->asxx && s->aszz && s->asxz,
+              "hmc_fwi_adjoint_shot: missing adjoint buffer");
+  HMC_REQUIRE(s->g_bx && s->g_bz && s->g_l2m && s->g_lam && s->g_muxz, "hmc_fwi_adjoint_shot: missing gradients");
+  cudaStream_t st = as_stream(stream);
+  const Grid g = grid_of(s);
+  const int64_t cells = (int64_t)s->nx * s->nz * s->chains;
+  const size_t fb = (size_t)cells * sizeof(float);
+  for (float* f : {s->avx, s->avz, s->asxx, s->aszz, s->asxz}) {
+    cudaError_t e = cudaMemsetAsync(f, 0, fb, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fwi adjoint)");
+  }
+  const int64_t rows = (int64_t)s->nt * s->nrec * 2;
+  const int64_t shot_off = (int64_t)shot * rows;
+  residual_kernel<<<grid_for(rows * s->chains), 256, 0, st>>>(rows, s->chains, s->rec + shot_off * s->chains,
+                                                              s->obs + shot_off, s->w, s->resid);
+  HMC_TRY(check_launch("residual_kernel"));
+  Fields a{s->avx, s->avz, s->asxx, s->aszz, s->asxz};
+  Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
+  Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
+  const unsigned grid = grid_for(cells);
+  for (int n = s->nt - 1; n >= 0; --n) {
+    const float* vn = s->store + (int64_t)n * 2 * cells;
+    const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
+    adj_velocity_kernel<<<grid, 256, 0, st>>>(g, a, p, gr, s->taper, s->rec_map,
+                                              s->resid + (int64_t)n * s->nrec * 2 * s->chains, vn, vp);
+    HMC_TRY(check_launch("adj_velocity_kernel"));
+    adj_stress_kernel<<<grid, 256, 0, st>>>(g, a, p, s->taper);
+    HMC_TRY(check_launch("adj_stress_kernel"));
+  }
+  return HMC_OK;
+}
+
+HMC_API int hmc_fwi_zero_gradients(const hmc_fwi* s, void* stream) {
+  HMC_REQUIRE(s && s->g_bx && s->g_bz && s->g_l2m && s->g_lam && s->g_muxz, "hmc_fwi_zero_gradients: missing buffer");
+  const size_t fb = (size_t)s->nx * s->nz * s->chains * sizeof(float);
+  for (float* f : {s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz}) {
+    cudaError_t e = cudaMemsetAsync(f, 0, fb, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fwi gradients)");
+  }
+  return HMC_OK;
+}
+
+HMC_API int hmc_fwi_param_gradient(const hmc_fwi* s, float* g_rho, float* g_vp, float* g_vs, int accumulate,
+                                   void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_param_gradient"));
+  HMC_REQUIRE(g_rho && g_vp && g_vs, "hmc_fwi_param_gradient: null output");
+  const Grid g = grid_of(s);
+  Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
+  param_gradient_kernel<<<grid_for((int64_t)s->nx * s->nz * s->chains), 256, 0, as_stream(stream)>>>(
+      g, gr, s->rho, s->vp, s->vs, g_rho, g_vp, g_vs, accumulate);
+  return check_launch("param_gradient_kernel");
+}
+
+}  // extern "C"

@@ -312,6 +312,68 @@ HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C,
                                 int* status, void* stream);
 HMC_API int64_t hmc_tc_partials_size(int64_t n, int64_t C);
 
+/* ---- 2-D elastic P-SV full-waveform misfit and gradient ------------------
+ * Replaces psvWave's forward_simulate / calculate_l2_misfit / adjoint_simulate
+ * / map_kernels_to_velocity as called by ElasticFullWaveform2D.misfit and
+ * .gradient (ElasticFullWaveform2D.py:138-184): FP32 fourth-order staggered
+ * velocity-stress finite differences with a sponge, explosive sources, an L2
+ * waveform misfit and the exact discrete adjoint, for C chains at once.
+ * Every field is [nz][nx][C] (chain fastest); one shot is run per call.     */
+typedef struct hmc_fwi {
+  int32_t nx, nz, nt, nrec; /* simulation grid, time steps, receivers       */
+  int64_t chains;           /* C                                            */
+  float h, dt;              /* grid spacing, time step                      */
+  float w;                  /* misfit weight 1 / (sigma^2 * temperature)    */
+  const float* taper;       /* [nz][nx] sponge factors                      */
+  const float* stf_host;    /* [nt] source time function, HOST memory       */
+  const int32_t* rec_map;   /* [nz][nx] receiver index of a cell or -1      */
+  const float* rho;         /* [nz][nx][C] model of every chain             */
+  const float* vp;
+  const float* vs;
+  float* bx;                /* [nz][nx][C] derived parameters (work)        */
+  float* bz;
+  float* l2m;
+  float* lam;
+  float* muxz;
+  float* vx;                /* [nz][nx][C] wavefields (work)                */
+  float* vz;
+  float* sxx;
+  float* szz;
+  float* sxz;
+  float* store;             /* [nt][2][nz][nx][C] forward velocities       */
+  float* rec;               /* [shots][nt][nrec][2][C] synthetic records    */
+  const float* obs;         /* [shots][nt][nrec][2] observed records        */
+  float* resid;             /* [nt][nrec][2][C] weighted residuals (work)   */
+  float* avx;               /* [nz][nx][C] adjoint wavefields (work)        */
+  float* avz;
+  float* asxx;
+  float* aszz;
+  float* asxz;
+  float* g_bx;              /* [nz][nx][C] gradient accumulators            */
+  float* g_bz;
+  float* g_l2m;
+  float* g_lam;
+  float* g_muxz;
+} hmc_fwi;
+
+/* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */
+HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream);
+/* One shot with an explosive source at (src_x, src_z); records into
+ * rec[shot]; stores the velocities of every step when store != 0.          */
+HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x,
+                                 int src_z, int store, void* stream);
+/* out_x[c] (+)= 0.5 * w * sum over shots < nshots of (rec - obs)^2, FP64.   */
+HMC_API int hmc_fwi_misfit(const hmc_fwi* s, int nshots, double* out_x,
+                           int accumulate, void* stream);
+HMC_API int hmc_fwi_zero_gradients(const hmc_fwi* s, void* stream);
+/* Adjoint of the shot just simulated with store != 0; accumulates into the
+ * gradient accumulators.                                                   */
+HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream);
+/* Accumulators -> gradients with respect to rho, vp, vs ([nz][nx][C]).     */
+HMC_API int hmc_fwi_param_gradient(const hmc_fwi* s, float* g_rho,
+                                   float* g_vp, float* g_vs, int accumulate,
+                                   void* stream);
+
 /* ---- dense matrix product used by the ops above -------------------------
  * out[m][n] = alpha * A[m][k] B[k][n] + (bias ? bias[m] : 0)
  *             + (accumulate ? out[m][n] : 0), all row-major.                */

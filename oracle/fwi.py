@@ -1,0 +1,68 @@
+"""ctypes wrapper of the FP64 elastic FD oracle (oracle/fwi_oracle.c) —
+TEST INFRASTRUCTURE ONLY.  Arrays are numpy float64 in [z][x] layout."""
+import ctypes
+
+import numpy as np
+
+from oracle import build_oracle
+
+_lib = None
+
+
+class _Shot(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int),
+        ("nz", ctypes.c_int),
+        ("nt", ctypes.c_int),
+        ("h", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("taper", ctypes.c_void_p),
+        ("stf", ctypes.c_void_p),
+        ("src_x", ctypes.c_int),
+        ("src_z", ctypes.c_int),
+        ("nrec", ctypes.c_int),
+        ("rec_x", ctypes.c_void_p),
+        ("rec_z", ctypes.c_void_p),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build_oracle.build())
+        _lib.fwi_forward.restype = ctypes.c_int
+        _lib.fwi_forward.argtypes = [ctypes.c_void_p] * 8
+        _lib.fwi_gradient.restype = ctypes.c_double
+        _lib.fwi_gradient.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_double] + [ctypes.c_void_p] * 3
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Shot:
+    def __init__(self, nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z):
+        self.taper = np.ascontiguousarray(taper, np.float64)
+        self.stf = np.ascontiguousarray(stf, np.float64)
+        self.rec_x = np.ascontiguousarray(rec_x, np.int32)
+        self.rec_z = np.ascontiguousarray(rec_z, np.int32)
+        self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, _p(self.stf).value, int(src[0]), int(src[1]),
+                       len(self.rec_x), _p(self.rec_x).value, _p(self.rec_z).value)
+        self.nt, self.nrec = nt, len(self.rec_x)
+
+    def forward(self, rho, vp, vs):
+        rvx = np.zeros((self.nt, self.nrec))
+        rvz = np.zeros((self.nt, self.nrec))
+        args = [np.ascontiguousarray(a, np.float64) for a in (rho, vp, vs)]
+        rc = lib().fwi_forward(ctypes.byref(self.s), *[_p(a) for a in args], _p(rvx), _p(rvz), None, None)
+        assert rc == 0
+        return rvx, rvz
+
+    def gradient(self, rho, vp, vs, obs_vx, obs_vz, w):
+        args = [np.ascontiguousarray(a, np.float64) for a in (rho, vp, vs)]
+        g = [np.zeros_like(args[0]) for _ in range(3)]
+        chi = lib().fwi_gradient(ctypes.byref(self.s), *[_p(a) for a in args],
+                                 _p(np.ascontiguousarray(obs_vx, np.float64)),
+                                 _p(np.ascontiguousarray(obs_vz, np.float64)), float(w), *[_p(x) for x in g])
+        return chi, g  # g = [g_rho, g_vp, g_vs]
