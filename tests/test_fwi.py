@@ -3,9 +3,8 @@
 oracle (GPU).
 
 Tolerances: oracle gradient vs central differences 1e-6 relative (FP64);
-FP32 device records vs FP64 oracle 2e-5 of the record scale; FP32 device
-gradients vs FP64 oracle 1e-3 of the gradient scale (thousands of FP32
-time steps accumulate round-off in the adjoint correlation)."""
+FP32 device misfits vs the FP64 oracle 2e-5 relative; FP32 device gradients
+vs the FP64 oracle 2e-5 of the gradient scale (measured ~2e-6)."""
 import numpy as np
 import pytest
 
@@ -45,7 +44,7 @@ def test_oracle_adjoint_matches_finite_differences():
     chi, grads = shot.gradient(rho, vp, vs, ovx, ovz, w)
     rng = np.random.default_rng(3)
     for k in range(3):
-        dm = rng.normal(size=vp.shape) * [rho, vp, vs][k] * 1e-3
+        dm = rng.normal(size=vp.shape) * [rho, vp, vs][k] * 1e-5
         args = [rho, vp, vs]
 
         def mis(sign):
@@ -92,16 +91,15 @@ def test_device_fwi_matches_oracle():
         vp, vs, rho = (cfg.extend(f) for f in dist.fine_model(m32))
         chi = 0.0
         gv = [np.zeros_like(vp) for _ in range(3)]
-        rec_scale = 0.0
         for k, s in enumerate(shots):
             ch, gk = s.gradient(rho, vp, vs, obs[k][0], obs[k][1], w)
             chi += ch
             for f in range(3):
                 gv[f] += gk[f]
         # device records of chain c agree with the oracle's
-        np.testing.assert_allclose(x[c], chi, rtol=2e-4)
+        np.testing.assert_allclose(x[c], chi, rtol=2e-5)
         g_ref = np.concatenate([Bs.T @ gv[1].reshape(-1), Bs.T @ gv[2].reshape(-1), Bs.T @ gv[0].reshape(-1)])
         scale = np.abs(g_ref).max()
         err = np.abs(g[:, c] - g_ref).max() / scale
         print(f"chain {c}: misfit {x[c]:.6e} vs oracle {chi:.6e}; gradient max rel err {err:.2e}")
-        assert err < 1e-3
+        assert err < 2e-5
