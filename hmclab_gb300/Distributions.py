@@ -738,7 +738,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         if with_gradient and "store" not in ws:
             z = lambda *shape: torch.zeros(shape, dtype=torch.float32, device=device)  # noqa: E731
             for name in ("avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam", "g_muxz", "g_vp",
-                         "g_vs", "g_rho"):
+                         "g_vs", "g_rho", "t1", "t2", "t3", "t4", "t5"):
                 ws[name] = z(cells, C)
             ws["store"] = z(cfg.nt * 2 * cells * C)
             ws["resid"] = z(cfg.nt * cfg.n_rec * 2 * C)
@@ -757,7 +757,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec"):
             setattr(d, name, ws[name].data_ptr())
         for name in ("store", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam",
-                     "g_muxz"):
+                     "g_muxz", "t1", "t2", "t3", "t4", "t5"):
             if name in ws:
                 setattr(d, name, ws[name].data_ptr())
         return d
@@ -771,6 +771,35 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             _lib.call("hmc_gemm", _lib.HMC_F32, cells, C, nb, 1.0, p["B"].data_ptr(), M[f * nb:(f + 1) * nb].data_ptr(),
                       p["bg"][f].data_ptr(), ws[name].data_ptr(), 0, stream)
 
+    def _shot_graph(self, ws, C, shot, store_and_adjoint):
+        """CUDA graph of one shot's 2*nt half-step launches (and its adjoint),
+        captured once per workspace on a private stream and replayed on the
+        caller's stream."""
+        import ctypes
+
+        import torch
+
+        graphs = ws.setdefault("graphs", {})
+        key = (shot, bool(store_and_adjoint), float(self.weight))
+        if key not in graphs:
+            d = self._descriptor(ws, C)
+            ws.setdefault("descriptors", []).append(d)  # keep the struct alive with the graph
+            ref = ctypes.byref(d)
+            sx, sz = self.config.src[shot]
+            cap = torch.cuda.Stream()
+            h = cap.cuda_stream
+            _lib.call("hmc_graph_begin", h)
+            try:
+                _lib.call("hmc_fwi_forward_shot", ref, shot, sx, sz, int(store_and_adjoint), h)
+                if store_and_adjoint:
+                    _lib.call("hmc_fwi_adjoint_shot", ref, shot, h)
+            finally:
+                ex = ctypes.c_void_p()
+                rc = _lib.load().hmc_graph_end(h, ctypes.byref(ex))
+            _lib.check(rc, "hmc_graph_end")
+            graphs[key] = ex
+        return graphs[key]
+
     def _forward_all(self, M, ws, stream, store_and_adjoint):
         import ctypes
 
@@ -782,10 +811,8 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         _lib.call("hmc_fwi_prepare", ref, stream)
         if store_and_adjoint:
             _lib.call("hmc_fwi_zero_gradients", ref, stream)
-        for k, (sx, sz) in enumerate(cfg.src):
-            _lib.call("hmc_fwi_forward_shot", ref, k, sx, sz, int(store_and_adjoint), stream)
-            if store_and_adjoint:
-                _lib.call("hmc_fwi_adjoint_shot", ref, k, stream)
+        for k in range(cfg.n_shots):
+            _lib.call("hmc_graph_launch", self._shot_graph(ws, C, k, store_and_adjoint), stream)
         return d
 
     def _check_dtype(self, dtype):

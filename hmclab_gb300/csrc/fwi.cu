@@ -31,46 +31,58 @@ constexpr float C2 = -1.0f / 24.0f;
 
 struct Grid {
   int nx, nz;
-  int64_t C;
+  int C;
   float inv_h;
   float dt;
-  __device__ __forceinline__ int64_t at(int j, int i) const { return ((int64_t)j * nx + i) * C; }
+  __device__ __forceinline__ int at(int j, int i) const { return (j * nx + i) * C; }
   __device__ __forceinline__ bool valid(int i, int j) const { return i >= 2 && i < nx - 2 && j >= 2 && j < nz - 2; }
 };
 
-// Fourth-order staggered differences of field f at cell (j, i) for chain c
-// (offsets in units of cells; sx = C, sz = nx*C).
-__device__ __forceinline__ float dxp(const float* f, int64_t k, int64_t sx, float ih) {
-  return (C1 * (f[k + sx] - f[k]) + C2 * (f[k + 2 * sx] - f[k - sx])) * ih;
+// Fourth-order staggered differences of field f around flat index k with
+// stride s (C along x, nx*C along z).
+__device__ __forceinline__ float dxp(const float* __restrict__ f, int k, int s, float ih) {
+  return (C1 * (f[k + s] - f[k]) + C2 * (f[k + 2 * s] - f[k - s])) * ih;
 }
-__device__ __forceinline__ float dxm(const float* f, int64_t k, int64_t sx, float ih) {
-  return (C1 * (f[k] - f[k - sx]) + C2 * (f[k + sx] - f[k - 2 * sx])) * ih;
+__device__ __forceinline__ float dxm(const float* __restrict__ f, int k, int s, float ih) {
+  return (C1 * (f[k] - f[k - s]) + C2 * (f[k + s] - f[k - 2 * s])) * ih;
 }
 
-template <typename F>
-__device__ __forceinline__ void for_cells(const Grid& g, F&& fn) {
-  const int64_t total = (int64_t)g.nx * g.nz * g.C;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = t % g.C, cell = t / g.C;
-    const int i = (int)(cell % g.nx), j = (int)(cell / g.nx);
-    fn(i, j, c, t);
-  }
+// Thread mapping: block (32 chains, 8 cells along x), grid.x over (x tiles,
+// chain tiles), grid.y = row j.  No integer division per thread.
+constexpr int TX = 32, TY = 8;
+struct Cell {
+  int i, j, c, k;
+  bool in;
+};
+__device__ __forceinline__ Cell cell_of(const Grid& g) {
+  const int ctiles = (g.C + TX - 1) / TX;
+  const int it = blockIdx.x / ctiles, ct = blockIdx.x - it * ctiles;
+  Cell e;
+  e.c = ct * TX + threadIdx.x;
+  e.i = it * TY + threadIdx.y;
+  e.j = blockIdx.y;
+  e.in = e.c < g.C && e.i < g.nx;
+  e.k = e.in ? g.at(e.j, e.i) + e.c : 0;
+  return e;
+}
+inline dim3 cell_grid(int nx, int nz, int64_t C) {
+  return dim3((unsigned)(((nx + TY - 1) / TY) * ((C + TX - 1) / TX)), (unsigned)nz);
 }
 
 __global__ void derive_params_kernel(Grid g, const float* __restrict__ rho, const float* __restrict__ vp,
                                      const float* __restrict__ vs, float* bx, float* bz, float* l2m, float* lam,
                                      float* muxz) {
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    const int i1 = i + 1 < g.nx ? i + 1 : i, j1 = j + 1 < g.nz ? j + 1 : j;
-    const int64_t kx = g.at(j, i1) + c, kz = g.at(j1, i) + c, kxz = g.at(j1, i1) + c;
-    const float r = rho[k], p = vp[k], s = vs[k];
-    const float mu = r * s * s;
-    lam[k] = r * (p * p - 2.f * s * s);
-    l2m[k] = lam[k] + 2.f * mu;
-    bx[k] = 0.5f * (1.f / r + 1.f / rho[kx]);
-    bz[k] = 0.5f * (1.f / r + 1.f / rho[kz]);
-    muxz[k] = 0.25f * (mu + rho[kx] * vs[kx] * vs[kx] + rho[kz] * vs[kz] * vs[kz] + rho[kxz] * vs[kxz] * vs[kxz]);
-  });
+  const Cell e = cell_of(g);
+  if (!e.in) return;
+  const int i1 = e.i + 1 < g.nx ? e.i + 1 : e.i, j1 = e.j + 1 < g.nz ? e.j + 1 : e.j;
+  const int k = e.k, kx = g.at(e.j, i1) + e.c, kz = g.at(j1, e.i) + e.c, kxz = g.at(j1, i1) + e.c;
+  const float r = rho[k], p = vp[k], s = vs[k];
+  const float mu = r * s * s;
+  lam[k] = r * (p * p - 2.f * s * s);
+  l2m[k] = lam[k] + 2.f * mu;
+  bx[k] = 0.5f * (1.f / r + 1.f / rho[kx]);
+  bz[k] = 0.5f * (1.f / r + 1.f / rho[kz]);
+  muxz[k] = 0.25f * (mu + rho[kx] * vs[kx] * vs[kx] + rho[kz] * vs[kz] * vs[kz] + rho[kxz] * vs[kxz] * vs[kxz]);
 }
 
 struct Fields {
@@ -80,150 +92,132 @@ struct Params {
   const float *bx, *bz, *l2m, *lam, *muxz;
 };
 
-__global__ void velocity_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
-                                const int32_t* __restrict__ rec_map, int nrec, float* rec_n, float* store_n) {
-  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C;
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    float vx = f.vx[k], vz = f.vz[k];
-    if (g.valid(i, j)) {
-      vx += g.dt * p.bx[k] * (dxp(f.sxx, k, sx, g.inv_h) + dxm(f.sxz, k, sz, g.inv_h));
-      vz += g.dt * p.bz[k] * (dxm(f.sxz, k, sx, g.inv_h) + dxp(f.szz, k, sz, g.inv_h));
-    }
-    const float t = taper[(int64_t)j * g.nx + i];
-    vx *= t;
-    vz *= t;
-    f.vx[k] = vx;
-    f.vz[k] = vz;
-    const int r = rec_map[(int64_t)j * g.nx + i];
-    if (r >= 0) {
-      rec_n[((int64_t)r * 2 + 0) * g.C + c] = vx;
-      rec_n[((int64_t)r * 2 + 1) * g.C + c] = vz;
-    }
-    if (store_n) {
-      store_n[k] = vx;
-      store_n[(int64_t)g.nx * g.nz * g.C + k] = vz;
-    }
-  });
+__global__ void __launch_bounds__(TX* TY) velocity_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
+                                                            const int32_t* __restrict__ rec_map, float* rec_n,
+                                                            float* store_n) {
+  const Cell e = cell_of(g);
+  if (!e.in) return;
+  const int k = e.k, sx = g.C, sz = g.nx * g.C;
+  float vx = f.vx[k], vz = f.vz[k];
+  if (g.valid(e.i, e.j)) {
+    vx += g.dt * p.bx[k] * (dxp(f.sxx, k, sx, g.inv_h) + dxm(f.sxz, k, sz, g.inv_h));
+    vz += g.dt * p.bz[k] * (dxm(f.sxz, k, sx, g.inv_h) + dxp(f.szz, k, sz, g.inv_h));
+  }
+  const int cell = e.j * g.nx + e.i;
+  const float t = taper[cell];
+  vx *= t;
+  vz *= t;
+  f.vx[k] = vx;
+  f.vz[k] = vz;
+  const int r = rec_map[cell];
+  if (r >= 0) {
+    rec_n[(r * 2 + 0) * g.C + e.c] = vx;
+    rec_n[(r * 2 + 1) * g.C + e.c] = vz;
+  }
+  if (store_n) {
+    store_n[k] = vx;
+    store_n[g.nx * g.nz * g.C + k] = vz;
+  }
 }
 
-__global__ void stress_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper, int src_i, int src_j,
-                              float src_value) {
-  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C;
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    float sxx = f.sxx[k], szz = f.szz[k], sxz = f.sxz[k];
-    if (g.valid(i, j)) {
-      const float exx = dxm(f.vx, k, sx, g.inv_h), ezz = dxm(f.vz, k, sz, g.inv_h);
-      sxx += g.dt * (p.l2m[k] * exx + p.lam[k] * ezz);
-      szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
-      sxz += g.dt * p.muxz[k] * (dxp(f.vx, k, sz, g.inv_h) + dxp(f.vz, k, sx, g.inv_h));
-    }
-    if (i == src_i && j == src_j) {
-      sxx += src_value;
-      szz += src_value;
-    }
-    const float t = taper[(int64_t)j * g.nx + i];
-    f.sxx[k] = sxx * t;
-    f.szz[k] = szz * t;
-    f.sxz[k] = sxz * t;
-  });
+__global__ void __launch_bounds__(TX* TY) stress_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
+                                                          int src_i, int src_j, float src_value) {
+  const Cell e = cell_of(g);
+  if (!e.in) return;
+  const int k = e.k, sx = g.C, sz = g.nx * g.C;
+  float sxx = f.sxx[k], szz = f.szz[k], sxz = f.sxz[k];
+  if (g.valid(e.i, e.j)) {
+    const float exx = dxm(f.vx, k, sx, g.inv_h), ezz = dxm(f.vz, k, sz, g.inv_h);
+    sxx += g.dt * (p.l2m[k] * exx + p.lam[k] * ezz);
+    szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
+    sxz += g.dt * p.muxz[k] * (dxp(f.vx, k, sz, g.inv_h) + dxp(f.vz, k, sx, g.inv_h));
+  }
+  if (e.i == src_i && e.j == src_j) {
+    sxx += src_value;
+    szz += src_value;
+  }
+  const float t = taper[e.j * g.nx + e.i];
+  f.sxx[k] = sxx * t;
+  f.szz[k] = szz * t;
+  f.sxz[k] = sxz * t;
 }
 
 // ---- adjoint ---------------------------------------------------------------
 struct Grads {
   float *bx, *bz, *l2m, *lam, *muxz;
 };
+// Inputs of the transposed difference operators, zero outside valid cells:
+// t1 = dt (l2m asxx + lam aszz), t2 = dt (lam asxx + l2m aszz), t3 = dt muxz asxz
+// (velocity pass), t4 = dt bx avx, t5 = dt bz avz (stress pass).
+struct Temps {
+  float *t1, *t2, *t3, *t4, *t5;
+};
 
-// Adjoint velocity pass of step n (reverse of stress step 4, receivers 3,
-// taper 2, and the buoyancy gradient of velocity step 1).  The adjoint
-// stresses are already multiplied by the taper of step n.
-__global__ void adj_velocity_kernel(Grid g, Fields a, Params p, Grads gr, const float* __restrict__ taper,
-                                    const int32_t* __restrict__ rec_map, const float* __restrict__ resid_n,
-                                    const float* __restrict__ vn, const float* __restrict__ vprev) {
-  const int64_t sx = g.C, sz = (int64_t)g.nx * g.C, plane = (int64_t)g.nx * g.nz * g.C;
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    if (!g.valid(i, j)) return;
-    // t1 = dt (l2m asxx + lam aszz), t2 = dt (lam asxx + l2m aszz), t3 = dt muxz asxz,
-    // zero outside the valid cells.
-    auto t1 = [&](int ii, int jj) {
-      if (!g.valid(ii, jj)) return 0.f;
-      const int64_t q = g.at(jj, ii) + c;
-      return g.dt * (p.l2m[q] * a.sxx[q] + p.lam[q] * a.szz[q]);
-    };
-    auto t2 = [&](int ii, int jj) {
-      if (!g.valid(ii, jj)) return 0.f;
-      const int64_t q = g.at(jj, ii) + c;
-      return g.dt * (p.lam[q] * a.sxx[q] + p.l2m[q] * a.szz[q]);
-    };
-    auto t3 = [&](int ii, int jj) {
-      if (!g.valid(ii, jj)) return 0.f;
-      const int64_t q = g.at(jj, ii) + c;
-      return g.dt * p.muxz[q] * a.sxz[q];
-    };
-    const float ih = g.inv_h;
-    // -Dx+ t1 - Dz- t3  and  -Dz+ t2 - Dx- t3
-    const float dxp_t1 = (C1 * (t1(i + 1, j) - t1(i, j)) + C2 * (t1(i + 2, j) - t1(i - 1, j))) * ih;
-    const float dzm_t3 = (C1 * (t3(i, j) - t3(i, j - 1)) + C2 * (t3(i, j + 1) - t3(i, j - 2))) * ih;
-    const float dzp_t2 = (C1 * (t2(i, j + 1) - t2(i, j)) + C2 * (t2(i, j + 2) - t2(i, j - 1))) * ih;
-    const float dxm_t3 = (C1 * (t3(i, j) - t3(i - 1, j)) + C2 * (t3(i + 1, j) - t3(i - 2, j))) * ih;
-    float ax = a.vx[k] - dxp_t1 - dzm_t3;
-    float az = a.vz[k] - dzp_t2 - dxm_t3;
-    // stiffness gradients: strains of the stored forward velocities at step n
-    const float* vxn = vn;
-    const float* vzn = vn + plane;
-    const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
-    const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
-    const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
-    gr.l2m[k] += g.dt * (exx * asxx + ezz * aszz);
-    gr.lam[k] += g.dt * (ezz * asxx + exx * aszz);
-    gr.muxz[k] += g.dt * exz * asxz;
-    // adjoint sources (residuals already weighted)
-    const int r = rec_map[(int64_t)j * g.nx + i];
-    if (r >= 0) {
-      ax += resid_n[((int64_t)r * 2 + 0) * g.C + c];
-      az += resid_n[((int64_t)r * 2 + 1) * g.C + c];
-    }
-    const float tp = taper[(int64_t)j * g.nx + i];
-    ax *= tp;
-    az *= tp;
-    a.vx[k] = ax;
-    a.vz[k] = az;
-    // buoyancy gradients: dt * (divergence of stress) = (v' - v_prev) / b
-    const float dvx = vxn[k] / tp - (vprev ? vprev[k] : 0.f);
-    const float dvz = vzn[k] / tp - (vprev ? vprev[plane + k] : 0.f);
-    gr.bx[k] += dvx / p.bx[k] * ax;
-    gr.bz[k] += dvz / p.bz[k] * az;
-  });
+// Adjoint velocity pass of step n: reverse of stress step 4 (adjoint
+// velocities and stiffness gradients), receivers 3, taper 2, and the
+// buoyancy gradients of velocity step 1; writes t4, t5 for the stress pass.
+__global__ void __launch_bounds__(TX* TY) adj_velocity_kernel(Grid g, Fields a, Params p, Grads gr, Temps tm,
+                                                                const float* __restrict__ taper,
+                                                                const int32_t* __restrict__ rec_map,
+                                                                const float* __restrict__ resid_n,
+                                                                const float* __restrict__ vn,
+                                                                const float* __restrict__ vprev) {
+  const Cell e = cell_of(g);
+  if (!e.in || !g.valid(e.i, e.j)) return;
+  const int k = e.k, sx = g.C, sz = g.nx * g.C, plane = g.nx * g.nz * g.C;
+  const float ih = g.inv_h;
+  // (Dx+)^T = -Dx-, etc.: -Dx+ t1 - Dz- t3 and -Dz+ t2 - Dx- t3
+  float ax = a.vx[k] - dxp(tm.t1, k, sx, ih) - dxm(tm.t3, k, sz, ih);
+  float az = a.vz[k] - dxp(tm.t2, k, sz, ih) - dxm(tm.t3, k, sx, ih);
+  const float* vxn = vn;
+  const float* vzn = vn + plane;
+  const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
+  const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
+  const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
+  gr.l2m[k] += g.dt * (exx * asxx + ezz * aszz);
+  gr.lam[k] += g.dt * (ezz * asxx + exx * aszz);
+  gr.muxz[k] += g.dt * exz * asxz;
+  const int cell = e.j * g.nx + e.i;
+  const int r = rec_map[cell];
+  if (r >= 0) {
+    ax += resid_n[(r * 2 + 0) * g.C + e.c];
+    az += resid_n[(r * 2 + 1) * g.C + e.c];
+  }
+  const float tp = taper[cell];
+  ax *= tp;
+  az *= tp;
+  a.vx[k] = ax;
+  a.vz[k] = az;
+  const float dvx = vxn[k] / tp - (vprev ? vprev[k] : 0.f);
+  const float dvz = vzn[k] / tp - (vprev ? vprev[plane + k] : 0.f);
+  gr.bx[k] += dvx / p.bx[k] * ax;
+  gr.bz[k] += dvz / p.bz[k] * az;
+  tm.t4[k] = g.dt * p.bx[k] * ax;
+  tm.t5[k] = g.dt * p.bz[k] * az;
 }
 
-// Adjoint stress pass of step n (reverse of velocity step 1), followed by the
-// taper of step n-1 (reverse of its stress taper).
-__global__ void adj_stress_kernel(Grid g, Fields a, Params p, const float* __restrict__ taper) {
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    if (!g.valid(i, j)) return;
-    auto t4 = [&](int ii, int jj) {
-      if (!g.valid(ii, jj)) return 0.f;
-      const int64_t q = g.at(jj, ii) + c;
-      return g.dt * p.bx[q] * a.vx[q];
-    };
-    auto t5 = [&](int ii, int jj) {
-      if (!g.valid(ii, jj)) return 0.f;
-      const int64_t q = g.at(jj, ii) + c;
-      return g.dt * p.bz[q] * a.vz[q];
-    };
-    const float ih = g.inv_h;
-    const float dxm_t4 = (C1 * (t4(i, j) - t4(i - 1, j)) + C2 * (t4(i + 1, j) - t4(i - 2, j))) * ih;
-    const float dzp_t4 = (C1 * (t4(i, j + 1) - t4(i, j)) + C2 * (t4(i, j + 2) - t4(i, j - 1))) * ih;
-    const float dxp_t5 = (C1 * (t5(i + 1, j) - t5(i, j)) + C2 * (t5(i + 2, j) - t5(i - 1, j))) * ih;
-    const float dzm_t5 = (C1 * (t5(i, j) - t5(i, j - 1)) + C2 * (t5(i, j + 1) - t5(i, j - 2))) * ih;
-    const float tp = taper[(int64_t)j * g.nx + i];
-    a.sxx[k] = (a.sxx[k] - dxm_t4) * tp;
-    a.sxz[k] = (a.sxz[k] - dzp_t4 - dxp_t5) * tp;
-    a.szz[k] = (a.szz[k] - dzm_t5) * tp;
-  });
+// Adjoint stress pass of step n (reverse of velocity step 1), then the taper
+// of step n-1 (reverse of its stress taper); writes t1..t3 for step n-1.
+__global__ void __launch_bounds__(TX* TY) adj_stress_kernel(Grid g, Fields a, Params p, Temps tm,
+                                                              const float* __restrict__ taper) {
+  const Cell e = cell_of(g);
+  if (!e.in || !g.valid(e.i, e.j)) return;
+  const int k = e.k, sx = g.C, sz = g.nx * g.C;
+  const float ih = g.inv_h;
+  const float tp = taper[e.j * g.nx + e.i];
+  const float asxx = (a.sxx[k] - dxm(tm.t4, k, sx, ih)) * tp;
+  const float asxz = (a.sxz[k] - dxp(tm.t4, k, sz, ih) - dxp(tm.t5, k, sx, ih)) * tp;
+  const float aszz = (a.szz[k] - dxm(tm.t5, k, sz, ih)) * tp;
+  a.sxx[k] = asxx;
+  a.sxz[k] = asxz;
+  a.szz[k] = aszz;
+  tm.t1[k] = g.dt * (p.l2m[k] * asxx + p.lam[k] * aszz);
+  tm.t2[k] = g.dt * (p.lam[k] * asxx + p.l2m[k] * aszz);
+  tm.t3[k] = g.dt * p.muxz[k] * asxz;
 }
 
 // Weighted residuals w (rec - obs) of one shot, all steps: [nt][nrec][2][C];
-// obs is shared by all chains: [nt][nrec][2].  Also the FP64 misfit partials.
+// obs is shared by all chains: [nt][nrec][2].
 __global__ void residual_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec,
                                 const float* __restrict__ obs, float w, float* resid) {
   const int64_t total = n_rows * C;
@@ -253,31 +247,32 @@ __global__ void misfit_kernel(int64_t n_rows, int64_t C, const float* __restrict
 __global__ void param_gradient_kernel(Grid g, Grads gr, const float* __restrict__ rho, const float* __restrict__ vp,
                                       const float* __restrict__ vs, float* g_rho, float* g_vp, float* g_vs,
                                       int accumulate) {
-  for_cells(g, [&](int i, int j, int64_t c, int64_t k) {
-    float gl = gr.lam[k] + gr.l2m[k];
-    float gm = 2.f * gr.l2m[k];
-    float gb = 0.5f * gr.bx[k] + 0.5f * gr.bz[k];
-    if (i > 0) gb += 0.5f * gr.bx[g.at(j, i - 1) + c];
-    if (j > 0) gb += 0.5f * gr.bz[g.at(j - 1, i) + c];
-    float gmu = 0.25f * gr.muxz[k];
-    if (i > 0) gmu += 0.25f * gr.muxz[g.at(j, i - 1) + c];
-    if (j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i) + c];
-    if (i > 0 && j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i - 1) + c];
-    gm += gmu;
-    const float r = rho[k], p = vp[k], s = vs[k];
-    const float vgp = gl * 2.f * r * p;
-    const float vgs = gl * (-4.f * r * s) + gm * 2.f * r * s;
-    const float vgr = gl * (p * p - 2.f * s * s) + gm * s * s - gb / (r * r);
-    if (accumulate) {
-      g_vp[k] += vgp;
-      g_vs[k] += vgs;
-      g_rho[k] += vgr;
-    } else {
-      g_vp[k] = vgp;
-      g_vs[k] = vgs;
-      g_rho[k] = vgr;
-    }
-  });
+  const Cell e = cell_of(g);
+  if (!e.in) return;
+  const int k = e.k, i = e.i, j = e.j, c = e.c;
+  float gl = gr.lam[k] + gr.l2m[k];
+  float gm = 2.f * gr.l2m[k];
+  float gb = 0.5f * gr.bx[k] + 0.5f * gr.bz[k];
+  if (i > 0) gb += 0.5f * gr.bx[g.at(j, i - 1) + c];
+  if (j > 0) gb += 0.5f * gr.bz[g.at(j - 1, i) + c];
+  float gmu = 0.25f * gr.muxz[k];
+  if (i > 0) gmu += 0.25f * gr.muxz[g.at(j, i - 1) + c];
+  if (j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i) + c];
+  if (i > 0 && j > 0) gmu += 0.25f * gr.muxz[g.at(j - 1, i - 1) + c];
+  gm += gmu;
+  const float r = rho[k], pv = vp[k], s = vs[k];
+  const float vgp = gl * 2.f * r * pv;
+  const float vgs = gl * (-4.f * r * s) + gm * 2.f * r * s;
+  const float vgr = gl * (pv * pv - 2.f * s * s) + gm * s * s - gb / (r * r);
+  if (accumulate) {
+    g_vp[k] += vgp;
+    g_vs[k] += vgs;
+    g_rho[k] += vgr;
+  } else {
+    g_vp[k] = vgp;
+    g_vs[k] = vgs;
+    g_rho[k] = vgr;
+  }
 }
 
 inline unsigned grid_for(int64_t n) {
@@ -297,6 +292,8 @@ static int check_fwi(const hmc_fwi* s, const char* who) {
   HMC_REQUIRE(s->taper && s->stf_host && s->rec_map && s->rho && s->vp && s->vs, "%s: missing model buffer", who);
   HMC_REQUIRE(s->bx && s->bz && s->l2m && s->lam && s->muxz, "%s: missing parameter work buffer", who);
   HMC_REQUIRE(s->vx && s->vz && s->sxx && s->szz && s->sxz && s->rec, "%s: missing wavefield buffer", who);
+  HMC_REQUIRE((int64_t)s->nx * s->nz * s->chains * 2 < (1ll << 31), "%s: grid x chains too large for 32-bit indexing",
+              who);
   return HMC_OK;
 }
 
@@ -304,7 +301,7 @@ static Grid grid_of(const hmc_fwi* s) {
   Grid g;
   g.nx = s->nx;
   g.nz = s->nz;
-  g.C = s->chains;
+  g.C = (int)s->chains;
   g.inv_h = 1.f / s->h;
   g.dt = s->dt;
   return g;
@@ -315,7 +312,7 @@ extern "C" {
 HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream) {
   HMC_TRY(check_fwi(s, "hmc_fwi_prepare"));
   const Grid g = grid_of(s);
-  derive_params_kernel<<<grid_for((int64_t)s->nx * s->nz * s->chains), 256, 0, as_stream(stream)>>>(
+  derive_params_kernel<<<cell_grid(s->nx, s->nz, s->chains), dim3(TX, TY), 0, as_stream(stream)>>>(
       g, s->rho, s->vp, s->vs, s->bx, s->bz, s->l2m, s->lam, s->muxz);
   return check_launch("derive_params_kernel");
 }
@@ -335,16 +332,16 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
   }
   Fields f{s->vx, s->vz, s->sxx, s->szz, s->sxz};
   Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
-  const unsigned grid = grid_for(cells);
+  const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block(TX, TY);
   const float src_scale = s->dt / (s->h * s->h);
   float* rec_shot = s->rec + (int64_t)shot * s->nt * s->nrec * 2 * s->chains;
   // the source wavelet is read on the host: it is a handful of floats per step
   for (int n = 0; n < s->nt; ++n) {
     float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
     float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
-    velocity_kernel<<<grid, 256, 0, st>>>(g, f, p, s->taper, s->rec_map, s->nrec, rec_n, store_n);
+    velocity_kernel<<<grid, block, 0, st>>>(g, f, p, s->taper, s->rec_map, rec_n, store_n);
     HMC_TRY(check_launch("velocity_kernel"));
-    stress_kernel<<<grid, 256, 0, st>>>(g, f, p, s->taper, src_x, src_z, s->stf_host[n] * src_scale);
+    stress_kernel<<<grid, block, 0, st>>>(g, f, p, s->taper, src_x, src_z, s->stf_host[n] * src_scale);
     HMC_TRY(check_launch("stress_kernel"));
   }
   return HMC_OK;
@@ -364,11 +361,12 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   HMC_REQUIRE(s->store && s->obs && s->resid && s->avx && s->avz && s->asxx && s->aszz && s->asxz,
               "hmc_fwi_adjoint_shot: missing adjoint buffer");
   HMC_REQUIRE(s->g_bx && s->g_bz && s->g_l2m && s->g_lam && s->g_muxz, "hmc_fwi_adjoint_shot: missing gradients");
+  HMC_REQUIRE(s->t1 && s->t2 && s->t3 && s->t4 && s->t5, "hmc_fwi_adjoint_shot: missing adjoint temporaries");
   cudaStream_t st = as_stream(stream);
   const Grid g = grid_of(s);
   const int64_t cells = (int64_t)s->nx * s->nz * s->chains;
   const size_t fb = (size_t)cells * sizeof(float);
-  for (float* f : {s->avx, s->avz, s->asxx, s->aszz, s->asxz}) {
+  for (float* f : {s->avx, s->avz, s->asxx, s->aszz, s->asxz, s->t1, s->t2, s->t3, s->t4, s->t5}) {
     cudaError_t e = cudaMemsetAsync(f, 0, fb, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fwi adjoint)");
   }
@@ -380,14 +378,15 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   Fields a{s->avx, s->avz, s->asxx, s->aszz, s->asxz};
   Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
   Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
-  const unsigned grid = grid_for(cells);
+  Temps tm{s->t1, s->t2, s->t3, s->t4, s->t5};
+  const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block(TX, TY);
   for (int n = s->nt - 1; n >= 0; --n) {
     const float* vn = s->store + (int64_t)n * 2 * cells;
     const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
-    adj_velocity_kernel<<<grid, 256, 0, st>>>(g, a, p, gr, s->taper, s->rec_map,
-                                              s->resid + (int64_t)n * s->nrec * 2 * s->chains, vn, vp);
+    adj_velocity_kernel<<<grid, block, 0, st>>>(g, a, p, gr, tm, s->taper, s->rec_map,
+                                                s->resid + (int64_t)n * s->nrec * 2 * s->chains, vn, vp);
     HMC_TRY(check_launch("adj_velocity_kernel"));
-    adj_stress_kernel<<<grid, 256, 0, st>>>(g, a, p, s->taper);
+    adj_stress_kernel<<<grid, block, 0, st>>>(g, a, p, tm, s->taper);
     HMC_TRY(check_launch("adj_stress_kernel"));
   }
   return HMC_OK;
@@ -409,7 +408,7 @@ HMC_API int hmc_fwi_param_gradient(const hmc_fwi* s, float* g_rho, float* g_vp, 
   HMC_REQUIRE(g_rho && g_vp && g_vs, "hmc_fwi_param_gradient: null output");
   const Grid g = grid_of(s);
   Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
-  param_gradient_kernel<<<grid_for((int64_t)s->nx * s->nz * s->chains), 256, 0, as_stream(stream)>>>(
+  param_gradient_kernel<<<cell_grid(s->nx, s->nz, s->chains), dim3(TX, TY), 0, as_stream(stream)>>>(
       g, gr, s->rho, s->vp, s->vs, g_rho, g_vp, g_vs, accumulate);
   return check_launch("param_gradient_kernel");
 }

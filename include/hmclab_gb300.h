@@ -354,6 +354,11 @@ typedef struct hmc_fwi {
   float* g_l2m;
   float* g_lam;
   float* g_muxz;
+  float* t1;                /* [nz][nx][C] adjoint temporaries (work)       */
+  float* t2;
+  float* t3;
+  float* t4;
+  float* t5;
 } hmc_fwi;
 
 /* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */
