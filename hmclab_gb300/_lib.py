@@ -105,6 +105,28 @@ class HmcFwi(_ct.Structure):
         "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5")]
 
 
+class HmcMlpOut(_ct.Structure):
+    """Mirror of `hmc_mlp_out` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("z", c_void_p),
+        ("ldz", c_int64),
+        ("act", c_void_p),
+        ("ld_act", c_int64),
+        ("act_t", c_void_p),
+        ("ld_act_t", c_int64),
+        ("y", c_void_p),
+        ("ldy", c_int64),
+        ("g_state", c_void_p),
+        ("out_scale", c_void_p),
+        ("out_shift", c_void_p),
+        ("g", c_void_p),
+        ("accumulate", c_int32),
+    ]
+
+
+HMC_MLP_HIDDEN, HMC_MLP_OUT, HMC_MLP_BACK, HMC_MLP_WGRAD = 0, 1, 2, 3
+
 P = c_void_p
 I = c_int
 I64 = c_int64
@@ -145,6 +167,14 @@ SIGNATURES = {
     "hmc_tc_step": [P, P, P, I64, P, P, P, P, I64, P, P, I, P, P, D, D, P, S],
     "hmc_tc_resid_misfit": [I64, I64, I64, P, P, I64, P, P, I64, P, P, P, P, I, P, S],
     "hmc_tc_partials_size": [I64, I64],
+    "hmc_tc_mlp": [I, I64, I64, I64, P, I64, P, I64, P, P, P, S],
+    "hmc_mlp_input": [I64, I64, P, P, P, P, I64, S],
+    "hmc_mlp_gather": [I64, I64, P, P, P, P, P, P, P, P, I64, P, I64, P, I64, S],
+    "hmc_mlp_loss": [I64, I64, P, I64, P, I64, P, I64, P, I64, P, S],
+    "hmc_mlp_bias_grad": [I64, I64, P, I64, P, S],
+    "hmc_mlp_adam": [I64, P, P, P, P, _ct.c_float, _ct.c_float, _ct.c_float, _ct.c_float, I64, S],
+    "hmc_mlp_cast": [I64, I64, P, P, I64, P, I64, S],
+    "hmc_mlp_record": [I64, I64, P, P, I64, S],
     "hmc_fwi_prepare": [P, S],
     "hmc_fwi_forward_shot": [P, I, I, I, I, S],
     "hmc_fwi_misfit": [P, I, P, I, S],

@@ -42,13 +42,22 @@ constexpr int UK = 16;                    // k per tcgen05.mma (kind::f16)
 constexpr int STAGES = SWZ == 64 ? 4 : 2;
 constexpr int A_BYTES = BM * BK * 2;      // per operand half (chains)
 constexpr int B_BYTES = BN * BK * 2;      // per operand half (rows)
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi/lo split (3 products)
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+// Stage layout for NPROD products: q_hi | q_lo | a_hi | a_lo (NPROD = 3) or
+// q | a (NPROD = 1, plain BF16 operands).
+template <int NPROD>
+struct Stage {
+  static constexpr int bytes = NPROD == 3 ? STAGE_BYTES : A_BYTES + B_BYTES;
+  static constexpr int q_lo = A_BYTES;
+  static constexpr int a_hi = NPROD == 3 ? 2 * A_BYTES : A_BYTES;
+  static constexpr int a_lo = a_hi + B_BYTES;
+};
 constexpr int THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t TMEM_COLS = 256;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
 
-enum Epi { EPI_GRAD = 0, EPI_STEP = 1, EPI_MISFIT = 2 };
+enum Epi { EPI_GRAD = 0, EPI_STEP = 1, EPI_MISFIT = 2, EPI_MLP_HIDDEN = 3, EPI_MLP_OUT = 4, EPI_MLP_BACK = 5 };
 enum Prior { PRIOR_NONE = 0, PRIOR_NORMAL = 1, PRIOR_LAPLACE = 2 };
 
 struct EpiParams {
@@ -77,8 +86,26 @@ struct EpiParams {
   // EPI_MISFIT
   const float* inv_var;    // [rows]
   double* partial;         // [n_tiles][C]
+  // EPI_MLP_*: M = batch rows (C), N = features (rows)
+  float* z;                // [C][ldz] pre-activations (written by HIDDEN, read by BACK)
+  int64_t ldz;
+  __nv_bfloat16* act;      // [C][ld_act] activations / deltas (BF16)
+  int64_t ld_act;
+  __nv_bfloat16* act_t;    // [rows][ld_act_t] the same, transposed
+  int64_t ld_act_t;
+  float* y;                // [C][ldy] network output (OUT)
+  int64_t ldy;
+  float* g_state;          // [rows][C] scale * y + shift (OUT, may be null)
+  const float* out_scale;
+  const float* out_shift;
   int* status;
 };
+
+// GELU(z) = z Phi(z) and its derivative Phi(z) + z phi(z) (erf form).
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+}
 
 // ---- PTX helpers ------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -176,14 +203,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
 }
 
 // ---- the kernel -------------------------------------------------------------
-template <int EPI>
+template <int EPI, int NPROD>
 __global__ void __launch_bounds__(THREADS, 1)
     chain_gemm_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__ CUtensorMap tq_lo,
                       const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                       int num_kb, EpiParams ep) {
+  using S = Stage<NPROD>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* full = (uint64_t*)(smem + STAGES * S::bytes);
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
   uint32_t* tmem_slot = (uint32_t*)(accum + 1);
@@ -225,15 +253,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           break;
         }
       }
-      unsigned char* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
+      unsigned char* st = smem + s * S::bytes;
+      mbar_expect_tx(&full[s], S::bytes);
       // CTAs that share an operand tile start at different k-blocks, so
       // they do not all fetch the same lines from the same L2 slices at once.
       const int kx = ((kb + kb_rot) % num_kb) * BK;
       tma_load_2d(st, &tq_hi, &full[s], kx, m0);
-      tma_load_2d(st + A_BYTES, &tq_lo, &full[s], kx, m0);
-      tma_load_2d(st + 2 * A_BYTES, &ta_hi, &full[s], kx, n0);
-      tma_load_2d(st + 2 * A_BYTES + B_BYTES, &ta_lo, &full[s], kx, n0);
+      tma_load_2d(st + S::a_hi, &ta_hi, &full[s], kx, n0);
+      if (NPROD == 3) {
+        tma_load_2d(st + S::q_lo, &tq_lo, &full[s], kx, m0);
+        tma_load_2d(st + S::a_lo, &ta_lo, &full[s], kx, n0);
+      }
       ++tma_issued_stage_uses;
     }
   } else if (warp == 1 && lane == 0) {
@@ -248,18 +278,21 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       tc_fence_after();
-      const uint32_t sa_hi = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t sa_lo = sa_hi + A_BYTES;
-      const uint32_t sb_hi = sa_hi + 2 * A_BYTES;
-      const uint32_t sb_lo = sb_hi + B_BYTES;
+      const uint32_t sa_hi = smem_u32(smem + s * S::bytes);
+      const uint32_t sa_lo = sa_hi + S::q_lo;
+      const uint32_t sb_hi = sa_hi + S::a_hi;
+      const uint32_t sb_lo = sa_hi + S::a_lo;
 #pragma unroll
       for (int kk = 0; kk < BK / UK; ++kk) {
-        const uint32_t off = kk * UK * 2;  // bytes along the 128-byte row
-        const uint64_t qh = sdesc_k_sw(sa_hi + off), ql = sdesc_k_sw(sa_lo + off);
-        const uint64_t ah = sdesc_k_sw(sb_hi + off), al = sdesc_k_sw(sb_lo + off);
+        const uint32_t off = kk * UK * 2;  // bytes along the swizzled row
+        const uint64_t qh = sdesc_k_sw(sa_hi + off);
+        const uint64_t ah = sdesc_k_sw(sb_hi + off);
         umma_bf16(tmem, qh, ah, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-        umma_bf16(tmem, qh, al, idesc, 1u);
-        umma_bf16(tmem, ql, ah, idesc, 1u);
+        if (NPROD == 3) {
+          const uint64_t ql = sdesc_k_sw(sa_lo + off), al = sdesc_k_sw(sb_lo + off);
+          umma_bf16(tmem, qh, al, idesc, 1u);
+          umma_bf16(tmem, ql, ah, idesc, 1u);
+        }
       }
       umma_commit(&empty[s]);  // frees the stage once these MMAs complete
     }
@@ -323,7 +356,43 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int j = 0; j < 16; ++j) gold[j] = (ep.accumulate && j < nr) ? ep.g[(r0 + j) * C + c] : 0.f;
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          if (j < nr) ep.g[(r0 + j) * C + c] = acc[j] - ep.bias[r0 + j] + gold[j];
+          if (j < nr) ep.g[(r0 + j) * C + c] = acc[j] - (ep.bias ? ep.bias[r0 + j] : 0.f) + gold[j];
+      } else if (EPI == EPI_MLP_HIDDEN || EPI == EPI_MLP_BACK) {
+        // HIDDEN: z = acc + b, a = GELU(z); BACK: delta = acc * GELU'(z).
+        // Both write BF16 [c][r] (next contraction, K = features) and
+        // [r][c] (weight gradients, K = batch).
+        __align__(16) __nv_bfloat16 a16[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float v = 0.f;
+          if (j < nr) {
+            const int64_t r = r0 + j;
+            if (EPI == EPI_MLP_HIDDEN) {
+              const float zv = acc[j] + ep.bias[r];
+              ep.z[c * ep.ldz + r] = zv;
+              v = gelu(zv);
+            } else {
+              v = acc[j] * gelu_grad(ep.z[c * ep.ldz + r]);
+            }
+          }
+          a16[j] = __float2bfloat16_rn(v);
+          if (j < nr) ep.act_t[(r0 + j) * ep.ld_act_t + c] = a16[j];
+        }
+        if (r0 + 16 <= ep.ld_act) {
+          uint4* dst = (uint4*)(ep.act + c * ep.ld_act + r0);
+          dst[0] = ((const uint4*)a16)[0];
+          dst[1] = ((const uint4*)a16)[1];
+        }
+      } else if (EPI == EPI_MLP_OUT) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (j < nr) {
+            const int64_t r = r0 + j;
+            const float yv = acc[j] + ep.bias[r];
+            if (ep.y) ep.y[c * ep.ldy + r] = yv;
+            if (ep.g_state) ep.g_state[r * C + c] = ep.out_scale[r] * yv + ep.out_shift[r];
+          }
+        }
       } else {  // EPI_STEP
         // all loads of the chunk first (independent, in flight together)
         float qv[16], pv[16];
@@ -510,7 +579,7 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int
   return HMC_OK;
 }
 
-template <int EPI>
+template <int EPI, int NPROD = 3>
 int launch(int64_t C, int64_t rows, int64_t K, const void* q_hi, const void* q_lo, int64_t ldq, const void* a_hi,
            const void* a_lo, int64_t lda, const EpiParams& ep, cudaStream_t st) {
   HMC_REQUIRE(C > 0 && rows > 0 && K > 0, "tensor-core contraction: bad sizes");
@@ -518,20 +587,26 @@ int launch(int64_t C, int64_t rows, int64_t K, const void* q_hi, const void* q_l
   HMC_REQUIRE(ep.status != nullptr, "tensor-core contraction: null status word");
   CUtensorMap mq_hi, mq_lo, ma_hi, ma_lo;
   HMC_TRY(make_map(&mq_hi, q_hi, C, K, ldq, BM));
-  HMC_TRY(make_map(&mq_lo, q_lo, C, K, ldq, BM));
   HMC_TRY(make_map(&ma_hi, a_hi, rows, K, lda, BN));
-  HMC_TRY(make_map(&ma_lo, a_lo, rows, K, lda, BN));
-  static bool attr_set[3] = {false, false, false};
-  if (!attr_set[EPI]) {
-    cudaError_t e = cudaFuncSetAttribute(chain_gemm_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SMEM_BYTES);
+  if (NPROD == 3) {
+    HMC_TRY(make_map(&mq_lo, q_lo, C, K, ldq, BM));
+    HMC_TRY(make_map(&ma_lo, a_lo, rows, K, lda, BN));
+  } else {
+    mq_lo = mq_hi;
+    ma_lo = ma_hi;
+  }
+  constexpr int smem = STAGES * Stage<NPROD>::bytes + 1024 + 256;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(chain_gemm_kernel<EPI, NPROD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(chain_gemm_kernel)");
-    attr_set[EPI] = true;
+    attr_set = true;
   }
   const int num_kb = (int)((K + BK - 1) / BK);
   const dim3 grid((unsigned)((C + BM - 1) / BM), (unsigned)((rows + BN - 1) / BN));
   HMC_REQUIRE(grid.y <= 65535, "tensor-core contraction: too many rows");
-  chain_gemm_kernel<EPI><<<grid, THREADS, SMEM_BYTES, st>>>(mq_hi, mq_lo, ma_hi, ma_lo, num_kb, ep);
+  chain_gemm_kernel<EPI, NPROD><<<grid, THREADS, smem, st>>>(mq_hi, mq_lo, ma_hi, ma_lo, num_kb, ep);
   return check_launch("chain_gemm_kernel");
 }
 
@@ -634,5 +709,46 @@ HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C, const void* g_h
 }
 
 HMC_API int64_t hmc_tc_partials_size(int64_t n, int64_t C) { return (n + BN - 1) / BN * C; }
+
+HMC_API int hmc_tc_mlp(int mode, int64_t M, int64_t N, int64_t K, const void* x, int64_t ldx, const void* w,
+                       int64_t ldw, const float* bias, const hmc_mlp_out* out, int* status, void* stream) {
+  HMC_REQUIRE(out != nullptr && x != nullptr && w != nullptr, "hmc_tc_mlp: null argument");
+  HMC_REQUIRE(ldx % 8 == 0 && ldw % 8 == 0, "hmc_tc_mlp: pitches must be multiples of 8 elements");
+  EpiParams ep = {};
+  ep.C = M;
+  ep.rows = N;
+  ep.bias = bias;
+  ep.status = status;
+  ep.z = out->z;
+  ep.ldz = out->ldz;
+  ep.act = (__nv_bfloat16*)out->act;
+  ep.ld_act = out->ld_act;
+  ep.act_t = (__nv_bfloat16*)out->act_t;
+  ep.ld_act_t = out->ld_act_t;
+  ep.y = out->y;
+  ep.ldy = out->ldy;
+  ep.g_state = out->g_state;
+  ep.out_scale = out->out_scale;
+  ep.out_shift = out->out_shift;
+  ep.g = out->g;
+  ep.accumulate = out->accumulate;
+  cudaStream_t st = as_stream(stream);
+  switch (mode) {
+    case HMC_MLP_HIDDEN:
+      HMC_REQUIRE(bias && ep.z && ep.act && ep.act_t && ep.ld_act % 16 == 0, "hmc_tc_mlp: hidden outputs");
+      return launch<EPI_MLP_HIDDEN, 1>(M, N, K, x, nullptr, ldx, w, nullptr, ldw, ep, st);
+    case HMC_MLP_OUT:
+      HMC_REQUIRE(bias && (ep.y || (ep.g_state && ep.out_scale && ep.out_shift)), "hmc_tc_mlp: output buffers");
+      return launch<EPI_MLP_OUT, 1>(M, N, K, x, nullptr, ldx, w, nullptr, ldw, ep, st);
+    case HMC_MLP_BACK:
+      HMC_REQUIRE(ep.z && ep.act && ep.act_t && ep.ld_act % 16 == 0, "hmc_tc_mlp: backward buffers");
+      return launch<EPI_MLP_BACK, 1>(M, N, K, x, nullptr, ldx, w, nullptr, ldw, ep, st);
+    case HMC_MLP_WGRAD:
+      HMC_REQUIRE(ep.g != nullptr, "hmc_tc_mlp: weight-gradient output");
+      return launch<EPI_GRAD, 1>(M, N, K, x, nullptr, ldx, w, nullptr, ldw, ep, st);
+    default:
+      return fail(HMC_ERR_INVALID_ARG, "hmc_tc_mlp: unknown mode %d", mode);
+  }
+}
 
 }  // extern "C"

@@ -312,6 +312,78 @@ HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C,
                                 int* status, void* stream);
 HMC_API int64_t hmc_tc_partials_size(int64_t n, int64_t C);
 
+/* ---- MLP gradient surrogate (no counterpart in the reference: it stands in
+ * for the distribution.gradient calls of the leapfrog at Samplers.py:1562,
+ * 1573 once trained; the exact misfit still decides acceptance) -----------
+ * hmc_tc_mlp: out[m][n] = sum_k x[m][k] w[n][k] on the tensor cores (BF16
+ * operands, FP32 accumulation; x is [M][ldx], w is [N][ldw], both BF16), with
+ * the epilogue selected by mode:
+ *   HMC_MLP_HIDDEN  z = out + bias, a = GELU(z): z -> z [M][ldz] (FP32),
+ *                   a -> act [M][ld_act] and act_t [N][ld_act_t] (BF16)
+ *   HMC_MLP_OUT     y = out + bias -> y [M][ldy] (FP32, nullable) and/or
+ *                   g_state [N][M] = out_scale * y + out_shift
+ *   HMC_MLP_BACK    delta = out * GELU'(z) with z [M][ldz]: -> act, act_t
+ *   HMC_MLP_WGRAD   g [N][M] (+)= out (FP32, accumulate from `accumulate`)  */
+#define HMC_MLP_HIDDEN 0
+#define HMC_MLP_OUT 1
+#define HMC_MLP_BACK 2
+#define HMC_MLP_WGRAD 3
+typedef struct hmc_mlp_out {
+  float* z;
+  int64_t ldz;
+  void* act; /* BF16 */
+  int64_t ld_act;
+  void* act_t; /* BF16 */
+  int64_t ld_act_t;
+  float* y;
+  int64_t ldy;
+  float* g_state;
+  const float* out_scale;
+  const float* out_shift;
+  float* g;
+  int32_t accumulate;
+} hmc_mlp_out;
+HMC_API int hmc_tc_mlp(int mode, int64_t M, int64_t N, int64_t K,
+                       const void* x, int64_t ldx, const void* w,
+                       int64_t ldw, const float* bias, const hmc_mlp_out* out,
+                       int* status, void* stream);
+/* Network input from the sampler state: x[c][i] = bf16((q[i][c] - mu[i]) *
+ * inv_sigma[i]) for q [d][C]; x is [C][ldx].                                */
+HMC_API int hmc_mlp_input(int64_t d, int64_t C, const float* q, const float* mu,
+                          const float* inv_sigma, void* x, int64_t ldx,
+                          void* stream);
+/* Training minibatch: rows idx[0..B) of the sample stores q_store / g_store
+ * ([N][d], FP32) -> x [B][ldx], x_t [d][ldxt] (BF16, normalised inputs) and
+ * t [B][ldt] (FP32, normalised targets (g - g_mu) * g_inv_sigma).           */
+HMC_API int hmc_mlp_gather(int64_t B, int64_t d, const int32_t* idx,
+                           const float* q_store, const float* g_store,
+                           const float* mu, const float* inv_sigma,
+                           const float* g_mu, const float* g_inv_sigma,
+                           void* x, int64_t ldx, void* x_t, int64_t ldxt,
+                           float* t, int64_t ldt, void* stream);
+/* Loss 0.5/B sum (y - t)^2 and dY = (y - t)/B as BF16 dy [B][lddy] and
+ * dy_t [n][lddyt].  loss points to 1025 device doubles: loss[0] receives the
+ * loss, loss[1..1024] hold block partials.                                  */
+HMC_API int hmc_mlp_loss(int64_t B, int64_t n, const float* y, int64_t ldy,
+                         const float* t, int64_t ldt, void* dy, int64_t lddy,
+                         void* dy_t, int64_t lddyt, double* loss,
+                         void* stream);
+/* db[r] = sum_{c < B} delta_t[r][c] for BF16 delta_t [n][ld].               */
+HMC_API int hmc_mlp_bias_grad(int64_t n, int64_t B, const void* delta_t,
+                              int64_t ld, float* db, void* stream);
+/* One Adam step (Kingma & Ba 2015) on n FP32 parameters with bias-corrected
+ * moments; step is the 1-based step count.                                  */
+HMC_API int hmc_mlp_adam(int64_t n, float* w, const float* g, float* m,
+                         float* v, float lr, float beta1, float beta2,
+                         float eps, int64_t step, void* stream);
+/* FP32 weights w [rows][cols] -> BF16 w16 [rows][ld] and w16_t [cols][ldt]. */
+HMC_API int hmc_mlp_cast(int64_t rows, int64_t cols, const float* w,
+                         void* w16, int64_t ld, void* w16_t, int64_t ldt,
+                         void* stream);
+/* Append the sampler state src [d][C] as rows base..base+C-1 of dst [N][d]. */
+HMC_API int hmc_mlp_record(int64_t d, int64_t C, const float* src, float* dst,
+                           int64_t base, void* stream);
+
 /* ---- 2-D elastic P-SV full-waveform misfit and gradient ------------------
  * Replaces psvWave's forward_simulate / calculate_l2_misfit / adjoint_simulate
  * / map_kernels_to_velocity as called by ElasticFullWaveform2D.misfit and
