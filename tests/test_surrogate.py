@@ -29,7 +29,10 @@ def close_contraction(got, a, b, ref, tol=2e-5):
 
 
 def close_bf16(got, ref):
-    assert np.all(np.abs(got - ref) <= 2.0**-7 * np.abs(ref) + 1e-30), np.abs(got - ref).max()
+    """Equal up to one BF16 ulp (FP32 vs FP64 GELU may round across a BF16
+    boundary): |got - ref| <= 2^-7 max(|got|, |ref|)."""
+    bound = 2.0**-7 * np.maximum(np.abs(got), np.abs(ref)) * 1.0001 + 1e-30
+    assert np.all(np.abs(got - ref) <= bound), np.abs(got - ref).max()
 
 
 def test_oracle_bf16_rounding():
