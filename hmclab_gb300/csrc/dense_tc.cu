@@ -101,10 +101,13 @@ struct EpiParams {
   int* status;
 };
 
-// GELU(z) = z Phi(z) and its derivative Phi(z) + z phi(z) (erf form).
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// GELU(z) = z Phi(z) and its derivative Phi(z) + z phi(z), with
+// Phi(z) = erfc(-z / sqrt 2) / 2, which stays accurate in the negative tail
+// (1 + erf cancels there in FP32).
+__device__ __forceinline__ float std_normal_cdf(float z) { return 0.5f * erfcf(-z * 0.70710678118654752f); }
+__device__ __forceinline__ float gelu(float z) { return z * std_normal_cdf(z); }
 __device__ __forceinline__ float gelu_grad(float z) {
-  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+  return std_normal_cdf(z) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
 }
 
 // ---- PTX helpers ------------------------------------------------------------

@@ -32,7 +32,10 @@ def close_bf16(got, ref):
     """Equal up to one BF16 ulp (FP32 vs FP64 GELU may round across a BF16
     boundary): |got - ref| <= 2^-7 max(|got|, |ref|)."""
     bound = 2.0**-7 * np.maximum(np.abs(got), np.abs(ref)) * 1.0001 + 1e-30
-    assert np.all(np.abs(got - ref) <= bound), np.abs(got - ref).max()
+    bad = np.abs(got - ref) > bound
+    if bad.any():
+        k = np.unravel_index(np.argmax(np.abs(got - ref) - bound), got.shape)
+        raise AssertionError(f"{bad.sum()} of {bad.size} differ; worst at {k}: got {got[k]!r}, ref {ref[k]!r}")
 
 
 def test_oracle_bf16_rounding():
