@@ -381,7 +381,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           a16[j] = __float2bfloat16_rn(v);
           if (j < nr) ep.act_t[(r0 + j) * ep.ld_act_t + c] = a16[j];
         }
-        if (r0 + 16 <= ep.ld_act) {
+        // only chunks holding valid rows: the columns past `rows` may belong
+        // to another array stored in the same row (the output layer's skip input)
+        if (nr > 0 && r0 + 16 <= ep.ld_act) {
           uint4* dst = (uint4*)(ep.act + c * ep.ld_act + r0);
           dst[0] = ((const uint4*)a16)[0];
           dst[1] = ((const uint4*)a16)[1];

@@ -18,6 +18,8 @@ inline unsigned grid_for(int64_t n) {
 }
 
 // q [d][C] -> x [C][ldx] (normalised, BF16), 32x32 tiles through shared memory.
+// Only the d leading columns of each row are written: the contractions read
+// exactly K = d columns, and the rest of a row may hold other data.
 __global__ void input_kernel(int64_t d, int64_t C, const float* __restrict__ q, const float* __restrict__ mu,
                              const float* __restrict__ inv_s, __nv_bfloat16* x, int64_t ldx) {
   __shared__ float tile[32][33];
@@ -29,7 +31,7 @@ __global__ void input_kernel(int64_t d, int64_t C, const float* __restrict__ q, 
   __syncthreads();
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int64_t c = c0 + y, i = i0 + threadIdx.x;
-    if (c < C && i < ldx) x[c * ldx + i] = __float2bfloat16_rn(tile[threadIdx.x][y]);
+    if (c < C && i < d) x[c * ldx + i] = __float2bfloat16_rn(tile[threadIdx.x][y]);
   }
 }
 
@@ -142,8 +144,8 @@ HMC_API int hmc_mlp_input(int64_t d, int64_t C, const float* q, const float* mu,
                           int64_t ldx, void* stream) {
   HMC_REQUIRE(d > 0 && C > 0 && ldx >= d, "hmc_mlp_input: bad sizes");
   HMC_REQUIRE(q && mu && inv_sigma && x, "hmc_mlp_input: null argument");
-  HMC_REQUIRE((ldx + 31) / 32 <= 65535, "hmc_mlp_input: too many features");
-  const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((ldx + 31) / 32));
+  HMC_REQUIRE((d + 31) / 32 <= 65535, "hmc_mlp_input: too many features");
+  const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((d + 31) / 32));
   input_kernel<<<grid, dim3(32, 8), 0, as_stream(stream)>>>(d, C, q, mu, inv_sigma, (__nv_bfloat16*)x, ldx);
   return check_launch("mlp input_kernel");
 }

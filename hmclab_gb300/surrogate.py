@@ -13,6 +13,13 @@ while samples are collected (it is trained during burn-in, then frozen).
 Normalisation: inputs x = (q - mu_q) / sigma_q, targets
 y = (grad U - mu_g) / sigma_g (per coordinate, from the training set); the
 loss is 0.5 * mean over the batch of |f(x) - y|^2.
+
+Architecture: h1 = GELU(W1 x + b1), h2 = GELU(W2 h1 + b2),
+f(x) = W3 [h2 | x] + b3 — the output layer also sees the input (a linear
+skip path), initialised to the least-squares linear fit of the training set,
+so the hidden layers learn the nonlinear part of the gradient field.  The
+input is stored inside the output layer's activation buffer, so the skip
+costs no extra launch.
 """
 import numpy as _np
 
@@ -54,15 +61,24 @@ class MLPSurrogate:
         self.device = device or _dev.require_cuda()
         self.d = int(dimensions)
         self.sizes = [self.d, int(hidden[0]), int(hidden[1]), self.d]
+        # the input sits after the second hidden layer in one BF16 row: keep it
+        # on a 16-element (32-byte) boundary for the tensor-memory copies
+        assert self.sizes[1] % 16 == 0 and self.sizes[2] % 16 == 0, "hidden widths must be multiples of 16"
         rng = _np.random.default_rng(seed)
         f32 = dict(dtype=torch.float32, device=self.device)
         self.W, self.b, self.mW, self.vW, self.mb, self.vb, self.gW, self.gb = ([] for _ in range(8))
         self.W16, self.W16t = [], []
+        self.k3 = self.sizes[2] + self.d  # output layer reads [h2 | x]
+        # weights and biases uniform in +-1/sqrt(fan_in) (the output layer's
+        # hidden block 10x smaller): the larger He-normal scale with zero
+        # biases fits the training pairs equally well but generalises
+        # several times worse between them
         for l in range(3):
-            n_in, n_out = self.sizes[l], self.sizes[l + 1]
-            std = (2.0 / n_in) ** 0.5 if l < 2 else (1.0 / n_in) ** 0.5
-            self.W.append(torch.from_numpy(rng.normal(size=(n_out, n_in)) * std).to(**f32).contiguous())
-            self.b.append(torch.zeros(n_out, **f32))
+            n_in, n_out = (self.sizes[l] if l < 2 else self.k3), self.sizes[l + 1]
+            bound = (1.0 / n_in) ** 0.5 * (1.0 if l < 2 else 0.1)
+            self.W.append(torch.from_numpy(rng.uniform(-bound, bound, size=(n_out, n_in))).to(**f32).contiguous())
+            self.b.append(torch.from_numpy(rng.uniform(-bound, bound, size=n_out) if l < 2 else _np.zeros(n_out))
+                          .to(**f32))
             for lst, shape in ((self.mW, (n_out, n_in)), (self.vW, (n_out, n_in)), (self.gW, (n_out, n_in)),
                                (self.mb, (n_out,)), (self.vb, (n_out,)), (self.gb, (n_out,))):
                 lst.append(torch.zeros(shape, **f32))
@@ -92,14 +108,18 @@ class MLPSurrogate:
         d, h1, h2 = self.sizes[0], self.sizes[1], self.sizes[2]
         pB = _pad(B)
         z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=dev)  # noqa: E731
+        # A2 holds [h2 | x] per row: the second hidden activations and the input
+        A2 = z((B, _pad(self.k3)), bf)
+        A2t = z((self.k3, pB), bf)
         b = {
-            "X": z((B, _pad(d)), bf),
+            "A2": A2, "A2t": A2t,
+            "X": A2[:, h2:], "Xt": A2t[h2:],
             "Z1": z((B, h1), f32), "A1": z((B, _pad(h1)), bf), "A1t": z((h1, pB), bf),
-            "Z2": z((B, h2), f32), "A2": z((B, _pad(h2)), bf), "A2t": z((h2, pB), bf),
+            "Z2": z((B, h2), f32),
         }
         if training:
             b.update({
-                "idx": z((B,), torch.int32), "Xt": z((d, pB), bf), "T": z((B, d), f32), "Y": z((B, d), f32),
+                "idx": z((B,), torch.int32), "T": z((B, d), f32), "Y": z((B, d), f32),
                 "dY": z((B, _pad(d)), bf), "dYt": z((d, pB), bf),
                 "dZ2": z((B, _pad(h2)), bf), "dZ2t": z((h2, pB), bf),
                 "dZ1": z((B, _pad(h1)), bf), "dZ1t": z((h1, pB), bf),
@@ -129,15 +149,16 @@ class MLPSurrogate:
     def _forward(self, b, B, stream, g_state=None):
         d, h1, h2 = self.sizes[0], self.sizes[1], self.sizes[2]
         pB = _pad(B)
+        lda2 = b["A2"].shape[1]
         o1 = self._out(z=b["Z1"], ldz=h1, act=b["A1"], ld_act=_pad(h1), act_t=b["A1t"], ld_act_t=pB)
-        self._mm(_lib.HMC_MLP_HIDDEN, B, h1, d, b["X"], _pad(d), 0, self.b[0], o1, stream)
-        o2 = self._out(z=b["Z2"], ldz=h2, act=b["A2"], ld_act=_pad(h2), act_t=b["A2t"], ld_act_t=pB)
+        self._mm(_lib.HMC_MLP_HIDDEN, B, h1, d, b["X"], lda2, 0, self.b[0], o1, stream)
+        o2 = self._out(z=b["Z2"], ldz=h2, act=b["A2"], ld_act=lda2, act_t=b["A2t"], ld_act_t=pB)
         self._mm(_lib.HMC_MLP_HIDDEN, B, h2, h1, b["A1"], _pad(h1), 1, self.b[1], o2, stream)
         if g_state is None:
             o3 = self._out(y=b["Y"], ldy=d)
         else:
             o3 = self._out(g_state=g_state, out_scale=self.sig_g, out_shift=self.mu_g)
-        self._mm(_lib.HMC_MLP_OUT, B, d, h2, b["A2"], _pad(h2), 2, self.b[2], o3, stream)
+        self._mm(_lib.HMC_MLP_OUT, B, d, self.k3, b["A2"], lda2, 2, self.b[2], o3, stream)
 
     # ---- normalisation ---------------------------------------------------
     def fit_normalization(self, data: TrainingSet):
@@ -153,6 +174,14 @@ class MLPSurrogate:
         self.mu_g.copy_(g.mean(dim=0).float())
         self.sig_g.copy_(sg.float())
         self.inv_g.copy_((1.0 / sg).float())
+        # linear skip initialised to the ridge least-squares map x -> y
+        x = ((q - q.mean(dim=0)) / sq).cpu().numpy()
+        y = ((g - g.mean(dim=0)) / sg).cpu().numpy()
+        lam = 1e-3 * n
+        ws = _np.linalg.solve(x.T @ x + lam * _np.eye(self.d), x.T @ y).T  # [d_out][d_in]
+        h2 = self.sizes[2]
+        self.W[2][:, h2:] = torch.from_numpy(ws).float().to(self.device)
+        self._cast(_dev.stream_handle())
         torch.cuda.synchronize(self.device)
 
     # ---- training --------------------------------------------------------
@@ -170,12 +199,12 @@ class MLPSurrogate:
         b["idx"].copy_(torch.from_numpy(_np.asarray(idx_host, _np.int32)), non_blocking=False)
         _lib.call("hmc_mlp_gather", B, d, b["idx"].data_ptr(), data.q.data_ptr(), data.g.data_ptr(),
                   self.mu_q.data_ptr(), self.inv_q.data_ptr(), self.mu_g.data_ptr(), self.inv_g.data_ptr(),
-                  b["X"].data_ptr(), _pad(d), b["Xt"].data_ptr(), pB, b["T"].data_ptr(), d, h)
+                  b["X"].data_ptr(), b["A2"].shape[1], b["Xt"].data_ptr(), pB, b["T"].data_ptr(), d, h)
         self._forward(b, B, h)
         _lib.call("hmc_mlp_loss", B, d, b["Y"].data_ptr(), d, b["T"].data_ptr(), d, b["dY"].data_ptr(), _pad(d),
                   b["dYt"].data_ptr(), pB, self.loss_buf.data_ptr(), h)
-        # layer 3
-        self._wgrad(h2, d, B, b["A2t"], pB, b["dYt"], 2, h)
+        # layer 3 (its input is [h2 | x])
+        self._wgrad(self.k3, d, B, b["A2t"], pB, b["dYt"], 2, h)
         _lib.call("hmc_mlp_bias_grad", d, B, b["dYt"].data_ptr(), pB, self.gb[2].data_ptr(), h)
         o = self._out(z=b["Z2"], ldz=h2, act=b["dZ2"], ld_act=_pad(h2), act_t=b["dZ2t"], ld_act_t=pB)
         self._mm(_lib.HMC_MLP_BACK, B, h2, d, b["dY"], _pad(d), 2, None, o, h, transposed_w=True)
@@ -229,7 +258,7 @@ class MLPSurrogate:
         C = q.shape[1]
         b = self._buffers(C, False)
         _lib.call("hmc_mlp_input", self.d, C, q.data_ptr(), self.mu_q.data_ptr(), self.inv_q.data_ptr(),
-                  b["X"].data_ptr(), _pad(self.d), stream)
+                  b["X"].data_ptr(), b["A2"].shape[1], stream)
         self._forward(b, C, stream, g_state=g)
 
     def check_status(self):

@@ -348,7 +348,8 @@ HMC_API int hmc_tc_mlp(int mode, int64_t M, int64_t N, int64_t K,
                        int64_t ldw, const float* bias, const hmc_mlp_out* out,
                        int* status, void* stream);
 /* Network input from the sampler state: x[c][i] = bf16((q[i][c] - mu[i]) *
- * inv_sigma[i]) for q [d][C]; x is [C][ldx].                                */
+ * inv_sigma[i]) for q [d][C]; x is [C][ldx], and only its d leading
+ * columns are written.                                                     */
 HMC_API int hmc_mlp_input(int64_t d, int64_t C, const float* q, const float* mu,
                           const float* inv_sigma, void* x, int64_t ldx,
                           void* stream);

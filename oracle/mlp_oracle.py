@@ -40,3 +40,14 @@ def adam(w, g, m, v, lr, b1, b2, eps, step):
     mh = m / (1 - b1**step)
     vh = v / (1 - b2**step)
     return w - lr * mh / (np.sqrt(vh) + eps), m, v
+
+
+def predict(q, mu_q, inv_q, mu_g, sig_g, W, b):
+    """Surrogate gradient at positions q [d][C] with weights W (FP32 masters,
+    rounded to BF16 here) and biases b: the output layer reads [h2 | x]."""
+    x = bf16(((q.T - mu_q) * inv_q).astype(np.float32))
+    w16 = [bf16(w) for w in W]
+    _, a1 = hidden(x, w16[0], b[0])
+    _, a2 = hidden(a1, w16[1], b[1])
+    y = np.c_[a2, x] @ w16[2].T + b[2]
+    return (y * sig_g + mu_g).T
