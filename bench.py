@@ -1,24 +1,35 @@
 """Benchmark of the batched HMC hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload dense]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload fwi|dense]
 
 A "step" is one HMC proposal (a full leapfrog trajectory plus the accept test)
 for every chain of the workload.  Prints one JSON line.
 
-Workload `dense` (the batched dense linear configuration): G 2000x1000 with
-N(0, 1/1000) entries, m_true ~ N(0, I), noise sigma 0.05, Normal prior N(0, I),
-diagonal mass drawn U[0.5, 2], 20 leapfrog steps, 4096 chains, FP32 state,
-FP64 dH accept.  Chains start at exact draws of the analytic posterior, so
-every timed proposal is a post-burn-in sample.
+Workload `fwi` (default; the metric's configuration): 2-D elastic P-SV
+waveform inversion, 200x100 cells plus a 20-cell sponge, 1500 time steps, 4
+shots, 20 receivers, 600 blob parameters, Normal prior of 10%, 64 chains.
+W exact-gradient burn-in proposals record (position, gradient) pairs; the MLP
+surrogate is trained on them on the device; then K surrogate-driven proposals
+(interior gradients from the network, exact misfit for the accept test) and
+--plain-steps plain proposals (exact gradients) are timed from the same
+start.  `value` is the surrogate run's min-ESS/s; `plain` and
+`speedup_vs_plain` give the comparison.
+
+Workload `dense`: G 2000x1000 with N(0, 1/1000) entries, m_true ~ N(0, I),
+noise sigma 0.05, Normal prior N(0, I), diagonal mass drawn U[0.5, 2], 20
+leapfrog steps, 4096 chains, FP32 state, FP64 dH accept.  Chains start at exact
+draws of the analytic posterior, so every timed proposal is a post-burn-in
+sample.
 
 metric: min over parameters of the multi-chain ESS of the timed proposals'
 samples, divided by the device time of those proposals (min-ESS/s).
 Synthetic seeded data; the L2 cache is flushed (256 MiB write) between timed
 steps, outside the CUDA-event intervals.
 
---impl reference: the CPU implementation of the same path (the numpy port of
-the reference algorithm, batched over chains, all host BLAS threads) on a
-bounded sample of the workload, same metric and unit.
+--impl reference: the CPU implementation of the same path on the host cores:
+for `dense`, the numpy port of the reference algorithm batched over chains on
+a bounded sample; for `fwi`, the FP64 C restatement of the stencils timed on
+full-size shots, one per core.  Same metric and unit.
 """
 import argparse
 import json
@@ -51,8 +62,10 @@ def peaks():
 # ---------------------------------------------------------------------------
 class DenseWorkload:
     name = "dense-linear G2000x1000, Normal prior, diag mass, L=20, 4096 chains, FP32"
+    kind = "dense"
     n_data, n_model, chains, L = 2000, 1000, 4096, 20
     noise = 0.05
+    default_steps, default_warmup = 100, 5
 
     def __init__(self, seed=0, chains=None):
         from hmclab_gb300 import problems
@@ -100,7 +113,83 @@ class DenseWorkload:
                 "start": "exact posterior draws"}
 
 
-WORKLOADS = {"dense": DenseWorkload}
+# ---------------------------------------------------------------------------
+# Workload: 2-D elastic FWI, surrogate-driven vs plain batched HMC, 64 chains
+# ---------------------------------------------------------------------------
+# Plain-HMC min-ESS per chain-proposal on the FWI workload, measured by this
+# bench's GPU arm (the `plain.ess_per_chain_proposal` field of its line); the
+# reference arm, which can only afford to time the CPU cost of a proposal,
+# converts that cost into min-ESS/s with it.
+FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.241
+
+
+class FwiWorkload:
+    name = ("elastic P-SV FWI 200x100 cells (+20-cell sponge), h=5 m, dt=0.5 ms, nt=1500, 4 shots x 20 receivers, "
+            "25 Hz Ricker, blobs 20x10 x (vp,vs,rho) = 600 params, Normal prior 10%, 64 chains, FP32 stencils, "
+            "MLP 600-512-512-600 surrogate vs plain HMC")
+    kind = "fwi"
+    chains, L = 64, 10
+    stepsize = 0.12  # prior-whitened units: the mass matrix is the prior precision
+    noise_fraction = 10.0  # data noise std / RMS of the true records
+    hidden = (512, 512)
+    default_steps, default_warmup = 100, 12
+
+    def __init__(self, seed=0, chains=None):
+        from hmclab_gb300 import fwi as F
+
+        if chains is not None:
+            self.chains = chains
+        self.seed = seed
+        self.cfg = F.ElasticConfig()
+        self.cells = self.cfg.nxc * self.cfg.nzc
+        self.built = False
+
+    def build(self):
+        """Synthesise the observed records on the device (forward of the true
+        model plus noise) and draw the chains' starting points."""
+        from hmclab_gb300 import problems
+
+        pb = problems.elastic_fwi(self.cfg, 20, 10, prior_fraction=0.1, noise_fraction=self.noise_fraction,
+                                  seed=self.seed)
+        self.pb = pb
+        self.d = pb["likelihood"].dimensions
+        rng = np.random.default_rng(self.seed + 11)
+        self.q0 = pb["m_true"][:, None] + 0.3 * pb["prior_std"][:, None] * rng.normal(size=(self.d, self.chains))
+        self.built = True
+        return self
+
+    def posterior(self):
+        return self.pb["posterior"]
+
+    def mass(self):
+        import hmclab_gb300 as H
+
+        return H.MassMatrices.Diagonal(1.0 / self.pb["prior_std"] ** 2)
+
+    def sampler_kwargs(self):
+        return dict(stepsize=self.stepsize, amount_of_steps=self.L, mass_matrix=self.mass(), chains=self.chains,
+                    dtype="float32")
+
+    # algorithmic HBM bytes of one forward time step (velocity + stress
+    # kernels) for all chains: velocity phase reads vx, vz, sxx, szz, sxz, bx,
+    # bz and writes vx, vz; stress phase reads vx, vz, sxx, szz, sxz, l2m, lam,
+    # muxz and writes sxx, szz, sxz: 20 FP32 words per cell and chain
+    def stencil_bytes_per_step(self):
+        return 80.0 * self.cells * self.chains
+
+    def config(self):
+        return {"workload": self.name, "grid": [self.cfg.nx, self.cfg.nz], "sponge_cells": self.cfg.pad,
+                "nt": self.cfg.nt, "shots": self.cfg.n_shots, "receivers": self.cfg.n_rec, "params": 600,
+                "chains": self.chains, "leapfrog_steps": self.L, "stepsize": self.stepsize,
+                "stepsize_units": "prior-whitened (diagonal mass = prior precision), randomised x U(0.5,1.5)",
+                "prior": "Normal(background, (10% of background at blob centre)^2)",
+                "noise": f"{self.noise_fraction} x RMS of the true records (seeded Gaussian)",
+                "surrogate": "MLP 600-512-512-600 GELU + linear skip, BF16 weights, FP32 accumulate",
+                "precision": "FP32 state and stencils, FP64 dH", "l2": "flushed between timed steps (256 MiB write)",
+                "start": "end states of the exact burn-in"}
+
+
+WORKLOADS = {"dense": DenseWorkload, "fwi": FwiWorkload}
 
 
 # ---------------------------------------------------------------------------
@@ -336,25 +425,265 @@ def run_gpu_arm(args, wl):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+def fwi_cpu_costs(wl, cores):
+    """Seconds of one forward and one forward+adjoint shot of the FP64 C
+    restatement (oracle/fwi_oracle.c) on the full grid, `cores` shots at once
+    on a spawn process pool (one task per core); returns the medians and the
+    wall time."""
+    import multiprocessing as mp
+
+    from oracle import build_oracle
+    from oracle import fwi as OF
+    from hmclab_gb300 import fwi as F
+
+    build_oracle.build()
+    cfg = wl.cfg
+    bg = F.layered_model(cfg, anomalies=True)
+    vp, vs, rho = (cfg.extend(f) for f in bg)
+    tasks = [(cfg.nxc, cfg.nzc, cfg.nt, cfg.h, cfg.dt, cfg.taper(), cfg.ricker(), cfg.src[k % cfg.n_shots],
+              cfg.rec_x, cfg.rec_z, rho, vp, vs) for k in range(cores)]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(OF.timed_shot, tasks)
+    wall = time.perf_counter() - t0
+    return float(np.median([r[0] for r in res])), float(np.median([r[1] for r in res])), wall
+
+
+def fwi_cpu_rate(wl, cores):
+    """CPU chain-proposals/s of plain HMC on the FWI workload: L exact
+    gradients (4 shots forward + adjoint) plus one misfit (4 forward shots)
+    per chain-proposal, one chain per core."""
+    t_fwd, t_grad, wall = fwi_cpu_costs(wl, cores)
+    per_chain_proposal = wl.cfg.n_shots * (wl.L * t_grad + t_fwd)
+    return cores / per_chain_proposal, t_fwd, t_grad, wall
+
+
+def run_fwi_reference_arm(args, wl):
+    cores = os.cpu_count()
+    rate, t_fwd, t_grad, wall = fwi_cpu_rate(wl, cores)
+    e = FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL
+    value = rate * e if e is not None else None
+    sample = (f"{cores} full-size shots (forward {t_fwd:.2f} s, forward+adjoint {t_grad:.2f} s each, FP64 C "
+              f"restatement, one per core, {wall:.1f} s wall); chain-proposals/s = cores / (4 shots x (L x "
+              f"gradient + misfit)) = {rate:.4g}, times the plain-HMC min-ESS per chain-proposal measured on "
+              f"the GPU ({e})")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": 1, "warmup": 0,
+        "ms_per_step": 1e3 * wl.chains / rate, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference", "config": wl.config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "chain_proposals_per_s": rate,
+    }
+    print(json.dumps(line))
+
+
+def timed_proposals(smp, K, flush, evs):
+    import torch
+
+    for k in range(K):
+        with torch.cuda.stream(smp.stream):
+            flush.fill_(float(k))
+            evs[k][0].record(smp.stream)
+        smp.run(1)
+        evs[k][1].record(smp.stream)
+    smp.stream.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+
+def forward_step_timing(lik, smp, n_iter=2):
+    """Seconds of one forward time step (velocity + stress kernel) over all
+    chains: the exact misfit (4 shots x nt steps of the two stencil kernels,
+    plus the blob-to-grid GEMMs and the misfit reduction) timed with CUDA
+    events on the sampler stream, divided by shots x nt."""
+    import torch
+
+    st = smp.stream
+    h = st.cuda_stream
+    out = torch.empty(smp.chains, dtype=torch.float64, device=smp.q.device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        lik._device_misfit(smp.q_cur, out, False, "float32", h)
+        ev0.record(st)
+        for _ in range(n_iter):
+            lik._device_misfit(smp.q_cur, out, False, "float32", h)
+        ev1.record(st)
+    st.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / n_iter / (lik.config.n_shots * lik.config.nt)
+
+
+def run_fwi_arm(args, wl):
+    import torch
+
+    import hmclab_gb300 as H
+    from hmclab_gb300 import _lib, diagnostics
+    from hmclab_gb300 import surrogate as S
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    t_setup = time.perf_counter()
+    wl.build()
+    post, lik = wl.posterior(), wl.pb["likelihood"]
+    d, C, L = wl.d, wl.chains, wl.L
+    K, W, Kp = args.steps, args.warmup, args.plain_steps
+    kw = wl.sampler_kwargs()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t_setup = time.perf_counter() - t_setup
+
+    # ---- exact burn-in, recording (position, gradient) pairs -------------
+    data = S.TrainingSet(d, W * L * C)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    burn = H.Samplers.HMC(seed=100 + rank).sample(None, post, initial_model=wl.q0, proposals=W, training_set=data,
+                                                  **kw)
+    t_burn = time.perf_counter() - t0
+    q_start = burn.current_model
+    acc_burn = float(np.mean(burn.accepted_proposals) / W)
+
+    # ---- surrogate training on the device ---------------------------------
+    net = S.MLPSurrogate(d, hidden=wl.hidden, seed=rank)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fit = net.fit(data, steps=args.train_steps, batch=256, lr=1e-3, holdout_fraction=0.1)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    net.freeze()
+
+    # ---- timed: surrogate-driven HMC --------------------------------------
+    kw_s = dict(kw, amount_of_steps=args.surrogate_L, stepsize=args.surrogate_stepsize)
+
+    def timed_run(seed, n, surrogate):
+        smp = H.Samplers.HMC(seed=seed)
+        smp.prepare(None, post, initial_model=q_start, proposals=n, keep_samples=True, surrogate=surrogate,
+                    **(kw_s if surrogate is not None else kw))
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        torch.cuda.synchronize()
+        l0 = _lib.launch_count()
+        t = timed_proposals(smp, n, flush, evs)
+        launches = _lib.launch_count() - l0
+        return smp, t, launches, [a.elapsed_time(b) / 1e3 for a, b in evs]
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    smp_s, t_s, launches, _ = timed_run(200 + rank, K, net)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t_step = forward_step_timing(lik, smp_s)
+    smp_s.finish()
+    qs = smp_s.samples_device[0]  # [K][d][C]
+    ess_s = np.abs(diagnostics.ess(qs, lags=min(K // 2, 100)))
+    acc_s = float(np.mean(smp_s.accepted_proposals) / K)
+
+    # ---- timed: plain HMC (exact gradients), same start -------------------
+    smp_p, t_p, _, per_p = timed_run(300 + rank, Kp, None)
+    smp_p.finish()
+    qp = smp_p.samples_device[0]
+    ess_p = np.abs(diagnostics.ess(qp, lags=max(2, Kp // 2)))
+    acc_p = float(np.mean(smp_p.accepted_proposals) / Kp)
+    if world > 1:
+        t = torch.tensor(np.concatenate([ess_s, ess_p, [t_s, t_p]]), dtype=torch.float64)
+        parts = [torch.zeros_like(t) for _ in range(world)]
+        torch.distributed.all_gather(parts, t)
+        ess_s = sum(p[:d].numpy() for p in parts)
+        ess_p = sum(p[d:2 * d].numpy() for p in parts)
+        t_s = max(float(p[-2]) for p in parts)
+        t_p = max(float(p[-1]) for p in parts)
+    value = float(ess_s.min() / t_s)
+    plain_value = float(ess_p.min() / t_p)
+    mean_s, std_s = diagnostics.moments(qs)
+    mean_p, std_p = diagnostics.moments(qp)
+    me, se = diagnostics.moment_error(mean_s, std_s, mean_p, std_p)
+    e_plain = float(ess_p.min() / (C * world * Kp))
+
+    # ---- end to end through the public API with host buffers -------------
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    smp_e = H.Samplers.HMC(seed=400 + rank).sample(None, post, initial_model=q_start, proposals=K,
+                                                   keep_samples=True, surrogate=net, **kw_s)
+    host_q, host_x = smp_e.samples_host()
+    t_e2e = time.perf_counter() - t0
+    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K // 2, 100)))
+    e2e_value = float(ess_e.min() / t_e2e)
+
+    hbm, bf16, bf16s, src = peaks()
+    achieved = wl.stencil_bytes_per_step() / t_step / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * t_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; records from the device forward of the true model + noise)",
+        "config": wl.config(),
+        "speedup_vs_plain": float(value / plain_value),
+        "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": args.surrogate_L,
+                                                      "stepsize": args.surrogate_stepsize},
+        "plain": {"value": plain_value, "steps": Kp, "ms_per_step": 1e3 * t_p / Kp, "acceptance": acc_p,
+                  "ess_per_chain_proposal": e_plain},
+        "moment_error_vs_plain": {"mean": me, "std": se,
+                                  "mc_floor": float(1.0 / np.sqrt(max(1.0, ess_p.min())))},
+        "burn_in": {"proposals": W, "seconds": t_burn, "acceptance": acc_burn, "pairs": data.count},
+        "surrogate": {"train_steps": args.train_steps, "train_seconds": t_train, "train_pairs": fit["train_pairs"],
+                      "heldout_pairs": fit["heldout_pairs"], "loss_first": fit["history"][0][1],
+                      "loss_last": fit["history"][-1][1], "heldout_rel_error_linear_start": fit["heldout"][0][1],
+                      "heldout_rel_error": fit["best_heldout"], "best_step": fit["best_step"],
+                      "heldout_curve": [[k, round(e, 5)] for k, e in fit["heldout"]]},
+        "setup_seconds": t_setup,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(q_start.size * 8 / K),
+                "d2h_bytes_per_step": int(d * C * 4 + C * 8), "seconds": t_e2e},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "fwi forward time step: velocity_kernel + stress_kernel (the exact misfit)",
+                     "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_source": src, "step_s": t_step,
+                     "algorithmic_bytes_per_step": wl.stencil_bytes_per_step()},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count()
+        rate, t_fwd, t_grad, wall = fwi_cpu_rate(wl, cores)
+        line["cpu_baseline"] = {
+            "value": rate * e_plain, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"{cores} full-size shots of the FP64 C restatement, one per core ({wall:.1f} s wall; "
+                       f"forward {t_fwd:.2f} s, forward+adjoint {t_grad:.2f} s); chain-proposals/s = {rate:.4g} "
+                       f"times the plain-HMC min-ESS per chain-proposal of this run ({e_plain:.4g})")}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="dense", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
+    ap.add_argument("--plain-steps", type=int, default=12, help="fwi: timed proposals of plain HMC")
+    ap.add_argument("--train-steps", type=int, default=3000, help="fwi: Adam steps of the surrogate")
+    ap.add_argument("--surrogate-L", type=int, default=4, help="fwi: leapfrog steps of the surrogate-driven run")
+    ap.add_argument("--surrogate-stepsize", type=float, default=0.06, help="fwi: its step size (whitened units)")
     ap.add_argument("--cpu-chains", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    assert args.warmup >= 3, "at least 3 warm-up steps"
     wl = WORKLOADS[args.workload]()
+    args.steps = wl.default_steps if args.steps is None else args.steps
+    args.warmup = wl.default_warmup if args.warmup is None else args.warmup
+    assert args.warmup >= 3, "at least 3 warm-up steps"
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
-        run_reference_arm(args, wl)
+        (run_fwi_reference_arm if args.workload == "fwi" else run_reference_arm)(args, wl)
         return
-    run_gpu_arm(args, wl)
+    (run_fwi_arm if args.workload == "fwi" else run_gpu_arm)(args, wl)
 
 
 if __name__ == "__main__":

@@ -54,22 +54,28 @@ class _AbstractDistribution:
     upper_bounds: _Union[_numpy.ndarray, None] = None
     normalized: bool = False
     normalization_constant: float = 0.0
+    # arithmetic type of the single-vector misfit()/gradient() calls
+    single_dtype: str = "float64"
+    # False when the device calls launch CUDA graphs of their own or need the
+    # host between launches: the sampler then issues proposals uncaptured
+    graph_safe: bool = True
 
     # ---- reference-facing single-vector API -------------------------------
     def misfit(self, coordinates: _numpy.ndarray) -> float:
-        """chi(m) for one column vector (d,1), in FP64 on the GPU
-        (reference `base.py:70-105`); +inf outside the bounds."""
+        """chi(m) for one column vector (d,1), on the GPU in `single_dtype`
+        (FP64 unless the target's kernels are FP32 only; reference
+        `base.py:70-105`); +inf outside the bounds."""
         m = _column(coordinates, self.dimensions)
-        x = self.misfit_batch(_dev.upload(m, "float64"))
+        x = self.misfit_batch(_dev.upload(m, self.single_dtype))
         return float(x.cpu()[0]) + self.normalization_constant + self.misfit_bounds(m)
 
     def gradient(self, coordinates: _numpy.ndarray) -> _numpy.ndarray:
-        """d chi / d m for one column vector, in FP64 on the GPU (reference
-        `base.py:140-168`); the bound misfit (0 or +inf) is added like the
-        reference does."""
+        """d chi / d m for one column vector, on the GPU in `single_dtype`
+        (reference `base.py:140-168`), returned as FP64; the bound misfit (0 or
+        +inf) is added like the reference does."""
         m = _column(coordinates, self.dimensions)
-        g = self.gradient_batch(_dev.upload(m, "float64"))
-        return g.cpu().numpy().reshape(self.dimensions, 1) + self.misfit_bounds(m)
+        g = self.gradient_batch(_dev.upload(m, self.single_dtype))
+        return g.double().cpu().numpy().reshape(self.dimensions, 1) + self.misfit_bounds(m)
 
     def misfit_v(self, coordinates: _numpy.ndarray, vectors_in_dim=None):
         """Misfits of many vectors at once (reference `base.py:107-138`), as
@@ -364,9 +370,18 @@ class AdditiveDistribution(_AbstractDistribution):
         self.upper_bounds = upper_bounds
         self.collapse_bounds()
 
+    @property
+    def single_dtype(self):
+        dts = {d.single_dtype for d in self.separate_distributions}
+        return "float32" if "float32" in dts else "float64"
+
+    @property
+    def graph_safe(self):
+        return all(d.graph_safe for d in self.separate_distributions)
+
     def misfit(self, coordinates):
         m = _column(coordinates, self.dimensions)
-        x = self.misfit_batch(_dev.upload(m, "float64"))
+        x = self.misfit_batch(_dev.upload(m, self.single_dtype))
         const = sum(d.normalization_constant for d in self.separate_distributions)
         bounds = sum(d.misfit_bounds(m) for d in self.separate_distributions)
         return float(x.cpu()[0]) + const + bounds + self.misfit_bounds(m)
@@ -645,6 +660,10 @@ class ElasticFullWaveform2D(_AbstractDistribution):
     (ElasticFullWaveform2D.py:159, 329-330)."""
 
     temperature: float = 1.0
+    # the stencils run in FP32 only; single-vector calls use one FP32 chain
+    single_dtype = "float32"
+    # each shot is a CUDA graph of its own, replayed from the host
+    graph_safe = False
 
     def __init__(self, _input, ux_obs=None, uz_obs=None, temperature=None, omp_threads_override=None,
                  free_parameter_grid=None, data_std=1.0, background=None, gradient_projection="chain_rule"):
@@ -849,6 +868,20 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             else:
                 _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(), None,
                           dst.data_ptr(), int(accumulate), stream)
+
+    def synthetic_records(self, m):
+        """Receiver records (ux, uz), each [shots][nt][receivers], of one blob
+        model vector, computed by the device forward (FP32)."""
+        import torch
+
+        cfg = self.config
+        M = _dev.upload(_numpy.asarray(m, _numpy.float64).reshape(self.dimensions, 1), "float32")
+        ws = self._workspace(1, M.device, False)
+        s = torch.cuda.current_stream(M.device)
+        self._forward_all(M, ws, s.cuda_stream, False)
+        s.synchronize()
+        r = ws["rec"].double().cpu().numpy().reshape(cfg.n_shots, cfg.nt, cfg.n_rec, 2)
+        return r[..., 0].copy(), r[..., 1].copy()
 
     def last_misfit(self, C, out, stream=None):
         """Misfit of the model of the last gradient call (its forward records

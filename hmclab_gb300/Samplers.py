@@ -16,8 +16,16 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
                 in the reference's draw order (reproduces the reference's
                 chain for chains=1); or an explicit tuple (z, f, u) of arrays
                 shaped [P][d][C], [P][C], [P][C]
-  graph         capture each block of proposals in a CUDA graph (default True)
+  graph         capture each block of proposals in a CUDA graph (default True;
+                targets whose `graph_safe` is False, e.g. the elastic FWI
+                misfit with its own per-shot graphs, run uncaptured)
   keep_samples  keep every thinned sample on the device (`samples_device`)
+  surrogate     a frozen `surrogate.MLPSurrogate`: it supplies every gradient
+                of the leapfrog; the exact misfit at the trajectory end still
+                decides acceptance, so the chain targets the exact posterior
+  training_set  a `surrogate.TrainingSet` that receives every exact
+                (position, gradient) pair the trajectories evaluate, until it
+                is full (burn-in data for the surrogate; runs uncaptured)
 
 Each proposal is issued as: begin (momentum, K0, first drift) -> for every
 kick: gradient of the target on the device, then kick+drift -> misfit at the
@@ -135,6 +143,8 @@ class HMC:
         graph: bool = True,
         proposals_per_graph: int = None,
         keep_samples: bool = False,
+        surrogate=None,
+        training_set=None,
     ):
         """Run `proposals` HMC proposals for every chain; returns self.
 
@@ -148,7 +158,7 @@ class HMC:
             diagnostic_mode=diagnostic_mode, overwrite_existing_file=overwrite_existing_file, max_time=max_time,
             autotuning=autotuning, target_acceptance_rate=target_acceptance_rate, learning_rate=learning_rate,
             chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
-            keep_samples=keep_samples,
+            keep_samples=keep_samples, surrogate=surrogate, training_set=training_set,
         )
         self._run()
         return self
@@ -377,9 +387,10 @@ class HMC:
         self.stream.wait_stream(_torch.cuda.current_stream(dev))
         h = self.stream.cuda_stream
         self.distribution._device_misfit(self.q_cur, self.x_cur, False, dt, h)
-        # Allocate every scratch buffer of the target before any capture.
-        self.distribution._device_gradient(self.q_cur, self.g, False, dt, h)
-        self.distribution._device_misfit(self.q_cur, self.x_prop, False, dt, h)
+        if self.use_graph:
+            # allocate every scratch buffer of the target before any capture
+            self.distribution._device_gradient(self.q_cur, self.g, False, dt, h)
+            self.distribution._device_misfit(self.q_cur, self.x_prop, False, dt, h)
         self.stream.synchronize()
         x0 = self.x_cur.cpu().numpy()
         assert not _numpy.any(_numpy.isnan(x0)), "Initial position in model space gives NaN probability"
@@ -388,7 +399,11 @@ class HMC:
         self._graph = None
         from hmclab_gb300._dense_tc import FusedDenseStep
 
-        self._fused = FusedDenseStep.applies(self)
+        self._fused = (
+            None if (self.surrogate is not None or self.training_set is not None) else FusedDenseStep.applies(self)
+        )
+        if self.surrogate is not None:
+            self.surrogate._buffers(C, False)  # allocate before any capture
 
     # ------------------------------------------------------------------
     def _issue_proposal(self, h):
@@ -410,7 +425,12 @@ class HMC:
             return
         for needs_grad, kick, drift in steps:
             if needs_grad:
-                dist._device_gradient(self.q, self.g, False, dt, h)
+                if self.surrogate is not None:
+                    self.surrogate.predict_into(self.q, self.g, h)
+                else:
+                    dist._device_gradient(self.q, self.g, False, dt, h)
+                    if self.training_set is not None:
+                        self.training_set.record(self.q, self.g, h)
             _lib.call("hmc_kick_drift", st, kick, drift, h)
         dist._device_misfit(self.q, self.x_prop, False, dt, h)
         _lib.call("hmc_end_trajectory", st, h)
@@ -464,6 +484,7 @@ class HMC:
             initial_model=None, proposals=100, online_thinning=1, diagnostic_mode=False, overwrite_existing_file=False,
             max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
             dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
+            surrogate=None, training_set=None,
         )
         unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
         if unknown:
@@ -477,6 +498,7 @@ class HMC:
             a["target_acceptance_rate"], a["learning_rate"], a["chains"], a["dtype"], a["rng_streams"], a["graph"],
             a["proposals_per_graph"], a["keep_samples"],
         )
+        self._parse_surrogate(a["surrogate"], a["training_set"])
         self._setup_device()
         self._open_files()
         self._done = 0
@@ -484,6 +506,19 @@ class HMC:
         self._start_time = _datetime.now()
         self._launches0 = _lib.launch_count()
         return self
+
+    def _parse_surrogate(self, surrogate, training_set):
+        self.surrogate = surrogate
+        self.training_set = training_set
+        for obj, what in ((surrogate, "surrogate"), (training_set, "training_set")):
+            if obj is None:
+                continue
+            assert self.dtype == "float32", f"`{what}` needs float32 chains"
+            assert obj.d == self.dimensions, f"`{what}` has {obj.d} dimensions, the target {self.dimensions}"
+        if surrogate is not None:
+            assert surrogate.frozen, "freeze() the surrogate before sampling with it (the chain must see a fixed field)"
+        if training_set is not None or not self.distribution.graph_safe:
+            self.use_graph = False
 
     def run(self, n_proposals):
         """Enqueue the next `n_proposals` proposals (whole graph blocks where

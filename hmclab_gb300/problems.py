@@ -8,6 +8,8 @@ of the sampling hot path.
   tomography     straight-ray travel-time tomography on a square grid, CSR ray
                  lengths from exact ray/cell intersections (Siddon 1985)
   source_loc     3-D earthquake location with surface stations (homogeneous v)
+  elastic_fwi    2-D elastic P-SV waveform inversion in Gaussian-blob
+                 parameters (data from the device forward of the true model)
 """
 import numpy as _np
 import scipy.sparse as _sparse
@@ -155,3 +157,46 @@ def source_location(n_events=32, n_stations=200, box=40.0, depth=10.0, v=5.0, no
     m[3:-1:4, 0] = et[:, 0]
     m[-1, 0] = v
     return dict(rx=sx, ry=sy, rz=sz, obs=obs, std=_np.full_like(obs, noise_std), m_true=m)
+
+
+# ---------------------------------------------------------------------------
+# 2-D elastic full-waveform inversion
+# ---------------------------------------------------------------------------
+def elastic_fwi(cfg=None, nbx=20, nbz=10, prior_fraction=0.1, noise_fraction=0.5, seed=0):
+    """Blob-parametrised elastic FWI posterior (needs the CUDA device: the
+    observed records are the device forward of the true model plus noise).
+
+    Model vector m = [vp | vs | rho] blob amplitudes (m/s, m/s, kg/m^3) added
+    to the layered background.  The true model is the least-squares blob fit
+    of the layered model with its two Gaussian anomalies.  Prior: Normal with
+    mean 0 (the background) and standard deviation `prior_fraction` times the
+    background value at each blob centre.  Data noise: Gaussian with standard
+    deviation `noise_fraction` times the RMS of the true records.
+
+    Returns a dict with the posterior (BayesRule of prior and likelihood), the
+    likelihood, the prior, m_true, prior_std and data_std."""
+    from hmclab_gb300 import Distributions as D
+    from hmclab_gb300 import fwi as F
+
+    cfg = cfg or F.ElasticConfig()
+    rng = _np.random.default_rng(seed)
+    bg = F.layered_model(cfg, anomalies=False)
+    truth = F.layered_model(cfg, anomalies=True)
+    blob = F.BlobBasis(cfg, nbx, nbz)
+    m_true = _np.concatenate([blob.fit(truth[f] - bg[f]) for f in range(3)])
+    zeros = _np.zeros((cfg.n_shots, cfg.nt, cfg.n_rec))
+    fwd = D.ElasticFullWaveform2D(cfg, zeros, zeros, free_parameter_grid=[nbx, nbz], background=bg)
+    ux, uz = fwd.synthetic_records(m_true)
+    rms = float(_np.sqrt(_np.mean(ux**2 + uz**2) / 2.0))
+    data_std = noise_fraction * rms
+    ux = ux + data_std * rng.normal(size=ux.shape)
+    uz = uz + data_std * rng.normal(size=uz.shape)
+    lik = D.ElasticFullWaveform2D(cfg, ux, uz, data_std=data_std, free_parameter_grid=[nbx, nbz], background=bg)
+    # background value at each blob centre (blob index = ibx * nbz + ibz)
+    X, Z = cfg.cell_centres()
+    centre = _np.argmax(blob.B, axis=0)
+    prior_std = _np.concatenate([prior_fraction * bg[f].reshape(-1)[centre] for f in range(3)])
+    prior = D.Normal(_np.zeros((lik.dimensions, 1)), (prior_std**2).reshape(-1, 1))
+    post = D.BayesRule([prior, lik])
+    return dict(posterior=post, likelihood=lik, prior=prior, m_true=m_true, prior_std=prior_std, data_std=data_std,
+                config=cfg)

@@ -161,12 +161,20 @@ class MLPSurrogate:
         self._mm(_lib.HMC_MLP_OUT, B, d, self.k3, b["A2"], lda2, 2, self.b[2], o3, stream)
 
     # ---- normalisation ---------------------------------------------------
-    def fit_normalization(self, data: TrainingSet):
+    def fit_normalization(self, data: TrainingSet, rows=None):
+        """Per-coordinate input/target normalisation and the least-squares
+        start of the linear skip, from the stored pairs (or the given rows)."""
         import torch
 
         n = data.count
-        q = data.q[:n].double()
-        g = data.g[:n].double()
+        if rows is None:
+            q = data.q[:n].double()
+            g = data.g[:n].double()
+        else:
+            r = torch.as_tensor(_np.asarray(rows), device=self.device)
+            q = data.q[r].double()
+            g = data.g[r].double()
+            n = len(rows)
         sq = q.std(dim=0).clamp_min(1e-12)
         sg = g.std(dim=0).clamp_min(1e-12)
         self.mu_q.copy_(q.mean(dim=0).float())
@@ -233,10 +241,11 @@ class MLPSurrogate:
         _lib.call("hmc_tc_mlp", _lib.HMC_MLP_WGRAD, n_in, n_out, B, act_t.data_ptr(), ld_act_t, delta_t.data_ptr(),
                   delta_t.shape[1], None, ctypes.byref(o), self.status.data_ptr(), stream)
 
-    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None):
-        """Fit the network on data with Adam; returns the loss history (host)."""
+    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
+        """Fit the network with Adam on the first `rows` pairs of data (all by
+        default); returns the loss history (host)."""
         rng = _np.random.default_rng(seed)
-        n = data.count
+        n = data.count if rows is None else min(int(rows), data.count)
         assert n >= batch, "not enough training pairs"
         history = []
         for s in range(steps):
@@ -247,6 +256,51 @@ class MLPSurrogate:
                 history.append((s, float(loss[0].item())))
         self.check_status()
         return history
+
+    def fit(self, data: TrainingSet, steps=3000, batch=256, lr=1e-3, holdout_fraction=0.1, check_every=200,
+            seed=0, stream=None):
+        """Train with early stopping: a random `holdout_fraction` of the stored
+        pairs is held out, and every `check_every` steps its relative error
+        is measured; the weights with the lowest one are kept.  Returns a
+        dict with the loss history, the held-out errors (step 0 is the
+        least-squares linear start) and the best step."""
+        import torch
+
+        n = data.count
+        rng = _np.random.default_rng(seed)
+        perm = rng.permutation(n)
+        n_hold = max(1, int(round(holdout_fraction * n)))
+        held = torch.from_numpy(_np.sort(perm[:n_hold])).to(self.device)
+        train_rows = _np.sort(perm[n_hold:])
+        assert len(train_rows) >= batch, "not enough training pairs"
+        self.fit_normalization(data, rows=train_rows)
+        err0 = self.relative_error(data, held, stream=stream)
+        best = (err0, 0, [w.clone() for w in self.W], [b.clone() for b in self.b])
+        errors = [(0, err0)]
+        history = []
+        done = 0
+        while done < steps:
+            chunk = min(check_every, steps - done)
+            for s in range(chunk):
+                k = done + s
+                rate = lr * 0.5 * (1 + _np.cos(_np.pi * k / steps))
+                idx = train_rows[rng.integers(0, len(train_rows), size=batch)]
+                loss = self.train_step(data, idx, lr=float(rate), stream=stream)
+                if k % 50 == 0:
+                    history.append((k, float(loss[0].item())))
+            done += chunk
+            e = self.relative_error(data, held, stream=stream)
+            errors.append((done, e))
+            if e < best[0]:
+                best = (e, done, [w.clone() for w in self.W], [b.clone() for b in self.b])
+        self.check_status()
+        for l in range(3):
+            self.W[l].copy_(best[2][l])
+            self.b[l].copy_(best[3][l])
+        self._cast(_dev.stream_handle(stream))
+        torch.cuda.synchronize(self.device)
+        return {"history": history, "heldout": errors, "best_step": best[1], "best_heldout": best[0],
+                "train_pairs": len(train_rows), "heldout_pairs": n_hold}
 
     def freeze(self):
         self.frozen = True
@@ -260,6 +314,20 @@ class MLPSurrogate:
         _lib.call("hmc_mlp_input", self.d, C, q.data_ptr(), self.mu_q.data_ptr(), self.inv_q.data_ptr(),
                   b["X"].data_ptr(), b["A2"].shape[1], stream)
         self._forward(b, C, stream, g_state=g)
+
+    def relative_error(self, data: TrainingSet, rows, stop=None, stream=None):
+        """|f(q) - g| / |g| (Frobenius norms) over stored pairs of data: the
+        rows [rows, stop) when `stop` is given, else the index tensor `rows`.
+        The held-out error when those pairs were not trained on."""
+        import torch
+
+        sel = slice(rows, stop) if stop is not None else rows
+        q = data.q[sel].t().contiguous()
+        g = data.g[sel].t().contiguous()
+        out = torch.empty_like(g)
+        self.predict_into(q, out, _dev.stream_handle(stream))
+        torch.cuda.synchronize(self.device)
+        return float(torch.linalg.norm((out - g).double()) / torch.linalg.norm(g.double()))
 
     def check_status(self):
         from hmclab_gb300.Helpers.CustomExceptions import DeviceTimeoutError

@@ -66,3 +66,20 @@ class Shot:
                                  _p(np.ascontiguousarray(obs_vx, np.float64)),
                                  _p(np.ascontiguousarray(obs_vz, np.float64)), float(w), *[_p(x) for x in g])
         return chi, g  # g = [g_rho, g_vp, g_vs]
+
+
+def timed_shot(task):
+    """CPU cost of one shot of the FP64 restatement: returns (forward seconds,
+    forward + adjoint gradient seconds).  `task` = (nx, nz, nt, h, dt, taper,
+    stf, src, rec_x, rec_z, rho, vp, vs); used as a process-pool task to time
+    the CPU baseline on every host core at once."""
+    import time
+
+    nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z, rho, vp, vs = task
+    shot = Shot(nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z)
+    t0 = time.perf_counter()
+    ovx, ovz = shot.forward(rho, vp, vs)
+    t1 = time.perf_counter()
+    shot.gradient(rho, vp * 1.01, vs, ovx, ovz, 1.0)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
