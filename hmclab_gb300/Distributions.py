@@ -762,6 +762,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             ws["store"] = z(cfg.nt * 2 * cells * C)
             ws["resid"] = z(cfg.nt * cfg.n_rec * 2 * C)
             ws["gtmp"] = z(self.blob.n_blobs, C)
+            ws["proj_work"] = z(64 * self.blob.n_blobs * C)  # split-k partial products
         return ws
 
     def _descriptor(self, ws, C):
@@ -860,14 +861,15 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         cells = self.config.nzc * self.config.nxc
         for f, name in enumerate(("g_vp", "g_vs", "g_rho")):
             dst = out[f * nb:(f + 1) * nb]
+            work, nwork = ws["proj_work"].data_ptr(), ws["proj_work"].numel()
             if self.gradient_projection == "least_squares":
-                _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(), None,
-                          ws["gtmp"].data_ptr(), 0, stream)
+                _lib.call("hmc_gemm_splitk", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(),
+                          ws["gtmp"].data_ptr(), 0, work, nwork, stream)
                 _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, nb, 1.0, p["proj"].data_ptr(), ws["gtmp"].data_ptr(),
                           None, dst.data_ptr(), int(accumulate), stream)
             else:
-                _lib.call("hmc_gemm", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(), None,
-                          dst.data_ptr(), int(accumulate), stream)
+                _lib.call("hmc_gemm_splitk", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(),
+                          dst.data_ptr(), int(accumulate), work, nwork, stream)
 
     def synthetic_records(self, m):
         """Receiver records (ux, uz), each [shots][nt][receivers], of one blob

@@ -161,6 +161,7 @@ SIGNATURES = {
     "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
+    "hmc_gemm_splitk": [I, I64, I64, I64, D, P, P, P, I, P, I64, S],
     "hmc_split_bf16": [I64, I64, P, I64, P, P, S],
     "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],
     "hmc_tc_gradient": [I64, I64, I64, P, P, I64, P, P, I64, P, P, I, P, S],

@@ -47,6 +47,30 @@ __device__ __forceinline__ float dxm(const float* __restrict__ f, int k, int s, 
   return (C1 * (f[k] - f[k - s]) + C2 * (f[k + s] - f[k - 2 * s])) * ih;
 }
 
+// Programmatic dependent launch: the stencil kernels of a time loop are
+// launched with programmatic stream serialisation, so the next step's CTAs
+// are scheduled while this step's last wave runs; every such kernel waits
+// for its predecessor grid (completion and memory visibility) before its
+// first memory access.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void step_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void step_dependents_go() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_step(bool overlap, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st,
+                        Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = overlap ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Thread mapping: block (32 chains, 8 cells along x), grid.x over (x tiles,
 // chain tiles), grid.y = row j.  No integer division per thread.
 constexpr int TX = 32, TY = 8;
@@ -95,6 +119,8 @@ struct Params {
 __global__ void __launch_bounds__(TX* TY) velocity_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
                                                             const int32_t* __restrict__ rec_map, float* rec_n,
                                                             float* store_n) {
+  step_dependency_wait();
+  step_dependents_go();
   const Cell e = cell_of(g);
   if (!e.in) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C;
@@ -122,6 +148,8 @@ __global__ void __launch_bounds__(TX* TY) velocity_kernel(Grid g, Fields f, Para
 
 __global__ void __launch_bounds__(TX* TY) stress_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
                                                           int src_i, int src_j, float src_value) {
+  step_dependency_wait();
+  step_dependents_go();
   const Cell e = cell_of(g);
   if (!e.in) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C;
@@ -162,6 +190,8 @@ __global__ void __launch_bounds__(TX* TY) adj_velocity_kernel(Grid g, Fields a, 
                                                                 const float* __restrict__ resid_n,
                                                                 const float* __restrict__ vn,
                                                                 const float* __restrict__ vprev) {
+  step_dependency_wait();
+  step_dependents_go();
   const Cell e = cell_of(g);
   if (!e.in || !g.valid(e.i, e.j)) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C, plane = g.nx * g.nz * g.C;
@@ -200,6 +230,8 @@ __global__ void __launch_bounds__(TX* TY) adj_velocity_kernel(Grid g, Fields a, 
 // of step n-1 (reverse of its stress taper); writes t1..t3 for step n-1.
 __global__ void __launch_bounds__(TX* TY) adj_stress_kernel(Grid g, Fields a, Params p, Temps tm,
                                                               const float* __restrict__ taper) {
+  step_dependency_wait();
+  step_dependents_go();
   const Cell e = cell_of(g);
   if (!e.in || !g.valid(e.i, e.j)) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C;
@@ -339,9 +371,14 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
   for (int n = 0; n < s->nt; ++n) {
     float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
     float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
-    velocity_kernel<<<grid, block, 0, st>>>(g, f, p, s->taper, s->rec_map, rec_n, store_n);
+    // the first launch follows the memsets: ordinary stream order
+    cudaError_t e = launch_step(n > 0, velocity_kernel, grid, block, st, g, f, p, s->taper, s->rec_map, rec_n,
+                                store_n);
+    if (e != cudaSuccess) return cuda_fail(e, "launch velocity_kernel");
     HMC_TRY(check_launch("velocity_kernel"));
-    stress_kernel<<<grid, block, 0, st>>>(g, f, p, s->taper, src_x, src_z, s->stf_host[n] * src_scale);
+    e = launch_step(true, stress_kernel, grid, block, st, g, f, p, s->taper, src_x, src_z,
+                    s->stf_host[n] * src_scale);
+    if (e != cudaSuccess) return cuda_fail(e, "launch stress_kernel");
     HMC_TRY(check_launch("stress_kernel"));
   }
   return HMC_OK;
@@ -383,10 +420,13 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   for (int n = s->nt - 1; n >= 0; --n) {
     const float* vn = s->store + (int64_t)n * 2 * cells;
     const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
-    adj_velocity_kernel<<<grid, block, 0, st>>>(g, a, p, gr, tm, s->taper, s->rec_map,
-                                                s->resid + (int64_t)n * s->nrec * 2 * s->chains, vn, vp);
+    // the first launch follows the residual kernel and memsets: ordinary stream order
+    cudaError_t e = launch_step(n < s->nt - 1, adj_velocity_kernel, grid, block, st, g, a, p, gr, tm, s->taper,
+                                s->rec_map, (const float*)(s->resid + (int64_t)n * s->nrec * 2 * s->chains), vn, vp);
+    if (e != cudaSuccess) return cuda_fail(e, "launch adj_velocity_kernel");
     HMC_TRY(check_launch("adj_velocity_kernel"));
-    adj_stress_kernel<<<grid, block, 0, st>>>(g, a, p, tm, s->taper);
+    e = launch_step(true, adj_stress_kernel, grid, block, st, g, a, p, tm, s->taper);
+    if (e != cudaSuccess) return cuda_fail(e, "launch adj_stress_kernel");
     HMC_TRY(check_launch("adj_stress_kernel"));
   }
   return HMC_OK;

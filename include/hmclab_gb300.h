@@ -458,6 +458,16 @@ HMC_API int hmc_fwi_param_gradient(const hmc_fwi* s, float* g_rho,
 HMC_API int hmc_gemm(int dtype, int64_t m, int64_t n, int64_t k, double alpha,
              const void* A, const void* B, const void* bias, void* out,
              int accumulate, void* stream);
+/* The same product without bias for a long k and a small m x n (the
+ * grid-to-blob projection of the FWI gradient, k = simulation cells): the
+ * k range is split over CTAs, each writes its partial product into work
+ * (work_elems elements of the dtype, at least m * n; more allows more
+ * splits), and a second kernel sums the partials in a fixed order, so the
+ * result is deterministic.                                                 */
+HMC_API int hmc_gemm_splitk(int dtype, int64_t m, int64_t n, int64_t k,
+                            double alpha, const void* A, const void* B,
+                            void* out, int accumulate, void* work,
+                            int64_t work_elems, void* stream);
 
 /* ---- effective sample size (no counterpart in the reference, whose only
  * mixing diagnostic is Helpers/Processing.py:6-13) --------------------------

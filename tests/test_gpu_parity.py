@@ -273,3 +273,35 @@ def test_philox_mode_targets_the_analytic_posterior(golden):
     assert np.max(np.abs(mean - g["post_mean"][:, 0]) / ref_std) < 0.1
     assert np.max(np.abs(std / ref_std - 1)) < 0.1
     assert 0.2 < np.mean(np.atleast_1d(smp.accepted_proposals)) / 60 < 1.0
+
+
+def test_split_k_product_matches_numpy_and_is_deterministic():
+    """hmc_gemm_splitk (the FWI grid-to-blob projection shape: m=200, n=64,
+    k=33600) against numpy in FP64 to 1e-12 and FP32 to 1e-5 of sum |a||b|;
+    two launches give bit-identical results; accumulate adds to out."""
+    rng = np.random.default_rng(11)
+    m, n, k = 200, 64, 33600
+    A = rng.normal(size=(m, k))
+    B = rng.normal(size=(k, n))
+    ref = A @ B
+    scale = np.abs(A) @ np.abs(B)
+    h = torch.cuda.current_stream().cuda_stream
+    for dt, code, tol in ((torch.float64, _lib.HMC_F64, 1e-12), (torch.float32, _lib.HMC_F32, 1e-5)):
+        a, b = dev(A, dt), dev(B, dt)
+        work = torch.empty(64 * m * n, dtype=dt, device="cuda")
+        outs = []
+        for _ in range(2):
+            out = torch.zeros((m, n), dtype=dt, device="cuda")
+            _lib.call("hmc_gemm_splitk", code, m, n, k, 0.5, a.data_ptr(), b.data_ptr(), out.data_ptr(), 0,
+                      work.data_ptr(), work.numel(), h)
+            outs.append(out.clone())
+        got = outs[0].double().cpu().numpy()
+        assert np.all(np.abs(got - 0.5 * ref) <= tol * 0.5 * scale)
+        assert torch.equal(outs[0], outs[1])
+        _lib.call("hmc_gemm_splitk", code, m, n, k, 1.0, a.data_ptr(), b.data_ptr(), out.data_ptr(), 1,
+                  work.data_ptr(), m * n * 3, h)  # three splits at most, accumulated onto 0.5 A B
+        got = out.double().cpu().numpy()
+        assert np.all(np.abs(got - 1.5 * ref) <= tol * 1.5 * scale)
+    with pytest.raises(ValueError):
+        _lib.call("hmc_gemm_splitk", _lib.HMC_F32, m, n, k, 1.0, a.data_ptr(), b.data_ptr(), out.data_ptr(), 0,
+                  work.data_ptr(), m * n - 1, h)
