@@ -753,6 +753,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             ws = {name: z(cells, C) for name in ("vp", "vs", "rho", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz",
                                                  "sxx", "szz", "sxz")}
             ws["rec"] = z(cfg.n_shots * cfg.nt * cfg.n_rec * 2 * C)
+            ws["partial"] = torch.zeros(64 * C, dtype=torch.float64, device=device)
             cache[key] = ws
         if with_gradient and "store" not in ws:
             z = lambda *shape: torch.zeros(shape, dtype=torch.float32, device=device)  # noqa: E731
@@ -774,7 +775,8 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         d.h, d.dt, d.w = cfg.h, cfg.dt, self.weight
         d.taper, d.rec_map, d.obs = p["taper"].data_ptr(), p["rec_map"].data_ptr(), p["obs"].data_ptr()
         d.stf_host = p["stf_host"].ctypes.data
-        for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec"):
+        for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec",
+                     "partial"):
             setattr(d, name, ws[name].data_ptr())
         for name in ("store", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam",
                      "g_muxz", "t1", "t2", "t3", "t4", "t5"):

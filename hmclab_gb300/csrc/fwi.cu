@@ -257,22 +257,35 @@ __global__ void residual_kernel(int64_t n_rows, int64_t C, const float* __restri
     resid[t] = w * (rec[t] - obs[t / C]);
 }
 
-__global__ void misfit_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec, const float* __restrict__ obs,
-                              double w, double* out, int accumulate) {
+// Misfit in two deterministic passes: blockIdx.y takes one of MISFIT_SPLITS
+// contiguous row ranges and writes its sum per chain to partial[y][c]; the
+// second kernel adds the ranges in order.
+constexpr int MISFIT_SPLITS = 64;
+__global__ void misfit_partial_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec,
+                                      const float* __restrict__ obs, double* partial) {
   __shared__ double sh[RED_Y][RED_X + 1];
   const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  const int64_t per = (n_rows + MISFIT_SPLITS - 1) / MISFIT_SPLITS;
+  const int64_t r0 = (int64_t)blockIdx.y * per, r1 = r0 + per < n_rows ? r0 + per : n_rows;
   double acc = 0.0;
   if (c < C) {
-    for (int64_t r = threadIdx.y; r < n_rows; r += RED_Y) {
+    for (int64_t r = r0 + threadIdx.y; r < r1; r += RED_Y) {
       const double d = (double)rec[r * C + c] - (double)obs[r];
       acc += d * d;
     }
   }
   const double s = block_chain_sum(acc, sh);
-  if (c < C && threadIdx.y == 0) {
-    const double v = 0.5 * w * s;
-    out[c] = accumulate ? out[c] + v : v;
-  }
+  if (c < C && threadIdx.y == 0) partial[blockIdx.y * C + c] = s;
+}
+
+__global__ void misfit_final_kernel(int64_t C, const double* __restrict__ partial, double w, double* out,
+                                    int accumulate) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  double s = 0.0;
+  for (int y = 0; y < MISFIT_SPLITS; ++y) s += partial[y * C + c];
+  const double v = 0.5 * w * s;
+  out[c] = accumulate ? out[c] + v : v;
 }
 
 // (bx, bz, l+2m, l, muxz) gradients -> (rho, vp, vs) gradients, all cells.
@@ -386,11 +399,15 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
 
 HMC_API int hmc_fwi_misfit(const hmc_fwi* s, int nshots, double* out_x, int accumulate, void* stream) {
   HMC_TRY(check_fwi(s, "hmc_fwi_misfit"));
-  HMC_REQUIRE(s->obs && out_x, "hmc_fwi_misfit: missing observations or output");
+  HMC_REQUIRE(s->obs && out_x && s->partial, "hmc_fwi_misfit: missing observations, output or partial buffer");
   const int64_t rows = (int64_t)nshots * s->nt * s->nrec * 2;
-  misfit_kernel<<<red_grid(s->chains), red_block(), 0, as_stream(stream)>>>(rows, s->chains, s->rec, s->obs,
-                                                                           (double)s->w, out_x, accumulate);
-  return check_launch("fwi misfit_kernel");
+  cudaStream_t st = as_stream(stream);
+  const dim3 grid(red_grid(s->chains).x, MISFIT_SPLITS);
+  misfit_partial_kernel<<<grid, red_block(), 0, st>>>(rows, s->chains, s->rec, s->obs, s->partial);
+  HMC_TRY(check_launch("fwi misfit_partial_kernel"));
+  misfit_final_kernel<<<blocks_for(s->chains, 128), 128, 0, st>>>(s->chains, s->partial, (double)s->w, out_x,
+                                                                   accumulate);
+  return check_launch("fwi misfit_final_kernel");
 }
 
 HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {

@@ -432,6 +432,7 @@ typedef struct hmc_fwi {
   float* t3;
   float* t4;
   float* t5;
+  double* partial;          /* [64][C] misfit partial sums (work)           */
 } hmc_fwi;
 
 /* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */

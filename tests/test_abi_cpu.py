@@ -65,20 +65,22 @@ def test_invalid_arguments_fail_before_any_launch(lib):
     assert rc == _lib.HMC_ERR_INVALID_ARG
 
 
-def test_chains_struct_layout_matches_c(tmp_path):
-    """Compile a probe with gcc that prints sizeof/offsetof of hmc_chains and
-    compare with the ctypes Structure."""
-    fields = [f for f, _ in _lib.HmcChains._fields_]
+@pytest.mark.parametrize("cname, cls", [("hmc_chains", _lib.HmcChains), ("hmc_fwi", _lib.HmcFwi),
+                                         ("hmc_mlp_out", _lib.HmcMlpOut)])
+def test_struct_layout_matches_c(tmp_path, cname, cls):
+    """Compile a probe with gcc that prints sizeof/offsetof of the C struct
+    and compare with the ctypes Structure."""
+    fields = [f for f, _ in cls._fields_]
     src = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){",
-           'printf("%zu\\n", sizeof(hmc_chains));']
+           f'printf("%zu\\n", sizeof({cname}));']
     for f in fields:
-        src.append(f'printf("%zu\\n", offsetof(hmc_chains, {f}));')
+        src.append(f'printf("%zu\\n", offsetof({cname}, {f}));')
     src.append("return 0;}")
     c = tmp_path / "probe.c"
     c.write_text("\n".join(src))
     exe = tmp_path / "probe"
     subprocess.run(["gcc", "-o", str(exe), str(c)], check=True)
     out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    assert out[0] == ctypes.sizeof(_lib.HmcChains)
+    assert out[0] == ctypes.sizeof(cls)
     for f, off in zip(fields, out[1:]):
-        assert getattr(_lib.HmcChains, f).offset == off, f
+        assert getattr(cls, f).offset == off, f
