@@ -106,11 +106,184 @@ class DenseWorkload:
     def gemm_flops(self):
         return 2.0 * self.n_model**2 * self.chains
 
+    def oracle(self):
+        from oracle import hmc_oracle as O
+
+        post = O.Sum([O.NormalDiag(np.zeros(self.n_model), np.ones(self.n_model)),
+                      O.DensePremul(self.G, self.d, self.noise**2)])
+        return post, O.Mass("diag", diag=self.diag)
+
+    def roofline_spec(self, smp):
+        fused = smp._fused is not None
+        return {"kernel": ("chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
+                           if fused else "dense gradient GEMM"),
+                "bound": "tensor", "unit": "TFLOP/s", "work": self.gemm_flops(),
+                "work_name": "algorithmic_flop_per_launch",
+                "extra": {"executed_flop_per_launch": 3 * self.gemm_flops() if fused else self.gemm_flops()}}
+
     def config(self):
         return {"workload": self.name, "n_data": self.n_data, "n_model": self.n_model, "chains": self.chains,
                 "leapfrog_steps": self.L, "stepsize": self.stepsize, "prior": "Normal(0, I)",
                 "mass": "diagonal U[0.5,2]", "precision": "FP32 state, FP64 dH", "l2": "flushed between timed steps",
                 "start": "exact posterior draws"}
+
+
+# ---------------------------------------------------------------------------
+# Workload: straight-ray tomography, CSR ray lengths, 1024 chains
+# ---------------------------------------------------------------------------
+class TomoWorkload:
+    name = ("straight-ray tomography 64x64 slowness cells, 2000 rays (CSR, exact lengths), noise 0.01 s, "
+            "Normal prior around the background (sigma 0.05), Jacobi diagonal mass, L=20, 1024 chains, FP32")
+    kind = "tomo"
+    chains, L = 1024, 20
+    noise, prior_std = 0.01, 0.05
+    default_steps, default_warmup = 100, 5
+
+    def __init__(self, seed=0, chains=None):
+        import scipy.sparse.linalg as spla
+
+        from hmclab_gb300 import problems
+
+        if chains is not None:
+            self.chains = chains
+        t = problems.tomography(64, 64, 2000, 1.0, self.noise, seed)
+        self.G, self.d, self.bg = t["G"], t["d"], t["background"]
+        self.n_data, self.n_model = self.G.shape
+        self.nnz = self.G.nnz
+        self.post_mean, self.post_cov = problems.gaussian_posterior(self.G, self.d, self.noise**2, self.bg,
+                                                                    self.prior_std**2)
+        self.post_std = np.sqrt(np.diag(self.post_cov))
+        A = np.linalg.inv(self.post_cov)
+        self.diag = np.diag(A).reshape(-1, 1).copy()
+        s = 1.0 / np.sqrt(self.diag[:, 0])
+        w_max = np.sqrt(spla.eigsh(s[:, None] * A * s[None, :], k=1, which="LA")[0][0])
+        self.stepsize = 0.6 / w_max
+        rng = np.random.default_rng(seed + 1)
+        self.q0 = self.post_mean + np.linalg.cholesky(self.post_cov) @ rng.normal(size=(self.n_model, self.chains))
+
+    def posterior(self):
+        import hmclab_gb300 as H
+
+        prior = H.Distributions.Normal(self.bg, np.full((self.n_model, 1), self.prior_std**2))
+        lik = H.Distributions.LinearMatrix(self.G, self.d, self.noise**2)
+        return H.Distributions.BayesRule([prior, lik])
+
+    def mass(self):
+        import hmclab_gb300 as H
+
+        return H.MassMatrices.Diagonal(self.diag)
+
+    def sampler_kwargs(self):
+        return dict(stepsize=self.stepsize, amount_of_steps=self.L, mass_matrix=self.mass(), chains=self.chains,
+                    dtype="float32")
+
+    def oracle(self):
+        from oracle import hmc_oracle as O
+
+        post = O.Sum([O.NormalDiag(self.bg, np.full(self.n_model, self.prior_std**2)),
+                      O.SparseLinear(self.G, self.d, self.noise**2)])
+        return post, O.Mass("diag", diag=self.diag)
+
+    # the gradient's two sparse products: G @ Q (minus data, weighted) and
+    # G^T @ R, each reading the CSR arrays once (8 B per nonzero: value +
+    # column) and streaming the dense operands (4 B per element, FP32)
+    def roofline_spec(self, smp):
+        C = self.chains
+        work = 2 * (8.0 * self.nnz + 4.0 * C * (self.n_data + self.n_model)) + 4.0 * (self.n_data + 1) * 2
+        # every nonzero also gathers a row of the dense operand (C values)
+        # from L2: the traffic the kernel actually moves
+        gather = 2 * 4.0 * self.nnz * C
+        return {"kernel": "csr_spmm_kernel x2 (G @ Q - d, G^T @ R)", "bound": "hbm", "unit": "GB/s", "work": work,
+                "work_name": "algorithmic_bytes_per_launch",
+                "extra": {"nnz": int(self.nnz), "l2_gather_bytes_per_launch": gather}}
+
+    def config(self):
+        return {"workload": self.name, "cells": self.n_model, "rays": self.n_data, "nnz": int(self.nnz),
+                "chains": self.chains, "leapfrog_steps": self.L, "stepsize": self.stepsize,
+                "prior": "Normal(background, 0.05^2)", "mass": "diagonal of the posterior precision",
+                "precision": "FP32 state, FP64 dH", "l2": "flushed between timed steps",
+                "start": "exact posterior draws"}
+
+
+# ---------------------------------------------------------------------------
+# Workload: 3-D source location, 32 events + velocity, 8192 chains
+# ---------------------------------------------------------------------------
+class SrclocWorkload:
+    name = ("3-D source location: 32 events (x, y, z, t0) + one velocity = 129 params, 200 surface stations, "
+            "40x40 km box, depth 0-10 km, v = 5 km/s, noise 0.05 s, full mass = Gauss-Newton Hessian at the truth, "
+            "L=5, 8192 chains, FP32")
+    kind = "srcloc"
+    chains, L = 8192, 5
+    noise = 0.05
+    default_steps, default_warmup = 100, 10
+
+    def __init__(self, seed=0, chains=None):
+        from hmclab_gb300 import problems
+
+        if chains is not None:
+            self.chains = chains
+        t = problems.source_location(32, 200, 40.0, 10.0, 5.0, self.noise, seed)
+        self.t = t
+        self.E, self.S = t["obs"].shape
+        self.n_model = 4 * self.E + 1
+        m = t["m_true"][:, 0]
+        # Gauss-Newton Hessian J^T J / sigma^2 of the arrival times at the truth
+        J = np.zeros((self.E * self.S, self.n_model))
+        v = m[-1]
+        for e in range(self.E):
+            dx, dy, dz = m[4 * e] - t["rx"][0], m[4 * e + 1] - t["ry"][0], m[4 * e + 2] - t["rz"][0]
+            dist = np.sqrt(dx * dx + dy * dy + dz * dz)
+            rows = slice(e * self.S, (e + 1) * self.S)
+            J[rows, 4 * e] = dx / (v * dist)
+            J[rows, 4 * e + 1] = dy / (v * dist)
+            J[rows, 4 * e + 2] = dz / (v * dist)
+            J[rows, 4 * e + 3] = 1.0
+            J[rows, -1] = -dist / v**2
+        self.H = J.T @ J / self.noise**2
+        self.stepsize = 0.8
+        rng = np.random.default_rng(seed + 1)
+        Lc = np.linalg.cholesky(np.linalg.inv(self.H))
+        self.q0 = t["m_true"] + Lc @ rng.normal(size=(self.n_model, self.chains))
+        self.post_mean = self.post_std = None
+
+    def posterior(self):
+        import hmclab_gb300 as H
+
+        t = self.t
+        return H.Distributions.SourceLocation3D(t["rx"], t["ry"], t["rz"], t["obs"], self.noise)
+
+    def mass(self):
+        import hmclab_gb300 as H
+
+        return H.MassMatrices.Full(self.H)
+
+    def sampler_kwargs(self):
+        return dict(stepsize=self.stepsize, amount_of_steps=self.L, mass_matrix=self.mass(), chains=self.chains,
+                    dtype="float32")
+
+    def oracle(self):
+        from oracle import hmc_oracle as O
+
+        t = self.t
+        post = O.SourceLocation3D(t["rx"], t["ry"], t["rz"], t["obs"], t["std"])
+        return post, O.Mass("full", full=self.H)
+
+    # FP32 operations per (chain, event, station) pair of the gradient: the
+    # distance (3 sub, 3 mul/fma, sqrt), travel time and residual (div, add,
+    # sub, mul), four partials (mul, div, mul each) and their sums
+    FLOP_PER_PAIR = 23
+
+    def roofline_spec(self, smp):
+        work = float(self.FLOP_PER_PAIR) * self.chains * self.E * self.S
+        return {"kernel": "srcloc_kernel<float, true> (one thread per chain and event lane)", "bound": "fp32",
+                "unit": "TFLOP/s", "work": work, "work_name": "algorithmic_flop_per_launch",
+                "extra": {"pairs_per_launch": self.chains * self.E * self.S}}
+
+    def config(self):
+        return {"workload": self.name, "events": self.E, "stations": self.S, "params": self.n_model,
+                "chains": self.chains, "leapfrog_steps": self.L, "stepsize": self.stepsize,
+                "mass": "full (Gauss-Newton Hessian at the true model)", "precision": "FP32 state, FP64 dH",
+                "l2": "flushed between timed steps", "start": "draws of the Laplace approximation + warm-up"}
 
 
 # ---------------------------------------------------------------------------
@@ -189,7 +362,7 @@ class FwiWorkload:
                 "start": "end states of the exact burn-in"}
 
 
-WORKLOADS = {"dense": DenseWorkload, "fwi": FwiWorkload}
+WORKLOADS = {"dense": DenseWorkload, "tomo": TomoWorkload, "srcloc": SrclocWorkload, "fwi": FwiWorkload}
 
 
 # ---------------------------------------------------------------------------
@@ -251,9 +424,7 @@ def cpu_reference_run(wl, chains, warmup, steps, seed=0):
     chains: returns (min-ESS/s, moment errors, seconds, chain-steps/s)."""
     from oracle import hmc_oracle as O
 
-    lik = O.DensePremul(wl.G, wl.d, wl.noise**2)
-    post = O.Sum([O.NormalDiag(np.zeros(wl.n_model), np.ones(wl.n_model)), lik])
-    mass = O.Mass("diag", diag=wl.diag)
+    post, mass = wl.oracle()
     rng = np.random.default_rng(seed + 7)
     q0 = wl.q0[:, :chains]
     P = warmup + steps
@@ -270,8 +441,11 @@ def cpu_reference_run(wl, chains, warmup, steps, seed=0):
     ess, _ = O.ess_split(x, lags=max(2, steps // 2))
     ess = np.abs(ess)
     mean, std = x.mean(axis=(0, 2)), x.std(axis=(0, 2))
-    me = float(np.max(np.abs(mean - wl.post_mean[:, 0]) / wl.post_std))
-    se = float(np.max(np.abs(std - wl.post_std) / wl.post_std))
+    if wl.post_mean is not None:
+        me = float(np.max(np.abs(mean - wl.post_mean[:, 0]) / wl.post_std))
+        se = float(np.max(np.abs(std - wl.post_std) / wl.post_std))
+    else:
+        me = se = None
     return float(ess.min() / dt), (me, se), dt, chains * steps * wl.L / dt
 
 
@@ -302,7 +476,7 @@ def dominant_kernel_timing(post, smp, n_iter=20):
 
     st = smp.stream
     h = st.cuda_stream
-    lik = post.separate_distributions[1]
+    lik = post.separate_distributions[1] if hasattr(post, "separate_distributions") else post
     if smp._fused is not None:
         smp._fused.after_begin(h)
 
@@ -378,7 +552,10 @@ def run_gpu_arm(args, wl):
         torch.distributed.all_gather(parts, t)
         ess = sum(p[:-1].numpy() for p in parts)
         t_dev = max(float(p[-1]) for p in parts)
-    me, se = diagnostics.moment_error(mean, std, wl.post_mean, wl.post_std)
+    if wl.post_mean is not None:
+        me, se = diagnostics.moment_error(mean, std, wl.post_mean, wl.post_std)
+    else:
+        me = se = None
     value = float(ess.min() / t_dev)
     acc = float(np.mean(smp.accepted_proposals) / (W + K))
 
@@ -396,7 +573,14 @@ def run_gpu_arm(args, wl):
     d2h = (wl.n_model * wl.chains * 4 + wl.chains * 8)
 
     hbm, bf16, bf16s, src = peaks()
-    achieved = wl.gemm_flops() / t_gemm / 1e12
+    spec = wl.roofline_spec(smp)
+    if spec["bound"] == "tensor":
+        peak, psrc, scale = bf16, src, 1e12
+    elif spec["bound"] == "hbm":
+        peak, psrc, scale = hbm, src, 1e9
+    else:  # FP32 issue rate: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz, nominal
+        peak, psrc, scale = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal", 1e12
+    achieved = spec["work"] / t_gemm / scale
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -406,12 +590,9 @@ def run_gpu_arm(args, wl):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds": t_e2e},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": ("chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
-                                if smp._fused is not None else "dense gradient GEMM"),
-                     "bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": None, "peak_source": src, "launch_s": t_gemm,
-                     "algorithmic_flop_per_launch": wl.gemm_flops(),
-                     "executed_flop_per_launch": 3 * wl.gemm_flops() if smp._fused is not None else wl.gemm_flops()},
+        "roofline": {"kernel": spec["kernel"], "bound": spec["bound"], "achieved": achieved, "peak": peak,
+                     "unit": spec["unit"], "frac": achieved / peak, "traffic": None, "peak_source": psrc,
+                     "launch_s": t_gemm, spec["work_name"]: spec["work"], **spec["extra"]},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

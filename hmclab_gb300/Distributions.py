@@ -492,6 +492,12 @@ class LinearMatrix(_AbstractDistribution):
             G = self.G
             Gt = self.G.T.tocsr()
             Gt.sort_indices()
+            # the device kernels index the dense operand with these columns
+            for A in (G, Gt):
+                if A.nnz and not (0 <= int(A.indices.min()) and int(A.indices.max()) < A.shape[1]):
+                    raise ValueError("sparse matrix column index out of range")
+                if len(A.indptr) != A.shape[0] + 1 or int(A.indptr[-1]) != A.nnz or _numpy.any(_numpy.diff(A.indptr) < 0):
+                    raise ValueError("malformed sparse row pointers")
             p["rp"], p["col"], p["val"] = _dev.upload_int32(G.indptr), _dev.upload_int32(G.indices), _dev.upload(G.data, dtype)
             p["trp"], p["tcol"], p["tval"] = (
                 _dev.upload_int32(Gt.indptr),

@@ -104,6 +104,8 @@ class HMC:
     integrators_full_names = {"lf": "leapfrog integrator", "3s": "three stage integrator", "4s": "four stage integrator"}
     available_integrators = integrators_full_names.keys()
     minimal_stepsize = 1e-18
+    surrogate = None
+    training_set = None
 
     def __init__(self, seed: int = None):
         self.seed = seed

@@ -159,16 +159,30 @@ __global__ void csr_spmm_kernel(int64_t rows, int64_t C, const int32_t* __restri
   if (j >= rows || c >= C) return;
   T acc = (T)0;
   const int32_t b = rp[j], e = rp[j + 1];
-  for (int32_t k = b; k < e; ++k) acc += val[k] * X[(int64_t)col[k] * C + c];
+  int32_t k = b;
+  // four nonzeros at a time: their rows of X are loaded together (four
+  // coalesced 128-byte requests in flight per warp), then accumulated in CSR
+  // order, so the sum equals the one-at-a-time loop's
+  for (; k + 4 <= e; k += 4) {
+    const T x0 = X[(int64_t)col[k] * C + c], x1 = X[(int64_t)col[k + 1] * C + c];
+    const T x2 = X[(int64_t)col[k + 2] * C + c], x3 = X[(int64_t)col[k + 3] * C + c];
+    acc += val[k] * x0;
+    acc += val[k + 1] * x1;
+    acc += val[k + 2] * x2;
+    acc += val[k + 3] * x3;
+  }
+  for (; k < e; ++k) acc += val[k] * X[(int64_t)col[k] * C + c];
   if (bias) acc -= bias[j];
   if (rs) acc *= rs[j];
   const int64_t o = j * C + c;
   out[o] = accumulate ? out[o] + acc : acc;
 }
 
+// X has x_rows rows (the column count of the sparse matrix) and C columns.
 template <typename T>
-int csr_spmm(int64_t rows, int64_t C, const int32_t* rp, const int32_t* col, const void* val, const void* X,
-             const void* bias, const void* rs, void* out, int accumulate, cudaStream_t st) {
+int csr_spmm(int64_t rows, int64_t x_rows, int64_t C, const int32_t* rp, const int32_t* col, const void* val,
+             const void* X, const void* bias, const void* rs, void* out, int accumulate, cudaStream_t st) {
+  (void)x_rows;
   HMC_REQUIRE(rows <= 65535 * 1024ll, "csr: too many rows");
   const int threads = C >= 256 ? 256 : (C >= 128 ? 128 : (C >= 64 ? 64 : 32));
   dim3 grid((unsigned)((C + threads - 1) / threads), 1);
@@ -188,7 +202,7 @@ int csr_spmm(int64_t rows, int64_t C, const int32_t* rp, const int32_t* col, con
 // One thread per (chain, event); stations are staged in shared memory.  The
 // per-pair terms mirror SourceLocation.py:495-540, including nansum's skipping
 // of NaN terms (missing observations, zero distances).
-constexpr int SL_EY = 8;  // event lanes per block (threadIdx.y)
+constexpr int SL_EY = 16;  // event lanes per block (threadIdx.y)
 
 template <typename T, bool GRAD>
 __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restrict__ M, const T* __restrict__ rx,
@@ -209,6 +223,7 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
   const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
   const bool live = c < C;
   const T v = live ? (infer_v ? M[(4 * E) * C + c] : v_fixed) : (T)1;
+  const T inv_v = (T)1 / v;
   double mis = 0.0;
   T gv = (T)0;
   if (live) {
@@ -220,7 +235,7 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
       for (int64_t s = 0; s < S; ++s) {
         const T dx = x - srx[s], dy = y - sry[s], dz = z - srz[s];
         const T dist = sqrt(dx * dx + dy * dy + dz * dz);
-        const T tc = t0 + dist / v;
+        const T tc = t0 + dist * inv_v;
         const T o = obs[e * S + s], w = iv[e * S + s];
         if (!GRAD) {
           const T r = o - tc;
@@ -228,16 +243,18 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
           if (!isnan(term)) me += (double)term;
         } else {
           const T mg = (tc - o) * w;  // (t_calc - obs) / std^2
-          const T vd = v * dist;
+          // one reciprocal per pair; at dist = 0 the partials are 0 * inf =
+          // NaN and skipped, like nansum's 0 / 0
+          const T inv_vd = inv_v / dist;
           T t;
-          t = mg * (dx / vd);
+          t = mg * (dx * inv_vd);
           if (!isnan(t)) gx += t;
-          t = mg * (dy / vd);
+          t = mg * (dy * inv_vd);
           if (!isnan(t)) gy += t;
-          t = mg * (dz / vd);
+          t = mg * (dz * inv_vd);
           if (!isnan(t)) gz += t;
           if (!isnan(mg)) gT += mg;
-          t = mg * (-dist / (v * v));
+          t = mg * (-dist * inv_v * inv_v);
           if (!isnan(t)) gv += t;
         }
       }
@@ -429,7 +446,7 @@ int hmc_csr_misfit(int dtype, int64_t n, int64_t d, int64_t C, const void* M, co
   HMC_REQUIRE(M && row_ptr && col && val && data && inv_var && resid && out_x, "hmc_csr_misfit: null argument");
   cudaStream_t st = as_stream(stream);
   return HMC_DISPATCH(dtype, T, [&] {
-    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, nullptr, resid, 0, st));
+    HMC_TRY(csr_spmm<T>(n, d, C, row_ptr, col, val, M, data, nullptr, resid, 0, st));
     weighted_sq_kernel<T><<<red_grid(C), red_block(), 0, st>>>(n, C, (const T*)resid, (const T*)inv_var, out_x,
                                                                accumulate);
     return check_launch("weighted_sq_kernel");
@@ -446,8 +463,8 @@ int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C, const void* M, 
               "hmc_csr_gradient: null argument");
   cudaStream_t st = as_stream(stream);
   return HMC_DISPATCH(dtype, T, [&] {
-    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
-    return csr_spmm<T>(d, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
+    HMC_TRY(csr_spmm<T>(n, d, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
+    return csr_spmm<T>(d, n, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
   });
 }
 

@@ -30,9 +30,7 @@ def dense_linear(n_data, n_model, g_std, noise_std, seed):
 def gaussian_posterior(G, d, noise_var, prior_mean, prior_var):
     """Analytic posterior of a linear Gaussian problem with a diagonal prior:
     Sigma = (G^T G / s^2 + P^-1)^-1, mu = Sigma (G^T d / s^2 + P^-1 mu_p)."""
-    G = _np.asarray(G, float)
-    if _sparse.issparse(G):
-        G = G.toarray()
+    G = G.toarray() if _sparse.issparse(G) else _np.asarray(G, float)
     pm = _np.broadcast_to(_np.asarray(prior_mean, float).reshape(-1, 1), (G.shape[1], 1))
     piv = 1.0 / _np.broadcast_to(_np.asarray(prior_var, float).reshape(-1), (G.shape[1],))
     A = G.T @ G / noise_var + _np.diag(piv)
