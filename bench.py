@@ -784,6 +784,10 @@ def run_fwi_arm(args, wl):
     mean_s, std_s = diagnostics.moments(qs)
     mean_p, std_p = diagnostics.moments(qp)
     me, se = diagnostics.moment_error(mean_s, std_s, mean_p, std_p)
+    # the same posterior mean in both runs? z = difference / its Monte Carlo
+    # standard error (std / sqrt(ESS) per run); for exact chains |z| ~ N(0, 1)
+    se_mean = np.sqrt(std_s**2 / np.maximum(ess_s, 1.0) + std_p**2 / np.maximum(ess_p, 1.0))
+    z = np.abs(mean_s - mean_p) / np.maximum(se_mean, 1e-300)
     e_plain = float(ess_p.min() / (C * world * Kp))
 
     # ---- end to end through the public API with host buffers -------------
@@ -809,7 +813,8 @@ def run_fwi_arm(args, wl):
         "plain": {"value": plain_value, "steps": Kp, "ms_per_step": 1e3 * t_p / Kp, "acceptance": acc_p,
                   "ess_per_chain_proposal": e_plain},
         "moment_error_vs_plain": {"mean": me, "std": se,
-                                  "mc_floor": float(1.0 / np.sqrt(max(1.0, ess_p.min())))},
+                                  "mc_floor": float(1.0 / np.sqrt(max(1.0, ess_p.min()))),
+                                  "mean_z_max": float(z.max()), "mean_z_frac_above_3": float(np.mean(z > 3.0))},
         "burn_in": {"proposals": W, "seconds": t_burn, "acceptance": acc_burn, "pairs": data.count},
         "surrogate": {"train_steps": args.train_steps, "train_seconds": t_train, "train_pairs": fit["train_pairs"],
                       "heldout_pairs": fit["heldout_pairs"], "loss_first": fit["history"][0][1],

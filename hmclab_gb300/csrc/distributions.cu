@@ -178,11 +178,9 @@ __global__ void csr_spmm_kernel(int64_t rows, int64_t C, const int32_t* __restri
   out[o] = accumulate ? out[o] + acc : acc;
 }
 
-// X has x_rows rows (the column count of the sparse matrix) and C columns.
 template <typename T>
-int csr_spmm(int64_t rows, int64_t x_rows, int64_t C, const int32_t* rp, const int32_t* col, const void* val,
-             const void* X, const void* bias, const void* rs, void* out, int accumulate, cudaStream_t st) {
-  (void)x_rows;
+int csr_spmm(int64_t rows, int64_t C, const int32_t* rp, const int32_t* col, const void* val, const void* X,
+             const void* bias, const void* rs, void* out, int accumulate, cudaStream_t st) {
   HMC_REQUIRE(rows <= 65535 * 1024ll, "csr: too many rows");
   const int threads = C >= 256 ? 256 : (C >= 128 ? 128 : (C >= 64 ? 64 : 32));
   dim3 grid((unsigned)((C + threads - 1) / threads), 1);
@@ -446,7 +444,7 @@ int hmc_csr_misfit(int dtype, int64_t n, int64_t d, int64_t C, const void* M, co
   HMC_REQUIRE(M && row_ptr && col && val && data && inv_var && resid && out_x, "hmc_csr_misfit: null argument");
   cudaStream_t st = as_stream(stream);
   return HMC_DISPATCH(dtype, T, [&] {
-    HMC_TRY(csr_spmm<T>(n, d, C, row_ptr, col, val, M, data, nullptr, resid, 0, st));
+    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, nullptr, resid, 0, st));
     weighted_sq_kernel<T><<<red_grid(C), red_block(), 0, st>>>(n, C, (const T*)resid, (const T*)inv_var, out_x,
                                                                accumulate);
     return check_launch("weighted_sq_kernel");
@@ -463,8 +461,8 @@ int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C, const void* M, 
               "hmc_csr_gradient: null argument");
   cudaStream_t st = as_stream(stream);
   return HMC_DISPATCH(dtype, T, [&] {
-    HMC_TRY(csr_spmm<T>(n, d, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
-    return csr_spmm<T>(d, n, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
+    HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
+    return csr_spmm<T>(d, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
   });
 }
 
