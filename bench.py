@@ -501,11 +501,9 @@ def run_gpu_arm(args, wl):
     import torch
 
     import hmclab_gb300 as H
-    from hmclab_gb300 import _lib, diagnostics
+    from hmclab_gb300 import _lib, diagnostics, sharding
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, world, local = sharding.rank_environment()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -516,7 +514,7 @@ def run_gpu_arm(args, wl):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     # ---- device-resident timed run ---------------------------------------
-    smp = H.Samplers.HMC(seed=1000 + rank)
+    smp = H.Samplers.HMC(seed=sharding.rank_seed(1000, rank))
     smp.prepare(None, post, initial_model=wl.q0, proposals=W + K, keep_samples=True, proposals_per_graph=1,
                 **wl.sampler_kwargs())
     smp.run(W)
@@ -546,12 +544,8 @@ def run_gpu_arm(args, wl):
     timed = q[W:]
     ess = np.abs(diagnostics.ess(timed, lags=min(K // 2, 100)))
     mean, std = diagnostics.moments(timed)
-    if world > 1:
-        t = torch.tensor(np.concatenate([ess, [t_dev]]), dtype=torch.float64)
-        parts = [torch.zeros_like(t) for _ in range(world)]
-        torch.distributed.all_gather(parts, t)
-        ess = sum(p[:-1].numpy() for p in parts)
-        t_dev = max(float(p[-1]) for p in parts)
+    ess, t_dev = sharding.combine_ess(ess, t_dev)
+    mean, std = sharding.combine_moments(mean, std, K * wl.chains)
     if wl.post_mean is not None:
         me, se = diagnostics.moment_error(mean, std, wl.post_mean, wl.post_std)
     else:
@@ -560,7 +554,7 @@ def run_gpu_arm(args, wl):
     acc = float(np.mean(smp.accepted_proposals) / (W + K))
 
     # ---- end to end through the public API with host buffers -------------
-    smp2 = H.Samplers.HMC(seed=2000 + rank)
+    smp2 = H.Samplers.HMC(seed=sharding.rank_seed(2000, rank))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     smp2.sample(None, post, initial_model=wl.q0, proposals=K, keep_samples=True, proposals_per_graph=min(K, 10),
@@ -698,12 +692,10 @@ def run_fwi_arm(args, wl):
     import torch
 
     import hmclab_gb300 as H
-    from hmclab_gb300 import _lib, diagnostics
+    from hmclab_gb300 import _lib, diagnostics, sharding
     from hmclab_gb300 import surrogate as S
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank, world, local = sharding.rank_environment()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -722,8 +714,8 @@ def run_fwi_arm(args, wl):
     data = S.TrainingSet(d, W * L * C)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    burn = H.Samplers.HMC(seed=100 + rank).sample(None, post, initial_model=wl.q0, proposals=W, training_set=data,
-                                                  **kw)
+    burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=wl.q0, proposals=W,
+                                                                     training_set=data, **kw)
     t_burn = time.perf_counter() - t0
     q_start = burn.current_model
     acc_burn = float(np.mean(burn.accepted_proposals) / W)
@@ -755,7 +747,7 @@ def run_fwi_arm(args, wl):
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    smp_s, t_s, launches, _ = timed_run(200 + rank, K, net)
+    smp_s, t_s, launches, _ = timed_run(sharding.rank_seed(200, rank), K, net)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -766,23 +758,17 @@ def run_fwi_arm(args, wl):
     acc_s = float(np.mean(smp_s.accepted_proposals) / K)
 
     # ---- timed: plain HMC (exact gradients), same start -------------------
-    smp_p, t_p, _, per_p = timed_run(300 + rank, Kp, None)
+    smp_p, t_p, _, per_p = timed_run(sharding.rank_seed(300, rank), Kp, None)
     smp_p.finish()
     qp = smp_p.samples_device[0]
     ess_p = np.abs(diagnostics.ess(qp, lags=max(2, Kp // 2)))
     acc_p = float(np.mean(smp_p.accepted_proposals) / Kp)
-    if world > 1:
-        t = torch.tensor(np.concatenate([ess_s, ess_p, [t_s, t_p]]), dtype=torch.float64)
-        parts = [torch.zeros_like(t) for _ in range(world)]
-        torch.distributed.all_gather(parts, t)
-        ess_s = sum(p[:d].numpy() for p in parts)
-        ess_p = sum(p[d:2 * d].numpy() for p in parts)
-        t_s = max(float(p[-2]) for p in parts)
-        t_p = max(float(p[-1]) for p in parts)
+    ess_s, t_s = sharding.combine_ess(ess_s, t_s)
+    ess_p, t_p = sharding.combine_ess(ess_p, t_p)
     value = float(ess_s.min() / t_s)
     plain_value = float(ess_p.min() / t_p)
-    mean_s, std_s = diagnostics.moments(qs)
-    mean_p, std_p = diagnostics.moments(qp)
+    mean_s, std_s = sharding.combine_moments(*diagnostics.moments(qs), K * C)
+    mean_p, std_p = sharding.combine_moments(*diagnostics.moments(qp), Kp * C)
     me, se = diagnostics.moment_error(mean_s, std_s, mean_p, std_p)
     # the same posterior mean in both runs? z = difference / its Monte Carlo
     # standard error (std / sqrt(ESS) per run); for exact chains |z| ~ N(0, 1)
@@ -793,8 +779,8 @@ def run_fwi_arm(args, wl):
     # ---- end to end through the public API with host buffers -------------
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    smp_e = H.Samplers.HMC(seed=400 + rank).sample(None, post, initial_model=q_start, proposals=K,
-                                                   keep_samples=True, surrogate=net, **kw_s)
+    smp_e = H.Samplers.HMC(seed=sharding.rank_seed(400, rank)).sample(
+        None, post, initial_model=q_start, proposals=K, keep_samples=True, surrogate=net, **kw_s)
     host_q, host_x = smp_e.samples_host()
     t_e2e = time.perf_counter() - t0
     ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K // 2, 100)))
