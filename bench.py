@@ -729,8 +729,29 @@ def run_fwi_arm(args, wl):
     t_train = time.perf_counter() - t0
     net.freeze()
 
+    # ---- pilot (untimed): the surrogate run's trajectory ------------------
+    # A few proposals per (L, stepsize) from the burn-in end states; the
+    # setting with the largest acceptance x (trajectory length)^2 — the
+    # diffusive-regime gain per proposal, length capped at the plain run's —
+    # is used for the timed run.  --surrogate-L / --surrogate-stepsize fix it.
+    pilot = []
+    if args.surrogate_L is None or args.surrogate_stepsize is None:
+        tau_max = wl.stepsize * wl.L
+        for L_s in (2, 4, 8):
+            for eps_s in (0.03, 0.06, 0.12):
+                if L_s * eps_s > tau_max + 1e-9:
+                    continue
+                p_smp = H.Samplers.HMC(seed=sharding.rank_seed(150 + 10 * L_s, rank)).sample(
+                    None, post, initial_model=q_start, proposals=4, surrogate=net,
+                    **dict(kw, amount_of_steps=L_s, stepsize=eps_s))
+                a = float(np.mean(p_smp.accepted_proposals) / 4)
+                pilot.append((a * (L_s * eps_s) ** 2, L_s, eps_s, a))
+        _, L_best, eps_best, _ = max(pilot)
+    else:
+        L_best, eps_best = args.surrogate_L, args.surrogate_stepsize
+
     # ---- timed: surrogate-driven HMC --------------------------------------
-    kw_s = dict(kw, amount_of_steps=args.surrogate_L, stepsize=args.surrogate_stepsize)
+    kw_s = dict(kw, amount_of_steps=L_best, stepsize=eps_best)
 
     def timed_run(seed, n, surrogate):
         smp = H.Samplers.HMC(seed=seed)
@@ -794,8 +815,8 @@ def run_fwi_arm(args, wl):
         "dtype": "f32", "data": "synthetic (seeded; records from the device forward of the true model + noise)",
         "config": wl.config(),
         "speedup_vs_plain": float(value / plain_value),
-        "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": args.surrogate_L,
-                                                      "stepsize": args.surrogate_stepsize},
+        "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
+                                                      "pilot": [[L_, e_, round(a_, 4)] for _, L_, e_, a_ in pilot]},
         "plain": {"value": plain_value, "steps": Kp, "ms_per_step": 1e3 * t_p / Kp, "acceptance": acc_p,
                   "ess_per_chain_proposal": e_plain},
         "moment_error_vs_plain": {"mean": me, "std": se,
@@ -838,10 +859,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
-    ap.add_argument("--plain-steps", type=int, default=12, help="fwi: timed proposals of plain HMC")
+    ap.add_argument("--plain-steps", type=int, default=10, help="fwi: timed proposals of plain HMC")
     ap.add_argument("--train-steps", type=int, default=3000, help="fwi: Adam steps of the surrogate")
-    ap.add_argument("--surrogate-L", type=int, default=4, help="fwi: leapfrog steps of the surrogate-driven run")
-    ap.add_argument("--surrogate-stepsize", type=float, default=0.06, help="fwi: its step size (whitened units)")
+    ap.add_argument("--surrogate-L", type=int, default=None,
+                    help="fwi: leapfrog steps of the surrogate-driven run (default: chosen by a pilot)")
+    ap.add_argument("--surrogate-stepsize", type=float, default=None,
+                    help="fwi: its step size in whitened units (default: chosen by a pilot)")
     ap.add_argument("--cpu-chains", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
