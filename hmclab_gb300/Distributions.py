@@ -323,7 +323,7 @@ class Laplace(_AbstractDistribution):
         self.means = means.reshape(self.dimensions, 1)
         dispersions = _numpy.asarray(dispersions, dtype=_numpy.float64)
         if dispersions.size == 1:
-            dispersions = _numpy.full((self.dimensions, 1), float(dispersions))
+            dispersions = _numpy.full((self.dimensions, 1), float(dispersions.reshape(-1)[0]))
         self.dispersions = dispersions.reshape(self.dimensions, 1)
         self.inverse_dispersions = 1.0 / self.dispersions
         self.normalization_constant = 0.0
