@@ -26,6 +26,13 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
   training_set  a `surrogate.TrainingSet` that receives every exact
                 (position, gradient) pair the trajectories evaluate, until it
                 is full (burn-in data for the surrogate; runs uncaptured)
+  temperatures  one temperature per chain: chain c targets
+                exp(-misfit / T_c) (the tempered posteriors that the
+                reference runs as separate distributions in parallel tempering)
+  exchange_interval
+                every this many proposals, the chains are paired at random
+                and each pair swaps its models with the replica-exchange
+                acceptance of `Samplers.py:589-669` (on the device)
 
 Each proposal is issued as: begin (momentum, K0, first drift) -> for every
 kick: gradient of the target on the device, then kick+drift -> misfit at the
@@ -106,6 +113,9 @@ class HMC:
     minimal_stepsize = 1e-18
     surrogate = None
     training_set = None
+    _temperatures = None
+    exchange_interval = None
+    beta = None
 
     def __init__(self, seed: int = None):
         self.seed = seed
@@ -147,6 +157,8 @@ class HMC:
         keep_samples: bool = False,
         surrogate=None,
         training_set=None,
+        temperatures=None,
+        exchange_interval: int = None,
     ):
         """Run `proposals` HMC proposals for every chain; returns self.
 
@@ -160,7 +172,8 @@ class HMC:
             diagnostic_mode=diagnostic_mode, overwrite_existing_file=overwrite_existing_file, max_time=max_time,
             autotuning=autotuning, target_acceptance_rate=target_acceptance_rate, learning_rate=learning_rate,
             chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
-            keep_samples=keep_samples, surrogate=surrogate, training_set=training_set,
+            keep_samples=keep_samples, surrogate=surrogate, training_set=training_set, temperatures=temperatures,
+            exchange_interval=exchange_interval,
         )
         self._run()
         return self
@@ -322,6 +335,14 @@ class HMC:
         self.k_cur = Z((C,), "float64")
         self.k_prop = Z((C,), "float64")
         self.accepted = _torch.zeros((C,), dtype=_torch.int64, device=dev)
+        self.beta = None
+        if self._temperatures is not None:
+            self.beta = _torch.from_numpy(1.0 / self._temperatures).to(dev)
+        if self.exchange_interval is not None:
+            self._ex_pairs = _torch.zeros((C,), dtype=_torch.int32, device=dev)
+            self._ex_u = _torch.zeros((C // 2,), dtype=_torch.float64, device=dev)
+            self._ex_swapped = _torch.zeros((C // 2,), dtype=_torch.int32, device=dev)
+            self._ex_total = _torch.zeros((1,), dtype=_torch.int64, device=dev)
         self.flags = _torch.zeros((C,), dtype=_torch.int32, device=dev)
         self.control = _torch.zeros((2,), dtype=_torch.int64, device=dev)
         lo, hi = self.distribution.lower_bounds, self.distribution.upper_bounds
@@ -383,6 +404,7 @@ class HMC:
         st.ring_slots, st.thinning = slots, self.online_thinning
         st.rec_stepsize, st.rec_acceptance = _dev.ptr(self.rec_eps), _dev.ptr(self.rec_acc)
         st.rec_len = self.proposals if self.autotuning else 0
+        st.beta = _dev.ptr(self.beta)
         self._state = st
         self._state_ref = _ct.byref(st)
         # Initial misfit (reference asserts it is finite, Samplers.py:419-426).
@@ -486,7 +508,7 @@ class HMC:
             initial_model=None, proposals=100, online_thinning=1, diagnostic_mode=False, overwrite_existing_file=False,
             max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
             dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
-            surrogate=None, training_set=None,
+            surrogate=None, training_set=None, temperatures=None, exchange_interval=None,
         )
         unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
         if unknown:
@@ -501,6 +523,7 @@ class HMC:
             a["proposals_per_graph"], a["keep_samples"],
         )
         self._parse_surrogate(a["surrogate"], a["training_set"])
+        self._parse_tempering(a["temperatures"], a["exchange_interval"])
         self._setup_device()
         self._open_files()
         self._done = 0
@@ -521,6 +544,35 @@ class HMC:
             assert surrogate.frozen, "freeze() the surrogate before sampling with it (the chain must see a fixed field)"
         if training_set is not None or not self.distribution.graph_safe:
             self.use_graph = False
+
+    def _parse_tempering(self, temperatures, exchange_interval):
+        self._temperatures = None
+        if temperatures is not None:
+            t = _numpy.asarray(temperatures, dtype=_numpy.float64).reshape(-1)
+            assert t.size == self.chains, "one temperature per chain is required"
+            assert _numpy.all(t > 0) and _numpy.all(_numpy.isfinite(t)), "temperatures must be positive and finite"
+            self._temperatures = t
+        self.exchange_interval = None
+        if exchange_interval is not None:
+            assert type(exchange_interval) == int and exchange_interval > 0, "exchange_interval must be a positive int"
+            assert self.chains >= 2, "replica exchange needs at least two chains"
+            assert exchange_interval % self.online_thinning == 0, (
+                "exchange_interval must be a multiple of online_thinning")
+            self.exchange_interval = exchange_interval
+            # exchanges happen between graph blocks: one block per interval
+            self.proposals_per_graph = exchange_interval
+
+    def _exchange(self, h):
+        """Pair the chains at random and let each pair swap models."""
+        C = self.chains
+        npairs = C // 2
+        perm = self.rng.permutation(C)[: 2 * npairs].astype(_numpy.int32)
+        u = self.rng.uniform(0, 1, size=npairs)
+        with _torch.cuda.stream(self.stream):
+            self._ex_pairs[: 2 * npairs].copy_(_torch.from_numpy(perm))
+            self._ex_u[:npairs].copy_(_torch.from_numpy(u))
+        _lib.call("hmc_exchange", self._state_ref, npairs, self._ex_pairs.data_ptr(), self._ex_u.data_ptr(),
+                  self._ex_swapped.data_ptr(), self._ex_total.data_ptr(), h)
 
     def run(self, n_proposals):
         """Enqueue the next `n_proposals` proposals (whole graph blocks where
@@ -546,6 +598,8 @@ class HMC:
                 _lib.call("hmc_graph_launch", self._graph, h)
             else:
                 self._issue_block(n, h)
+            if self.exchange_interval is not None and (self._done + n) % self.exchange_interval == 0:
+                self._exchange(h)
             self._drain(self._done, n)
             self._done += n
             issued += n
@@ -583,6 +637,7 @@ class HMC:
 
     def _finalise(self, done):
         C = self.chains
+        self.exchanges_accepted = int(self._ex_total.cpu()[0]) if self.exchange_interval is not None else 0
         self.current_proposal = max(done - 1, 0)
         acc = self.accepted.cpu().numpy()
         self.accepted_proposals = int(acc[0]) if C == 1 else acc

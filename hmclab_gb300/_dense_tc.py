@@ -122,6 +122,8 @@ class FusedDenseStep:
         dist = sampler.distribution
         if sampler.dtype != "float32" or sampler.mass_matrix.kind == _lib.HMC_MASS_FULL:
             return None
+        if getattr(sampler, "beta", None) is not None:  # tempered chains: the fused epilogue kicks at beta = 1
+            return None
         parts = dist.separate_distributions if isinstance(dist, D.AdditiveDistribution) else [dist]
         liks = [p for p in parts if isinstance(p, D.LinearMatrix)]
         priors = [p for p in parts if not isinstance(p, D.LinearMatrix)]

@@ -84,6 +84,7 @@ class HmcChains(_ct.Structure):
         ("rec_stepsize", c_void_p),
         ("rec_acceptance", c_void_p),
         ("rec_len", c_int64),
+        ("beta", c_void_p),
     ]
 
 
@@ -161,6 +162,7 @@ SIGNATURES = {
     "hmc_srcloc3d_misfit": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
+    "hmc_exchange": [P, I64, P, P, P, P, S],
     "hmc_gemm_splitk": [I, I64, I64, I64, D, P, P, P, I, P, I64, S],
     "hmc_split_bf16": [I64, I64, P, I64, P, P, S],
     "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],

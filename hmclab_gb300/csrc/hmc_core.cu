@@ -58,6 +58,7 @@ struct ChainView {
   double* rec_eps;
   double* rec_acc;
   int64_t rec_len;
+  const double* beta;  // per-chain inverse temperature, nullptr = 1
 };
 
 template <typename T>
@@ -100,6 +101,7 @@ ChainView<T> view(const hmc_chains* s) {
   v.rec_eps = s->rec_stepsize;
   v.rec_acc = s->rec_acceptance;
   v.rec_len = s->rec_len;
+  v.beta = s->beta;
   return v;
 }
 
@@ -249,7 +251,7 @@ __global__ void kick_drift_kernel(ChainView<T> s, double kick, double drift) {
     const T e = s.eps_local[c];
     T p = s.p[idx];
     if (DO_KICK) {
-      const T ck = (T)(kick * (double)e);
+      const T ck = (T)(kick * (double)e * (s.beta ? s.beta[c] : 1.0));
       p -= ck * s.g[idx];
     }
     if (DO_DRIFT) {
@@ -305,8 +307,9 @@ __global__ void end_kernel(ChainView<T> s) {
         x1 = INFINITY;
         s.x_prop[c] = x1;
       }
-      const double h0 = s.x_cur[c] + s.k_cur[c];
-      const double h1 = x1 + k1;
+      const double b = s.beta ? s.beta[c] : 1.0;
+      const double h0 = (s.beta ? b * s.x_cur[c] : s.x_cur[c]) + s.k_cur[c];
+      const double h1 = (s.beta ? b * x1 : x1) + k1;
       const double alpha = exp(h0 - h1);
       if (s.autotune) {
         const T eps_now = s.eps[c];
@@ -351,7 +354,7 @@ __global__ void end_kernel(ChainView<T> s) {
       }
       if (record) s.ring_q[slot * s.d * s.C + idx] = qv;
     }
-    if (record && threadIdx.y == 0) s.ring_x[slot * s.C + c] = s.x_cur[c];
+    if (record && threadIdx.y == 0) s.ring_x[slot * s.C + c] = s.beta ? s.beta[c] * s.x_cur[c] : s.x_cur[c];
   }
   // The last block to finish advances the proposal counter.
   __shared__ bool last;
@@ -530,11 +533,73 @@ int kinetic_grad_impl(const hmc_chains* s, const void* p, void* out, cudaStream_
 }
 
 }  // namespace
+// ---- replica exchange ----------------------------------------------------
+// Decision per pair from the current misfits and inverse temperatures; pairs
+// with an index outside [0, C) or a == b never swap.
+__global__ void exchange_decide_kernel(int64_t npairs, int64_t C, const int32_t* __restrict__ pairs,
+                                       const double* __restrict__ u, const double* __restrict__ beta,
+                                       const double* __restrict__ x, int32_t* swapped, int64_t* total) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= npairs) return;
+  const int32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+  int ok = 0;
+  if (a >= 0 && a < C && b >= 0 && b < C && a != b) {
+    const double ba = beta ? beta[a] : 1.0, bb = beta ? beta[b] : 1.0;
+    ok = exp((ba - bb) * (x[a] - x[b])) > u[k] ? 1 : 0;  // NaN compares false
+  }
+  swapped[k] = ok;
+  if (ok && total) atomicAdd((unsigned long long*)total, 1ull);
+}
+
+// Swap the columns of accepted pairs: thread (pair k, dimension i).
+template <typename T>
+__global__ void exchange_swap_kernel(int64_t npairs, int64_t d, int64_t C, const int32_t* __restrict__ pairs,
+                                     const int32_t* __restrict__ swapped, T* q_cur, double* x_cur) {
+  const int64_t total = npairs * d;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = e / d, i = e - k * d;
+    if (!swapped[k]) continue;
+    const int64_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    const T t = q_cur[i * C + a];
+    q_cur[i * C + a] = q_cur[i * C + b];
+    q_cur[i * C + b] = t;
+    if (i == 0) {
+      const double tx = x_cur[a];
+      x_cur[a] = x_cur[b];
+      x_cur[b] = tx;
+    }
+  }
+}
+
+template <typename T>
+int exchange_impl(const hmc_chains* s, int64_t npairs, const int32_t* pairs, const double* u, int32_t* swapped,
+                  int64_t* total, cudaStream_t st) {
+  HMC_REQUIRE(s->dims > 0 && s->chains > 0 && s->q_cur && s->x_cur, "hmc_exchange: missing state");
+  HMC_REQUIRE(npairs >= 0 && 2 * npairs <= s->chains, "hmc_exchange: %lld pairs for %lld chains",
+              (long long)npairs, (long long)s->chains);
+  if (npairs == 0) return HMC_OK;
+  HMC_REQUIRE(pairs && u && swapped, "hmc_exchange: null pairs, uniforms or decisions");
+  exchange_decide_kernel<<<blocks_for(npairs, 256), 256, 0, st>>>(npairs, s->chains, pairs, u, s->beta, s->x_cur,
+                                                                   swapped, total);
+  HMC_TRY(check_launch("exchange_decide_kernel"));
+  exchange_swap_kernel<T><<<ew_grid(npairs * s->dims), 256, 0, st>>>(npairs, s->dims, s->chains, pairs, swapped,
+                                                                      (T*)s->q_cur, s->x_cur);
+  return check_launch("exchange_swap_kernel");
+}
+
 }  // namespace hmc
 
 using namespace hmc;
 
 extern "C" {
+
+int hmc_exchange(const hmc_chains* s, int64_t npairs, const int32_t* pairs, const double* u, int32_t* swapped,
+                 int64_t* accepted_total, void* stream) {
+  if (!s) return fail(HMC_ERR_INVALID_ARG, "hmc_exchange: null state");
+  return HMC_DISPATCH(s->dtype, T, [&] {
+    return exchange_impl<T>(s, npairs, pairs, u, swapped, accepted_total, as_stream(stream));
+  });
+}
 
 int hmc_begin_trajectory(const hmc_chains* s, double drift, void* stream) {
   if (!s) return fail(HMC_ERR_INVALID_ARG, "hmc_begin_trajectory: null state");

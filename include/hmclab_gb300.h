@@ -127,6 +127,12 @@ typedef struct hmc_chains {
   double* rec_stepsize;
   double* rec_acceptance;
   int64_t rec_len;
+  /* Optional per-chain inverse temperatures [C] (NULL: all 1): chain c
+   * targets exp(-beta[c] * misfit), so kicks scale the gradient by beta[c]
+   * and the accept test uses beta[c] * misfit; x_cur / x_prop stay the
+   * untempered misfit, ring_x records beta[c] * x_cur (the misfit of the
+   * chain's own tempered target, as a tempered distribution would report).  */
+  const double* beta;
 } hmc_chains;
 
 /* Samplers.py:1463-1469 + 1524-1545 (and MassMatrices.py:100-314):
@@ -149,6 +155,19 @@ HMC_API int hmc_kick_drift(const hmc_chains* s, double kick, double drift,
  * on accept, count, optionally adapt eps, record the thinned sample and
  * advance the proposal counter.  x_prop must hold misfit(q).               */
 HMC_API int hmc_end_trajectory(const hmc_chains* s, void* stream);
+
+/* Replica exchange between tempered chains (the exchange step of
+ * Samplers.py:589-669, done in place on the device instead of over pipes):
+ * for each of the npairs pairs (a, b) = pairs[2k], pairs[2k+1] (distinct
+ * chains, each in at most one pair), swap the current models of a and b
+ * iff exp((beta[a] - beta[b]) * (x_cur[a] - x_cur[b])) > u[k] (the sum of
+ * both chains' misfit improvements; FP64, NaN rejects).  Positions and
+ * misfits move; step sizes stay with their chain.  swapped[k] receives the
+ * decision; accepted_total (nullable) counts the swaps.                    */
+HMC_API int hmc_exchange(const hmc_chains* s, int64_t npairs,
+                         const int32_t* pairs, const double* u,
+                         int32_t* swapped, int64_t* accepted_total,
+                         void* stream);
 
 /* MassMatrices.py:100-113,185-198,270-285: out[c] = 0.5 p_c^T M^-1 p_c (FP64).
  * For FULL, s->v is used as scratch.                                       */

@@ -456,6 +456,26 @@ def run_chains(
 # Effective sample size (the reference has none; BDA3 section 11.5 split-chain
 # multi-chain estimator with Geyer's initial monotone sequence).
 # ---------------------------------------------------------------------------
+def exchange(q, x, beta, pairs, u):
+    """Replica exchange of the reference's parallel sampler
+    (Samplers.py:589-669): chains a, b with tempered misfits beta * x swap
+    their models iff exp(improvement_a + improvement_b) > u, where
+    improvement_a = beta_a (x_a - x_b) and improvement_b = beta_b (x_b - x_a).
+    q is [d][C] (columns are chains), x and beta are [C]; pairs is [P][2].
+    Returns the new (q, x) and the decisions."""
+    q = np.array(q, copy=True)
+    x = np.array(x, copy=True)
+    swapped = np.zeros(len(pairs), bool)
+    for k, (a, b) in enumerate(pairs):
+        improvement = beta[a] * (x[a] - x[b]) + beta[b] * (x[b] - x[a])
+        with np.errstate(over="ignore"):
+            if np.exp(improvement) > u[k]:
+                swapped[k] = True
+                q[:, [a, b]] = q[:, [b, a]]
+                x[[a, b]] = x[[b, a]]
+    return q, x, swapped
+
+
 def ess_split(x, lags):
     """x: [N][d][C] samples.  Returns (ess[d], rhat[d]); ess is negated where
     the lag window was too short to truncate (same convention as hmc_ess)."""
