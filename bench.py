@@ -117,6 +117,8 @@ class DenseWorkload:
         fused = smp._fused is not None
         return {"kernel": ("chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
                            if fused else "dense gradient GEMM"),
+                # DRAM read + write of one step launch, ncu capture (54.4 + 2.9 MB)
+                "traffic": 57.3e6 if fused else None,
                 "bound": "tensor", "unit": "TFLOP/s", "work": self.gemm_flops(),
                 "work_name": "algorithmic_flop_per_launch",
                 "extra": {"executed_flop_per_launch": 3 * self.gemm_flops() if fused else self.gemm_flops()}}
@@ -294,6 +296,10 @@ class SrclocWorkload:
 # reference arm, which can only afford to time the CPU cost of a proposal,
 # converts that cost into min-ESS/s with it.
 FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.241
+# DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
+# capture of velocity_kernel (59.1 + 0.4 MB) and stress_kernel (67.6 + 1.6 MB)
+# on a cold cache; in the time loop the fields stay in L2 and DRAM moves less
+FWI_STEP_DRAM_BYTES = 128.7e6
 
 
 class FwiWorkload:
@@ -585,7 +591,8 @@ def run_gpu_arm(args, wl):
                 "seconds": t_e2e},
         "gpu_launches": int(launches),
         "roofline": {"kernel": spec["kernel"], "bound": spec["bound"], "achieved": achieved, "peak": peak,
-                     "unit": spec["unit"], "frac": achieved / peak, "traffic": None, "peak_source": psrc,
+                     "unit": spec["unit"], "frac": achieved / peak, "traffic": spec.get("traffic"),
+                     "peak_source": psrc,
                      "launch_s": t_gemm, spec["work_name"]: spec["work"], **spec["extra"]},
         "clocks": clk,
     }
@@ -834,7 +841,8 @@ def run_fwi_arm(args, wl):
         "gpu_launches": int(launches),
         "roofline": {"kernel": "fwi forward time step: velocity_kernel + stress_kernel (the exact misfit)",
                      "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": src, "step_s": t_step,
+                     "traffic": FWI_STEP_DRAM_BYTES, "traffic_source": "ncu capture of one velocity + one stress "
+                     "launch at C = 64, default (cold) cache control", "peak_source": src, "step_s": t_step,
                      "algorithmic_bytes_per_step": wl.stencil_bytes_per_step()},
         "clocks": clk,
     }
