@@ -29,6 +29,9 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
   temperatures  one temperature per chain: chain c targets
                 exp(-misfit / T_c) (the tempered posteriors that the
                 reference runs as separate distributions in parallel tempering)
+  persistent    None (default): small dense linear-Gaussian targets (d <= 128)
+                run whole blocks of proposals in one persistent launch, one
+                warp per chain; False forces one launch per leapfrog step
   exchange_interval
                 every this many proposals, the chains are paired at random
                 and each pair swaps its models with the replica-exchange
@@ -116,6 +119,8 @@ class HMC:
     _temperatures = None
     exchange_interval = None
     beta = None
+    use_persistent = None
+    _persistent = None
 
     def __init__(self, seed: int = None):
         self.seed = seed
@@ -159,6 +164,7 @@ class HMC:
         training_set=None,
         temperatures=None,
         exchange_interval: int = None,
+        persistent: bool = None,
     ):
         """Run `proposals` HMC proposals for every chain; returns self.
 
@@ -173,7 +179,7 @@ class HMC:
             autotuning=autotuning, target_acceptance_rate=target_acceptance_rate, learning_rate=learning_rate,
             chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
             keep_samples=keep_samples, surrogate=surrogate, training_set=training_set, temperatures=temperatures,
-            exchange_interval=exchange_interval,
+            exchange_interval=exchange_interval, persistent=persistent,
         )
         self._run()
         return self
@@ -423,8 +429,12 @@ class HMC:
         self._graph = None
         from hmclab_gb300._dense_tc import FusedDenseStep
 
+        from hmclab_gb300._persistent import PersistentDense
+
+        self._persistent = PersistentDense.applies(self)
         self._fused = (
-            None if (self.surrogate is not None or self.training_set is not None) else FusedDenseStep.applies(self)
+            None if (self._persistent is not None or self.surrogate is not None or self.training_set is not None)
+            else FusedDenseStep.applies(self)
         )
         if self.surrogate is not None:
             self.surrogate._buffers(C, False)  # allocate before any capture
@@ -508,7 +518,7 @@ class HMC:
             initial_model=None, proposals=100, online_thinning=1, diagnostic_mode=False, overwrite_existing_file=False,
             max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
             dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
-            surrogate=None, training_set=None, temperatures=None, exchange_interval=None,
+            surrogate=None, training_set=None, temperatures=None, exchange_interval=None, persistent=None,
         )
         unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
         if unknown:
@@ -524,6 +534,7 @@ class HMC:
         )
         self._parse_surrogate(a["surrogate"], a["training_set"])
         self._parse_tempering(a["temperatures"], a["exchange_interval"])
+        self.use_persistent = a["persistent"]
         self._setup_device()
         self._open_files()
         self._done = 0
@@ -585,7 +596,9 @@ class HMC:
         while self._done < target:
             n = min(k, target - self._done)
             self._load_streams(self._done, n)
-            if self.use_graph and n == k:
+            if self._persistent is not None:
+                self._persistent.run(n, h)
+            elif self.use_graph and n == k:
                 if self._graph is None:
                     _lib.call("hmc_graph_begin", h)
                     try:

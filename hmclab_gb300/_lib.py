@@ -106,6 +106,21 @@ class HmcFwi(_ct.Structure):
         "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial")]
 
 
+HMC_SCHEDULE_MAX = 64
+
+
+class HmcSchedule(_ct.Structure):
+    """Mirror of `hmc_schedule` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("first_drift", _ct.c_double),
+        ("steps", c_int32),
+        ("gradient", c_int32 * HMC_SCHEDULE_MAX),
+        ("kick", _ct.c_double * HMC_SCHEDULE_MAX),
+        ("drift", _ct.c_double * HMC_SCHEDULE_MAX),
+    ]
+
+
 class HmcMlpOut(_ct.Structure):
     """Mirror of `hmc_mlp_out` in include/hmclab_gb300.h."""
 
@@ -163,6 +178,7 @@ SIGNATURES = {
     "hmc_srcloc3d_gradient": [I, I64, I64, I64, P, P, P, P, P, P, I, D, P, I, S],
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
     "hmc_exchange": [P, I64, P, P, P, P, S],
+    "hmc_persistent_dense": [P, P, P, D, I, P, P, P, I64, I, I, S],
     "hmc_gemm_splitk": [I, I64, I64, I64, D, P, P, P, I, P, I64, S],
     "hmc_split_bf16": [I64, I64, P, I64, P, P, S],
     "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],

@@ -1,0 +1,120 @@
+"""Persistent fused proposals (csrc/persistent.cu) for small dense
+linear-Gaussian posteriors: whole blocks of proposals in one launch, one warp
+per chain, with an autotuner that picks the chains per block.
+
+Applies when the target is a premultiplied dense `LinearMatrix` with
+d <= 128, alone or in a `BayesRule` with one diagonal `Normal` or `Laplace`
+prior, the mass matrix is unit or diagonal, and the run has no bounds, no
+autotuning, no temperatures, no surrogate and no training set.
+"""
+import ctypes as _ct
+
+from hmclab_gb300 import _lib
+
+MAX_D = 128
+_WARPS = (1, 2, 4, 8, 16)
+# chosen launch shapes, per (dimension, chains, dtype, mass, prior, schedule length)
+_tuned = {}
+
+
+def _schedule(first, steps):
+    s = _lib.HmcSchedule()
+    s.first_drift = float(first)
+    s.steps = len(steps)
+    for k, (needs_grad, kick, drift) in enumerate(steps):
+        s.gradient[k] = int(bool(needs_grad))
+        s.kick[k] = float(kick)
+        s.drift[k] = float(drift)
+    return s
+
+
+class PersistentDense:
+    @staticmethod
+    def applies(sampler):
+        from hmclab_gb300 import Distributions as D
+
+        if getattr(sampler, "use_persistent", None) is False:
+            return None
+        if sampler.dimensions > MAX_D or sampler.mass_matrix.kind == _lib.HMC_MASS_FULL:
+            return None
+        if sampler.autotuning or getattr(sampler, "beta", None) is not None:
+            return None
+        if sampler.surrogate is not None or sampler.training_set is not None:
+            return None
+        if sampler.lower is not None or sampler.upper is not None:
+            return None
+        first, steps = sampler._schedule
+        if len(steps) > _lib.HMC_SCHEDULE_MAX:
+            return None
+        dist = sampler.distribution
+        parts = dist.separate_distributions if isinstance(dist, D.AdditiveDistribution) else [dist]
+        liks = [p for p in parts if type(p) is D.LinearMatrix]
+        others = [p for p in parts if type(p) is not D.LinearMatrix]
+        if len(liks) != 1 or len(others) > 1 or len(parts) != len(liks) + len(others):
+            return None
+        lik = liks[0]
+        if not (lik.dense and lik.premultiplication):
+            return None
+        prior = others[0] if others else None
+        if prior is not None:
+            if not ((type(prior) is D.Normal and prior.diagonal) or type(prior) is D.Laplace):
+                return None
+            if prior.lower_bounds is not None or prior.upper_bounds is not None:
+                return None
+        return PersistentDense(sampler, lik, prior)
+
+    def __init__(self, sampler, lik, prior):
+        from hmclab_gb300 import Distributions as D
+
+        self.smp = sampler
+        dt = sampler.dtype
+        p = lik._params(dt)
+        self.GtG, self.Gtd0, self.dtd = p["GtG"], p["Gtd0"], float(lik.dtd)
+        self.prior_kind, self.pmean, self.pw = 0, None, None
+        if prior is not None:
+            pp = prior._params(dt)
+            if type(prior) is D.Normal:
+                self.prior_kind, self.pmean, self.pw = 1, pp["mean"], pp["iv"]
+            else:
+                self.prior_kind, self.pmean, self.pw = 2, pp["mean"], pp["iw"]
+        first, steps = sampler._schedule
+        self.schedule = _schedule(first, steps)
+        self._sched_ref = _ct.byref(self.schedule)
+        self.key = (sampler.dimensions, sampler.chains, dt, sampler.mass_matrix.kind, self.prior_kind, len(steps))
+        self.warps = _tuned.get(self.key)
+
+    def _call(self, n, warps, dry, h):
+        _lib.call("hmc_persistent_dense", self.smp._state_ref, self.GtG.data_ptr(), self.Gtd0.data_ptr(), self.dtd,
+                  self.prior_kind, self.pmean.data_ptr() if self.pmean is not None else None,
+                  self.pw.data_ptr() if self.pw is not None else None, self._sched_ref, n, warps, int(dry), h)
+
+    def autotune(self, h, proposals=4):
+        """Time every chains-per-block choice on dry runs (which write no
+        state) of the live chains and keep the fastest."""
+        import torch
+
+        if self.warps is not None:
+            return self.warps
+        st = self.smp.stream
+        slen = self.smp._state.stream_len
+        if slen > 0:
+            proposals = min(proposals, slen)
+        best = None
+        for w in _WARPS:
+            self._call(1, w, True, h)  # warm
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            self._call(proposals, w, True, h)
+            e1.record(st)
+            st.synchronize()
+            t = e0.elapsed_time(e1)
+            if best is None or t < best[0]:
+                best = (t, w)
+        self.warps = best[1]
+        _tuned[self.key] = self.warps
+        return self.warps
+
+    def run(self, n, h):
+        if self.warps is None:
+            self.autotune(h)
+        self._call(n, self.warps, False, h)

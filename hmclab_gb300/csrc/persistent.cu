@@ -1,0 +1,349 @@
+// Persistent fused proposals for small dense linear-Gaussian targets: one
+// launch runs many whole HMC proposals for every chain, one warp per chain,
+// with the d x d GtG of the premultiplied LinearMatrix in shared memory.
+// Everything a proposal needs — Philox momenta (or injected streams), every
+// kick and drift of the integrator, the misfit at the end point, the FP64
+// accept test, the thinned sample record — happens in registers and shared
+// memory, so a chain of d <= 128 costs a handful of microseconds per
+// proposal instead of four launches per leapfrog step.
+//
+// Each lane owns the rows lane, lane + 32, ... of the chain's state.  The
+// arithmetic follows the launch-per-step path operation by operation (same
+// random draws, same order of the sums in the gradient, the same
+// (acc - Gtd0) + prior-gradient composition), so the two paths agree to the
+// last bits of the FP64 sums: only the order of the warp reductions differs.
+#include "common.cuh"
+
+namespace hmc {
+namespace pers {
+
+constexpr int MAX_D = 128;
+enum PriorKind { PRIOR_NONE = 0, PRIOR_NORMAL = 1, PRIOR_LAPLACE = 2 };
+
+template <typename T>
+struct Target {
+  int d, ld;  // dimension, odd row stride of GtG in shared memory
+  const T* GtG;
+  const T* Gtd0;
+  double dtd;
+  const T* pmean;
+  const T* pw;
+};
+
+template <typename T>
+struct State {
+  int64_t C;
+  T* q_cur;
+  double* x_cur;
+  const T* eps;
+  int64_t* accepted;
+  const int64_t* control;
+  uint64_t seed;
+  int randomize;
+  const T* mdiag;
+  const T* minv;
+  const T* sz;
+  const T* seps;
+  const double* su;
+  int64_t slen;
+  T* ring_q;
+  double* ring_x;
+  int64_t ring_slots, thin;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T sign_of(T x) {
+  return x > (T)0 ? (T)1 : (x < (T)0 ? (T)-1 : (T)0);
+}
+
+// Standard normal for row i of chain c at proposal n: the injected stream or
+// the Philox quad (i / 4) that the launch-per-step path draws.
+template <typename T>
+__device__ __forceinline__ T momentum_draw(const State<T>& s, int d, int i, int64_t c, int64_t n) {
+  if (s.sz) return s.sz[((n % s.slen) * d + i) * s.C + c];
+  T z[4];
+  philox_normal4<T>(s.seed, (uint32_t)(i >> 2), (uint32_t)c, (uint64_t)n, PURPOSE_MOMENTUM, z);
+  const int j = i & 3;  // select without a local-memory array index
+  return j == 0 ? z[0] : (j == 1 ? z[1] : (j == 2 ? z[2] : z[3]));
+}
+
+// out[k] = sum_j GtG[row][j] q[j] for the lane's rows (q published in qw)
+template <typename T, int E>
+__device__ __forceinline__ void matvec(const T* A, int ld, int d, const T* qw, int lane, T out[E]) {
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = lane + 32 * k;
+    T acc = (T)0;
+    if (i < d) {
+      const T* row = A + i * ld;
+      for (int j = 0; j < d; ++j) acc += row[j] * qw[j];
+    }
+    out[k] = acc;
+  }
+}
+
+template <typename T, int E, int MASS, int PRIOR>
+__global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Target<T> tg, hmc_schedule sch,
+                                                               int64_t nprop, int dry) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int d = tg.d, ld = tg.ld;
+  T* A = (T*)smem_raw;  // [d][ld]
+  T* qbuf = A + d * ld;  // [warps][d]
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    const int r = e / d;
+    A[r * ld + (e - r * d)] = tg.GtG[e];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (c >= s.C) return;  // whole warps only; no block barrier follows
+  T* qw = qbuf + warp * d;
+  const int64_t n0 = s.control[0];
+
+  // per-row constants of the lane's rows
+  T minv[E], msq[E], gtd[E], pm[E], pw[E], qc[E];
+  bool live[E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = lane + 32 * k;
+    live[k] = i < d;
+    minv[k] = (MASS == HMC_MASS_DIAG && live[k]) ? s.minv[i] : (T)1;
+    msq[k] = (MASS == HMC_MASS_DIAG && live[k]) ? (T)sqrt((double)s.mdiag[i]) : (T)1;
+    gtd[k] = live[k] ? tg.Gtd0[i] : (T)0;
+    pm[k] = (PRIOR != PRIOR_NONE && live[k]) ? tg.pmean[i] : (T)0;
+    pw[k] = (PRIOR != PRIOR_NONE && live[k]) ? tg.pw[i] : (T)0;
+    qc[k] = live[k] ? s.q_cur[(int64_t)i * s.C + c] : (T)0;
+  }
+  double xc = s.x_cur[c];
+  const T eps0 = s.eps[c];
+  int64_t n_acc = 0;
+
+  for (int64_t t = 0; t < nprop; ++t) {
+    const int64_t n = n0 + t;
+    // step size of this trajectory and the accept uniform
+    double ue = 0.0, ua = 0.0;
+    if (!s.seps || !s.su) philox_scalars(s.seed, (uint32_t)c, (uint64_t)n, &ue, &ua);
+    T e = eps0;
+    if (s.randomize) {
+      const T f = s.seps ? s.seps[(n % s.slen) * s.C + c] : (T)(0.5 + ue);
+      e = (T)((double)f * (double)e);
+    }
+    const double u = s.su ? s.su[(n % s.slen) * s.C + c] : ua;
+
+    // momenta, K0, first drift
+    T p[E], q[E];
+    double k0 = 0.0;
+    const T ce = (T)(sch.first_drift * (double)e);
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      p[k] = (T)0;
+      q[k] = qc[k];
+      if (live[k]) {
+        const T z = momentum_draw(s, d, lane + 32 * k, c, n);
+        p[k] = MASS == HMC_MASS_DIAG ? msq[k] * z : z;
+        const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
+        k0 += (double)p[k] * (double)mp;
+        q[k] = qc[k] + ce * mp;
+      }
+    }
+    k0 = 0.5 * warp_sum(k0);
+
+    // kicks and drifts
+    for (int st = 0; st < sch.steps; ++st) {
+      if (sch.gradient[st]) {
+#pragma unroll
+        for (int k = 0; k < E; ++k)
+          if (live[k]) qw[lane + 32 * k] = q[k];
+        __syncwarp();
+        T g[E];
+        matvec<T, E>(A, ld, d, qw, lane, g);
+        __syncwarp();
+        const T ck = (T)(sch.kick[st] * (double)e);
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+          T gk = g[k] - gtd[k];
+          if (PRIOR == PRIOR_NORMAL) gk = gk + -(pw[k] * (pm[k] - q[k]));
+          if (PRIOR == PRIOR_LAPLACE) gk = gk + sign_of(q[k] - pm[k]) * pw[k];
+          p[k] -= ck * gk;
+        }
+      }
+      if (sch.drift[st] != 0.0) {
+        const T cd = (T)(sch.drift[st] * (double)e);
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+          const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
+          q[k] = q[k] + cd * mp;
+        }
+      }
+    }
+
+    // misfit at the end point, K1 and the accept test (FP64)
+#pragma unroll
+    for (int k = 0; k < E; ++k)
+      if (live[k]) qw[lane + 32 * k] = q[k];
+    __syncwarp();
+    T aq[E];
+    matvec<T, E>(A, ld, d, qw, lane, aq);
+    __syncwarp();
+    double lik = 0.0, pri = 0.0, k1 = 0.0;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      if (!live[k]) continue;
+      const T w = aq[k] + (T)-2 * gtd[k];
+      lik += (double)q[k] * (double)w;
+      if (PRIOR == PRIOR_NORMAL) {
+        const T r = pm[k] - q[k];
+        pri += (double)r * (double)(pw[k] * r);
+      }
+      if (PRIOR == PRIOR_LAPLACE) pri += (double)(fabs(q[k] - pm[k]) * pw[k]);
+      const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
+      k1 += (double)p[k] * (double)mp;
+    }
+    lik = 0.5 * (warp_sum(lik) + tg.dtd);
+    k1 = 0.5 * warp_sum(k1);
+    double x1 = lik;
+    if (PRIOR == PRIOR_NORMAL) x1 = 0.5 * warp_sum(pri) + lik;
+    if (PRIOR == PRIOR_LAPLACE) x1 = warp_sum(pri) + lik;
+    const double alpha = exp((xc + k0) - (x1 + k1));
+    if (alpha > u) {  // strict; NaN compares false
+#pragma unroll
+      for (int k = 0; k < E; ++k) qc[k] = q[k];
+      xc = x1;
+      ++n_acc;
+    }
+    if (!dry && s.ring_q && (n % s.thin) == 0) {
+      const int64_t slot = (n / s.thin) % s.ring_slots;
+#pragma unroll
+      for (int k = 0; k < E; ++k)
+        if (live[k]) s.ring_q[(slot * d + lane + 32 * k) * s.C + c] = qc[k];
+      if (lane == 0) s.ring_x[slot * s.C + c] = xc;
+    }
+  }
+  if (dry) return;
+#pragma unroll
+  for (int k = 0; k < E; ++k)
+    if (live[k]) s.q_cur[(int64_t)(lane + 32 * k) * s.C + c] = qc[k];
+  if (lane == 0) {
+    s.x_cur[c] = xc;
+    s.accepted[c] += n_acc;
+  }
+}
+
+__global__ void advance_counter_kernel(int64_t* control, int64_t n) { control[0] += n; }
+
+}  // namespace pers
+}  // namespace hmc
+
+using namespace hmc;
+using namespace hmc::pers;
+
+namespace {
+
+template <typename T, int E, int MASS>
+int launch_prior(int prior, const State<T>& st, const Target<T>& tg, const hmc_schedule& sch, int64_t nprop,
+                 int dry, int warps, cudaStream_t stream) {
+  const size_t smem = ((size_t)tg.d * tg.ld + (size_t)warps * tg.d) * sizeof(T);
+  auto kern = prior == PRIOR_NORMAL    ? persistent_dense_kernel<T, E, MASS, PRIOR_NORMAL>
+              : prior == PRIOR_LAPLACE ? persistent_dense_kernel<T, E, MASS, PRIOR_LAPLACE>
+                                       : persistent_dense_kernel<T, E, MASS, PRIOR_NONE>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(persistent_dense_kernel)");
+  }
+  const unsigned blocks = (unsigned)((st.C + warps - 1) / warps);
+  kern<<<blocks, 32 * warps, smem, stream>>>(st, tg, sch, nprop, dry);
+  return check_launch("persistent_dense_kernel");
+}
+
+template <typename T>
+int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, double dtd, int prior,
+                    const void* pmean, const void* pw, const hmc_schedule* sch, int64_t nprop, int warps, int dry,
+                    cudaStream_t stream) {
+  const char* who = "hmc_persistent_dense";
+  HMC_REQUIRE(s->dims > 0 && s->dims <= MAX_D, "%s: dimension %lld outside 1..%d", who, (long long)s->dims, MAX_D);
+  HMC_REQUIRE(s->chains > 0 && s->chains <= 0x7FFFFFFFll * 16, "%s: bad number of chains", who);
+  HMC_REQUIRE(s->q_cur && s->x_cur && s->eps && s->accepted && s->proposal, "%s: missing state buffer", who);
+  HMC_REQUIRE(s->mass_kind == HMC_MASS_UNIT || s->mass_kind == HMC_MASS_DIAG, "%s: unit or diagonal mass only", who);
+  if (s->mass_kind == HMC_MASS_DIAG) HMC_REQUIRE(s->mass_diag && s->mass_inv_diag, "%s: diagonal mass buffers", who);
+  HMC_REQUIRE(!s->lower && !s->upper, "%s: bounded targets use the launch-per-step path", who);
+  HMC_REQUIRE(!s->autotune, "%s: autotuning uses the launch-per-step path", who);
+  HMC_REQUIRE(!s->beta, "%s: tempered chains use the launch-per-step path", who);
+  HMC_REQUIRE(GtG && Gtd0, "%s: null GtG or Gtd0", who);
+  HMC_REQUIRE(prior >= PRIOR_NONE && prior <= PRIOR_LAPLACE, "%s: unknown prior kind %d", who, prior);
+  HMC_REQUIRE(prior == PRIOR_NONE || (pmean && pw), "%s: prior parameters missing", who);
+  HMC_REQUIRE(sch && sch->steps >= 1 && sch->steps <= HMC_SCHEDULE_MAX, "%s: bad schedule", who);
+  HMC_REQUIRE(warps == 1 || warps == 2 || warps == 4 || warps == 8 || warps == 16, "%s: warps_per_block %d", who,
+              warps);
+  HMC_REQUIRE(nprop >= 0, "%s: negative proposal count", who);
+  if (s->stream_z || s->stream_eps || s->stream_u)
+    HMC_REQUIRE(s->stream_z && s->stream_u && s->stream_len >= nprop && (s->stream_eps || !s->randomize_stepsize),
+                "%s: injected streams shorter than the launch", who);
+  if (s->ring_q) HMC_REQUIRE(s->ring_x && s->ring_slots > 0 && s->thinning > 0, "%s: bad sample ring", who);
+  if (nprop == 0) return HMC_OK;
+  State<T> st;
+  st.C = s->chains;
+  st.q_cur = (T*)s->q_cur;
+  st.x_cur = s->x_cur;
+  st.eps = (const T*)s->eps;
+  st.accepted = s->accepted;
+  st.control = s->proposal;
+  st.seed = s->seed;
+  st.randomize = s->randomize_stepsize;
+  st.mdiag = (const T*)s->mass_diag;
+  st.minv = (const T*)s->mass_inv_diag;
+  st.sz = (const T*)s->stream_z;
+  st.seps = (const T*)s->stream_eps;
+  st.su = s->stream_u;
+  st.slen = s->stream_len;
+  st.ring_q = (T*)s->ring_q;
+  st.ring_x = s->ring_x;
+  st.ring_slots = s->ring_slots;
+  st.thin = s->thinning;
+  Target<T> tg;
+  tg.d = (int)s->dims;
+  tg.ld = tg.d | 1;
+  tg.GtG = (const T*)GtG;
+  tg.Gtd0 = (const T*)Gtd0;
+  tg.dtd = dtd;
+  tg.pmean = (const T*)pmean;
+  tg.pw = (const T*)pw;
+  const int E = (tg.d + 31) / 32;
+  const bool diag = s->mass_kind == HMC_MASS_DIAG;
+  int rc;
+#define HMC_PERSIST_CASE(EV)                                                                          \
+  case EV:                                                                                            \
+    rc = diag ? launch_prior<T, EV, HMC_MASS_DIAG>(prior, st, tg, *sch, nprop, dry, warps, stream)    \
+              : launch_prior<T, EV, HMC_MASS_UNIT>(prior, st, tg, *sch, nprop, dry, warps, stream);   \
+    break;
+  switch (E) {
+    HMC_PERSIST_CASE(1)
+    HMC_PERSIST_CASE(2)
+    HMC_PERSIST_CASE(3)
+    default:
+      HMC_PERSIST_CASE(4)
+  }
+#undef HMC_PERSIST_CASE
+  HMC_TRY(rc);
+  if (dry) return HMC_OK;
+  advance_counter_kernel<<<1, 1, 0, stream>>>(s->proposal, nprop);
+  return check_launch("advance_counter_kernel");
+}
+
+}  // namespace
+
+extern "C" HMC_API int hmc_persistent_dense(const hmc_chains* s, const void* GtG, const void* Gtd0, double dtd,
+                                            int prior, const void* prior_mean, const void* prior_w,
+                                            const hmc_schedule* schedule, int64_t proposals, int warps_per_block,
+                                            int dry, void* stream) {
+  if (!s) return fail(HMC_ERR_INVALID_ARG, "hmc_persistent_dense: null state");
+  return HMC_DISPATCH(s->dtype, T, [&] {
+    return persistent_impl<T>(s, GtG, Gtd0, dtd, prior, prior_mean, prior_w, schedule, proposals, warps_per_block,
+                              dry, as_stream(stream));
+  });
+}

@@ -506,6 +506,38 @@ HMC_API int hmc_moments(int dtype, int64_t N, int64_t d, int64_t C,
                         const void* samples, double* mean, double* var,
                         void* stream);
 
+/* ---- persistent fused proposals for small dense targets -----------------
+ * One launch runs `proposals` whole HMC proposals (Samplers.py:1463-1584:
+ * momentum draw, first drift, every kick and drift of the integrator, the
+ * misfit at the end point, the FP64 accept test of :1471-1492 and the
+ * thinned sample record) for every chain, one warp per chain, for the
+ * posterior  [prior +] premultiplied dense LinearMatrix
+ * (LinearMatrix.py:164-208: gradient GtG m - Gtd0, misfit
+ * 0.5 (m^T (GtG m - 2 Gtd0) + dtd)) with d <= 128, GtG held in shared
+ * memory.  prior: 0 none, 1 Normal with diagonal inverse variances prior_w
+ * (base.py:539-570), 2 Laplace with inverse dispersions prior_w
+ * (base.py:689-710).  Unit or diagonal mass, no bounds, no autotuning, no
+ * temperatures.  The proposals are numbered from s->proposal[0] on, as
+ * hmc_begin_trajectory / hmc_end_trajectory number them (same random draws,
+ * injected streams included), and the counter is advanced by `proposals`.
+ * warps_per_block (1, 2, 4, 8 or 16) sets the chains per block; dry != 0
+ * runs the arithmetic but writes no state (for timing launch shapes).      */
+#define HMC_SCHEDULE_MAX 64
+typedef struct hmc_schedule {
+  double first_drift;                  /* drift coefficient before the loop */
+  int32_t steps;                       /* entries used below                */
+  int32_t gradient[HMC_SCHEDULE_MAX];  /* 1: evaluate the gradient, kick    */
+  double kick[HMC_SCHEDULE_MAX];       /* kick coefficient (x step size)    */
+  double drift[HMC_SCHEDULE_MAX];      /* drift coefficient (x step size)   */
+} hmc_schedule;
+
+HMC_API int hmc_persistent_dense(const hmc_chains* s, const void* GtG,
+                                 const void* Gtd0, double dtd, int prior,
+                                 const void* prior_mean, const void* prior_w,
+                                 const hmc_schedule* schedule,
+                                 int64_t proposals, int warps_per_block,
+                                 int dry, void* stream);
+
 /* ---- CUDA graphs of whole proposals --------------------------------------
  * Capture the work issued on `stream` between begin and end into an
  * executable graph; launch it any number of times.                          */
