@@ -131,6 +131,59 @@ class DenseWorkload:
 
 
 # ---------------------------------------------------------------------------
+# Workload: the single-chain FP64 configuration the reference runs on a CPU
+# ---------------------------------------------------------------------------
+class Cfg1Workload:
+    name = ("dense-linear G100x50 (N(0,1) entries), noise 0.1, Normal prior N(0, I), unit mass, 10 leapfrog steps "
+            "of 0.01, 1 chain, FP64, 10,000 samples")
+    kind = "cfg1"
+    n_data, n_model, chains, L = 100, 50, 1, 10
+    noise, stepsize = 0.1, 0.01
+    proposals_per_step = 1000  # a step: 1000 proposals of the single chain
+    default_steps, default_warmup = 10, 3
+    cpu_sample = (1, 10000)
+
+    def __init__(self, seed=0, chains=None):
+        from hmclab_gb300 import problems
+
+        self.G, self.d, self.m_true = problems.dense_linear(self.n_data, self.n_model, 1.0, self.noise, seed)
+        self.post_mean, self.post_cov = problems.gaussian_posterior(self.G, self.d, self.noise**2, 0.0, 1.0)
+        self.post_std = np.sqrt(np.diag(self.post_cov))
+        self.q0 = self.post_mean.copy()
+
+    def posterior(self):
+        import hmclab_gb300 as H
+
+        prior = H.Distributions.Normal(np.zeros((self.n_model, 1)), np.ones((self.n_model, 1)))
+        lik = H.Distributions.LinearMatrix(self.G, self.d, self.noise**2, dtype=np.float64)
+        return H.Distributions.BayesRule([prior, lik])
+
+    def sampler_kwargs(self):
+        return dict(stepsize=self.stepsize, amount_of_steps=self.L, chains=1, dtype="float64")
+
+    def oracle(self):
+        from oracle import hmc_oracle as O
+
+        post = O.Sum([O.NormalDiag(np.zeros(self.n_model), np.ones(self.n_model)),
+                      O.DensePremul(self.G, self.d, self.noise**2)])
+        return post, O.Mass("unit")
+
+    # FP64 FLOP of one block of proposals in the persistent kernel: L
+    # gradients and one misfit, each a 50 x 50 product
+    def roofline_spec(self, smp):
+        work = float(self.proposals_per_step) * (self.L + 1) * 2 * self.n_model**2
+        return {"kernel": "persistent_dense_kernel (whole proposals, one warp per chain, GtG in shared memory)",
+                "bound": "fp64", "unit": "TFLOP/s", "work": work, "work_name": "algorithmic_flop_per_launch",
+                "extra": {"proposals_per_launch": self.proposals_per_step, "persistent": smp._persistent is not None}}
+
+    def config(self):
+        return {"workload": self.name, "n_data": self.n_data, "n_model": self.n_model, "chains": 1,
+                "leapfrog_steps": self.L, "stepsize": self.stepsize, "samples": 10000,
+                "step": f"{self.proposals_per_step} proposals of the chain", "precision": "FP64",
+                "l2": "flushed between timed steps", "start": "posterior mean"}
+
+
+# ---------------------------------------------------------------------------
 # Workload: straight-ray tomography, CSR ray lengths, 1024 chains
 # ---------------------------------------------------------------------------
 class TomoWorkload:
@@ -368,7 +421,8 @@ class FwiWorkload:
                 "start": "end states of the exact burn-in"}
 
 
-WORKLOADS = {"dense": DenseWorkload, "tomo": TomoWorkload, "srcloc": SrclocWorkload, "fwi": FwiWorkload}
+WORKLOADS = {"cfg1": Cfg1Workload, "dense": DenseWorkload, "tomo": TomoWorkload, "srcloc": SrclocWorkload,
+             "fwi": FwiWorkload}
 
 
 # ---------------------------------------------------------------------------
@@ -456,15 +510,16 @@ def cpu_reference_run(wl, chains, warmup, steps, seed=0):
 
 
 def run_reference_arm(args, wl):
-    chains = args.cpu_chains
-    v, (me, se), dt, lps = cpu_reference_run(wl, chains, args.warmup, args.steps)
-    cores = os.cpu_count()
+    B = getattr(wl, "proposals_per_step", 1)
+    chains = args.cpu_chains if not hasattr(wl, "cpu_sample") else wl.cpu_sample[0]
+    v, (me, se), dt, lps = cpu_reference_run(wl, chains, args.warmup * B, args.steps * B)
+    cores = os.cpu_count() if chains > 1 else 1
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference", "config": {**wl.config(), "chains": chains},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{chains} chains x {args.steps} proposals of the same workload, numpy port of "
+                         "sample": f"{chains} chains x {args.steps * B} proposals of the same workload, numpy port of "
                                    "the reference HMC path batched over chains (BLAS on all host threads)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "leapfrog_steps_per_s": lps, "moment_error": {"mean": me, "std": se},
@@ -475,15 +530,23 @@ def run_reference_arm(args, wl):
 # ---------------------------------------------------------------------------
 def dominant_kernel_timing(post, smp, n_iter=20):
     """Average duration of the dominant kernel with CUDA events on the sampler
-    stream, on the live chain state: the fused tensor-core leapfrog step
-    (GtG @ Q - Gtd0 + prior, kick, drift, operand re-split) when the sampler
-    uses it, else the gradient launch of the likelihood."""
+    stream, on the live chain state: the persistent kernel running one block
+    of proposals (dry: it writes no state) when the sampler uses it, the fused
+    tensor-core leapfrog step (GtG @ Q - Gtd0 + prior, kick, drift, operand
+    re-split) when it uses that, else the gradient launch of the likelihood."""
     import torch
 
     st = smp.stream
     h = st.cuda_stream
     lik = post.separate_distributions[1] if hasattr(post, "separate_distributions") else post
-    if smp._fused is not None:
+    if getattr(smp, "_persistent", None) is not None:
+        B = smp.proposals_per_graph
+        if smp._persistent.warps is None:
+            smp._persistent.autotune(h)
+
+        def launch():  # one block of proposals, writing no state
+            smp._persistent._call(B, smp._persistent.warps, True, h)
+    elif smp._fused is not None:
         smp._fused.after_begin(h)
 
         def launch():
@@ -517,13 +580,14 @@ def run_gpu_arm(args, wl):
         dist.init_process_group("gloo")
     post = wl.posterior()
     K, W = args.steps, args.warmup
+    B = getattr(wl, "proposals_per_step", 1)  # proposals of every chain in one step
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     # ---- device-resident timed run ---------------------------------------
     smp = H.Samplers.HMC(seed=sharding.rank_seed(1000, rank))
-    smp.prepare(None, post, initial_model=wl.q0, proposals=W + K, keep_samples=True, proposals_per_graph=1,
+    smp.prepare(None, post, initial_model=wl.q0, proposals=(W + K) * B, keep_samples=True, proposals_per_graph=B,
                 **wl.sampler_kwargs())
-    smp.run(W)
+    smp.run(W * B)
     smp.stream.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     clocks = ClockSampler(local)
@@ -536,10 +600,10 @@ def run_gpu_arm(args, wl):
         with torch.cuda.stream(smp.stream):
             flush.fill_(float(k))
             evs[k][0].record(smp.stream)
-        smp.run(1)
+        smp.run(B)
         evs[k][1].record(smp.stream)
     torch.cuda.synchronize()
-    launches = _lib.launch_count() - launches0 - 0
+    launches = _lib.launch_count() - launches0
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -547,30 +611,31 @@ def run_gpu_arm(args, wl):
     t_gemm = dominant_kernel_timing(post, smp)
     smp.finish()
     q, x = smp.samples_device  # [N][d][C]
-    timed = q[W:]
-    ess = np.abs(diagnostics.ess(timed, lags=min(K // 2, 100)))
+    timed = q[W * B:]
+    ess = np.abs(diagnostics.ess(timed, lags=min(K * B // 2, 100 if B == 1 else 200)))
     mean, std = diagnostics.moments(timed)
     ess, t_dev = sharding.combine_ess(ess, t_dev)
-    mean, std = sharding.combine_moments(mean, std, K * wl.chains)
+    mean, std = sharding.combine_moments(mean, std, K * B * wl.chains)
     if wl.post_mean is not None:
         me, se = diagnostics.moment_error(mean, std, wl.post_mean, wl.post_std)
     else:
         me = se = None
     value = float(ess.min() / t_dev)
-    acc = float(np.mean(smp.accepted_proposals) / (W + K))
+    acc = float(np.mean(smp.accepted_proposals) / ((W + K) * B))
 
     # ---- end to end through the public API with host buffers -------------
     smp2 = H.Samplers.HMC(seed=sharding.rank_seed(2000, rank))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    smp2.sample(None, post, initial_model=wl.q0, proposals=K, keep_samples=True, proposals_per_graph=min(K, 10),
-                **wl.sampler_kwargs())
+    smp2.sample(None, post, initial_model=wl.q0, proposals=K * B, keep_samples=True,
+                proposals_per_graph=B if B > 1 else min(K, 10), **wl.sampler_kwargs())
     host_q, host_x = smp2.samples_host()  # [N][d][C] and [N][C] on the host
     t_e2e = time.perf_counter() - t0
-    ess2 = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K // 2, 100)))
+    ess2 = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K * B // 2, 100 if B == 1 else 200)))
     e2e_value = float(ess2.min() / t_e2e)
+    esize = 8 if wl.sampler_kwargs().get("dtype") == "float64" else 4
     h2d = wl.q0.size * 8 / K
-    d2h = (wl.n_model * wl.chains * 4 + wl.chains * 8)
+    d2h = B * (wl.n_model * wl.chains * esize + wl.chains * 8)
 
     hbm, bf16, bf16s, src = peaks()
     spec = wl.roofline_spec(smp)
@@ -578,14 +643,16 @@ def run_gpu_arm(args, wl):
         peak, psrc, scale = bf16, src, 1e12
     elif spec["bound"] == "hbm":
         peak, psrc, scale = hbm, src, 1e9
+    elif spec["bound"] == "fp64":  # nominal FP64 rate of the part
+        peak, psrc, scale = 1.25, "nominal", 1e12
     else:  # FP32 issue rate: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz, nominal
         peak, psrc, scale = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal", 1e12
     achieved = spec["work"] / t_gemm / scale
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded)", "config": wl.config(),
-        "leapfrog_steps_per_s": wl.chains * wl.L * K / t_dev * world,
+        "dtype": "f64" if esize == 8 else "f32", "data": "synthetic (seeded)", "config": wl.config(),
+        "leapfrog_steps_per_s": wl.chains * wl.L * K * B / t_dev * world,
         "moment_error": {"mean": me, "std": se}, "acceptance": acc,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds": t_e2e},
@@ -597,9 +664,10 @@ def run_gpu_arm(args, wl):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        v, (cme, cse), dt, lps = cpu_reference_run(wl, args.cpu_chains, 2, args.cpu_steps)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{args.cpu_chains} chains x {args.cpu_steps} proposals, numpy port "
+        cc, cs = getattr(wl, "cpu_sample", (args.cpu_chains, args.cpu_steps))
+        v, (cme, cse), dt, lps = cpu_reference_run(wl, cc, 2, cs)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1 if cc == 1 else os.cpu_count(), "kind": "port",
+                                "sample": f"{cc} chains x {cs} proposals, numpy port "
                                           f"batched over chains ({dt:.1f} s, {lps:.0f} leapfrog steps/s)"}
     if rank == 0:
         print(json.dumps(line))

@@ -22,21 +22,27 @@ constexpr int ESS_CH = 32;  // half-chains per block
 // autocovariance sums for lags 0..T-1, written to part[(i*nblk + b)*(T+2) + ...]
 //   [0] sum of half-chain means, [1] sum of squared means, [2..] sum over
 //   half-chains of gamma_{m,t} (with 1/n normalisation).
-template <typename T>
+// STAGE: the half-chains' draws are copied to shared memory (n <= 1024);
+// otherwise they are read from the sample array in place (long single runs).
+template <typename T, bool STAGE>
 __global__ void ess_partial_kernel(const T* __restrict__ x, int64_t N, int64_t d, int64_t C, int n, int lags,
                                    double* __restrict__ part, double* __restrict__ wsum) {
-  extern __shared__ float sx[];  // [n][ESS_CH]
+  extern __shared__ float sx_raw[];  // [n][ESS_CH] when staged
   const int64_t i = blockIdx.y;
   const int nblk = gridDim.x;
   const int64_t m = (int64_t)blockIdx.x * ESS_CH + threadIdx.x;  // half-chain index
   const int64_t M = 2 * C;
   const bool live = m < M;
   const int64_t c = m % C, half = m / C;
+  // draw k of this half-chain (as FP32, staged or read in place)
+  auto draw = [&](int k) -> float {
+    return STAGE ? sx_raw[k * ESS_CH + threadIdx.x] : (float)x[((half * n + k) * d + i) * C + c];
+  };
   double mean = 0.0;
   if (live) {
     for (int k = 0; k < n; ++k) {
       const float v = (float)x[((half * n + k) * d + i) * C + c];
-      sx[k * ESS_CH + threadIdx.x] = v;
+      if (STAGE) sx_raw[k * ESS_CH + threadIdx.x] = v;
       mean += v;
     }
     mean /= n;
@@ -65,8 +71,7 @@ __global__ void ess_partial_kernel(const T* __restrict__ x, int64_t N, int64_t d
   for (int t = 0; t < lags; ++t) {
     double g = 0.0;
     if (live && t < n) {
-      for (int k = 0; k + t < n; ++k)
-        g += ((double)sx[k * ESS_CH + threadIdx.x] - mean) * ((double)sx[(k + t) * ESS_CH + threadIdx.x] - mean);
+      for (int k = 0; k + t < n; ++k) g += ((double)draw(k) - mean) * ((double)draw(k + t) - mean);
       g /= n;
       if (t == 0) var = g * n / (n - 1);  // unbiased within-half-chain variance
     }
@@ -139,25 +144,26 @@ extern "C" HMC_API int hmc_ess(int dtype, int64_t N, int64_t d, int64_t C, const
                                double* work, double* ess, double* rhat, void* stream) {
   HMC_REQUIRE(N >= 4 && d > 0 && C > 0, "hmc_ess: need at least 4 draws, 1 parameter, 1 chain");
   HMC_REQUIRE(samples && work && ess, "hmc_ess: null argument");
+  HMC_REQUIRE(N / 2 <= (1ll << 30), "hmc_ess: too many draws");
   const int n = (int)(N / 2);
-  HMC_REQUIRE(n <= 1024, "hmc_ess: at most 2048 draws per chain (thin the samples)");
   HMC_REQUIRE(lags >= 2 && lags <= n, "hmc_ess: lags must be in [2, N/2]");
+  const bool stage = n <= 1024;
   HMC_REQUIRE(d <= 65535, "hmc_ess: too many parameters for one call");
   const int64_t M = 2 * C;
   const int nblk = (int)((M + ESS_CH - 1) / ESS_CH);
   double* part = work;
   double* wsum = work + d * nblk * (lags + 2);
-  const size_t smem = (size_t)n * ESS_CH * sizeof(float);
+  const size_t smem = stage ? (size_t)n * ESS_CH * sizeof(float) : 0;
   cudaStream_t st = as_stream(stream);
   const dim3 grid(nblk, (unsigned)d);
   if (dtype == HMC_F32) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(ess_partial_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    ess_partial_kernel<float><<<grid, ESS_CH, smem, st>>>((const float*)samples, N, d, C, n, lags, part, wsum);
+    auto kern = stage ? ess_partial_kernel<float, true> : ess_partial_kernel<float, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, ESS_CH, smem, st>>>((const float*)samples, N, d, C, n, lags, part, wsum);
   } else if (dtype == HMC_F64) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(ess_partial_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    ess_partial_kernel<double><<<grid, ESS_CH, smem, st>>>((const double*)samples, N, d, C, n, lags, part, wsum);
+    auto kern = stage ? ess_partial_kernel<double, true> : ess_partial_kernel<double, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, ESS_CH, smem, st>>>((const double*)samples, N, d, C, n, lags, part, wsum);
   } else {
     return fail(HMC_ERR_INVALID_ARG, "hmc_ess: unknown dtype %d", dtype);
   }

@@ -9,9 +9,9 @@
 //
 // Each lane owns the rows lane, lane + 32, ... of the chain's state.  The
 // arithmetic follows the launch-per-step path operation by operation (same
-// random draws, same order of the sums in the gradient, the same
-// (acc - Gtd0) + prior-gradient composition), so the two paths agree to the
-// last bits of the FP64 sums: only the order of the warp reductions differs.
+// random draws, the same (GtG q - Gtd0) + prior-gradient composition, the
+// same casts); the sums of the products and of the energies are taken in a
+// different order, so the two paths agree to rounding of those sums.
 #include "common.cuh"
 
 namespace hmc {
@@ -73,18 +73,27 @@ __device__ __forceinline__ T momentum_draw(const State<T>& s, int d, int i, int6
   return j == 0 ? z[0] : (j == 1 ? z[1] : (j == 2 ? z[2] : z[3]));
 }
 
-// out[k] = sum_j GtG[row][j] q[j] for the lane's rows (q published in qw)
+// out[k] = sum_j GtG[row][j] q[j] for the lane's rows (q published in qw).
+// Four partial sums per row (j mod 4) keep four independent FMA chains in
+// flight; they are combined as (s0 + s1) + (s2 + s3).
 template <typename T, int E>
 __device__ __forceinline__ void matvec(const T* A, int ld, int d, const T* qw, int lane, T out[E]) {
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
-    T acc = (T)0;
+    T s0 = (T)0, s1 = (T)0, s2 = (T)0, s3 = (T)0;
     if (i < d) {
       const T* row = A + i * ld;
-      for (int j = 0; j < d; ++j) acc += row[j] * qw[j];
+      int j = 0;
+      for (; j + 4 <= d; j += 4) {
+        s0 += row[j] * qw[j];
+        s1 += row[j + 1] * qw[j + 1];
+        s2 += row[j + 2] * qw[j + 2];
+        s3 += row[j + 3] * qw[j + 3];
+      }
+      for (; j < d; ++j) s0 += row[j] * qw[j];
     }
-    out[k] = acc;
+    out[k] = (s0 + s1) + (s2 + s3);
   }
 }
 

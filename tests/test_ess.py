@@ -51,3 +51,19 @@ def test_device_ess_and_moments_match_oracle():
         mean, std = diagnostics.moments(t)
         np.testing.assert_allclose(mean, xr.mean(axis=(0, 2)), rtol=1e-9, atol=1e-12)
         np.testing.assert_allclose(std, xr.std(axis=(0, 2)), rtol=1e-9)
+
+
+@pytest.mark.gpu
+def test_device_ess_of_one_long_chain_matches_oracle():
+    """A single chain of 6000 draws (halves longer than the staged path
+    holds): the draws are read in place; same estimate as the oracle."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from hmclab_gb300 import diagnostics
+
+    x = ar1(6000, 3, 1, [0.0, 0.5, 0.95], seed=4)
+    t = torch.from_numpy(x).to("cuda", torch.float64)
+    e = diagnostics.ess(t, lags=300)
+    e_ref, _ = O.ess_split(t.double().cpu().numpy(), 300)
+    np.testing.assert_allclose(e, e_ref, rtol=1e-6)
