@@ -61,7 +61,9 @@ def test_persistent_matches_launch_per_step(d, prior, mass, integrator, dtype):
     assert differ == 0 if dtype == "float64" else differ <= 1
     acc = np.mean(runs[0].accepted_proposals) / P
     assert 0.1 < acc <= 1.0, acc
-    tol = 1e-12 if dtype == "float64" else 1e-5
+    # FP32 at d >= 64: the launch-per-step path contracts on the tensor cores
+    # (BF16 hi/lo products, ~1e-6 per gradient), and 42 kicks compound it
+    tol = 1e-12 if dtype == "float64" else (1e-5 if d < 64 else 5e-5)
     same = np.asarray(runs[0].accepted_proposals) == np.asarray(runs[1].accepted_proposals)
     err = np.abs(a - b) / np.abs(b).max(axis=(0, 2), keepdims=True)
     if dtype == "float32":
