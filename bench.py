@@ -821,7 +821,10 @@ def run_fwi_arm(args, wl):
                     **dict(kw, amount_of_steps=L_s, stepsize=eps_s))
                 a = float(np.mean(p_smp.accepted_proposals) / 4)
                 pilot.append((a * (L_s * eps_s) ** 2, L_s, eps_s, a))
-        _, L_best, eps_best, _ = max(pilot)
+        # settings that kept at least a quarter of the pilot proposals: the
+        # estimate of a lower acceptance from 4 proposals is too noisy to trust
+        usable = [x for x in pilot if x[3] >= 0.25] or pilot
+        _, L_best, eps_best, _ = max(usable)
     else:
         L_best, eps_best = args.surrogate_L, args.surrogate_stepsize
 

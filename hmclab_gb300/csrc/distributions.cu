@@ -232,7 +232,18 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
       double me = 0.0;
       for (int64_t s = 0; s < S; ++s) {
         const T dx = x - srx[s], dy = y - sry[s], dz = z - srz[s];
-        const T dist = sqrt(dx * dx + dy * dy + dz * dz);
+        const T r2 = dx * dx + dy * dy + dz * dz;
+        // FP32: one reciprocal square root per pair gives both the distance
+        // and 1 / distance (within 2 ulp); FP64 keeps the correctly rounded
+        // square root of the reference's arithmetic
+        T dist, inv_dist;
+        if (sizeof(T) == 4) {
+          inv_dist = (T)rsqrtf((float)r2);
+          dist = r2 > (T)0 ? r2 * inv_dist : (T)0;
+        } else {
+          dist = sqrt(r2);
+          inv_dist = (T)1 / dist;
+        }
         const T tc = t0 + dist * inv_v;
         const T o = obs[e * S + s], w = iv[e * S + s];
         if (!GRAD) {
@@ -243,7 +254,7 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
           const T mg = (tc - o) * w;  // (t_calc - obs) / std^2
           // one reciprocal per pair; at dist = 0 the partials are 0 * inf =
           // NaN and skipped, like nansum's 0 / 0
-          const T inv_vd = inv_v / dist;
+          const T inv_vd = inv_v * inv_dist;
           T t;
           t = mg * (dx * inv_vd);
           if (!isnan(t)) gx += t;

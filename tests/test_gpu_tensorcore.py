@@ -108,7 +108,8 @@ def test_fused_sampler_tracks_fp64_oracle(golden):
     smp = H.Samplers.HMC(seed=0)
     smp.sample(None, post, stepsize=float(g["stepsize"]), amount_of_steps=20,
                mass_matrix=H.MassMatrices.Diagonal(g["diag"]), initial_model=g["q0"], proposals=P, chains=3,
-               dtype="float32", rng_streams=(g["z"], g["f"], g["u"]), keep_samples=True, proposals_per_graph=4)
+               dtype="float32", rng_streams=(g["z"], g["f"], g["u"]), keep_samples=True, proposals_per_graph=4,
+               persistent=False)
     assert smp._fused is not None
     opost = O.Sum([O.NormalDiag(np.zeros(d), np.ones(d)), O.DensePremul(g["G"], g["d"], 0.0025)])
     res = O.run_chains(opost, O.Mass("diag", diag=g["diag"]), g["q0"], float(g["stepsize"]), (g["z"], g["f"], g["u"]),
@@ -121,3 +122,27 @@ def test_fused_sampler_tracks_fp64_oracle(golden):
     assert rel < 1e-5
     xr = np.transpose(res["samples"][:, -1], (1, 0))
     np.testing.assert_allclose(smp.samples_numpy()[:, -1], xr, rtol=1e-5)
+
+
+def test_persistent_fp32_sampler_tracks_fp64_oracle(golden):
+    """The same cfg2-small chains through the persistent kernel (FP32, one
+    launch per block of proposals) against the FP64 oracle."""
+    g = golden("cfg2_small_normal.npz")
+    d = g["G"].shape[1]
+    lik = H.Distributions.LinearMatrix(g["G"], g["d"], 0.0025, dtype=np.float64)
+    post = H.Distributions.BayesRule([H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1))), lik])
+    P = 8
+    smp = H.Samplers.HMC(seed=0).sample(
+        None, post, stepsize=float(g["stepsize"]), amount_of_steps=20, mass_matrix=H.MassMatrices.Diagonal(g["diag"]),
+        initial_model=g["q0"], proposals=P, chains=3, dtype="float32", rng_streams=(g["z"], g["f"], g["u"]),
+        keep_samples=True, proposals_per_graph=4)
+    assert smp._persistent is not None
+    opost = O.Sum([O.NormalDiag(np.zeros(d), np.ones(d)), O.DensePremul(g["G"], g["d"], 0.0025)])
+    res = O.run_chains(opost, O.Mass("diag", diag=g["diag"]), g["q0"], float(g["stepsize"]), (g["z"], g["f"], g["u"]),
+                       P, amount_of_steps=20)
+    got = smp.samples_numpy()[:, :-1]
+    ref = np.transpose(res["samples"][:, :-1], (2, 1, 0))
+    assert np.array_equal(np.atleast_1d(smp.accepted_proposals), res["accepted"])
+    rel = np.abs(got - ref).max() / np.abs(ref).max()
+    print(f"persistent FP32 chains vs FP64 oracle: max relative deviation {rel:.2e}")
+    assert rel < 1e-5
