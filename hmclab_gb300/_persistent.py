@@ -4,8 +4,9 @@ per chain, with an autotuner that picks the chains per block.
 
 Applies when the target is a premultiplied dense `LinearMatrix` with
 d <= 128, alone or in a `BayesRule` with one diagonal `Normal` or `Laplace`
-prior, the mass matrix is unit or diagonal, and the run has no bounds, no
-autotuning, no temperatures, no surrogate and no training set.
+prior, the mass matrix is unit, diagonal or full (its inverse and Cholesky
+factor then share the block's shared memory with GtG), and the run has no
+bounds, no autotuning, no temperatures, no surrogate and no training set.
 """
 import ctypes as _ct
 
@@ -13,6 +14,13 @@ from hmclab_gb300 import _lib
 
 MAX_D = 128
 _WARPS = (1, 2, 4, 8, 16)
+_SMEM = 227 * 1024
+
+
+def _smem(d, full, warps, esize):
+    """Shared memory of one block: GtG (and M^-1, L for a full mass) with an
+    odd row stride, plus one vector per warp (as in csrc/persistent.cu)."""
+    return ((3 if full else 1) * d * (d | 1) + warps * d) * esize
 # chosen launch shapes, per (dimension, chains, dtype, mass, prior, schedule length)
 _tuned = {}
 
@@ -35,7 +43,9 @@ class PersistentDense:
 
         if getattr(sampler, "use_persistent", None) is False:
             return None
-        if sampler.dimensions > MAX_D or sampler.mass_matrix.kind == _lib.HMC_MASS_FULL:
+        full = sampler.mass_matrix.kind == _lib.HMC_MASS_FULL
+        esize = 8 if sampler.dtype == "float64" else 4
+        if sampler.dimensions > MAX_D or _smem(sampler.dimensions, full, 1, esize) > _SMEM:
             return None
         if sampler.autotuning or getattr(sampler, "beta", None) is not None:
             return None
@@ -100,7 +110,11 @@ class PersistentDense:
         if slen > 0:
             proposals = min(proposals, slen)
         best = None
+        full = self.smp.mass_matrix.kind == _lib.HMC_MASS_FULL
+        esize = 8 if self.smp.dtype == "float64" else 4
         for w in _WARPS:
+            if _smem(self.smp.dimensions, full, w, esize) > _SMEM:
+                continue
             self._call(1, w, True, h)  # warm
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)

@@ -42,6 +42,8 @@ struct State {
   int randomize;
   const T* mdiag;
   const T* minv;
+  const T* mchol;      // FULL: lower Cholesky factor of M, [d][d]
+  const T* mfull_inv;  // FULL: M^-1, [d][d]
   const T* sz;
   const T* seps;
   const double* su;
@@ -97,16 +99,47 @@ __device__ __forceinline__ void matvec(const T* A, int ld, int d, const T* qw, i
   }
 }
 
+// mp = M^-1 p for the lane's rows: unit, diagonal, or (FULL) the product
+// with the explicit inverse held in shared memory (p published in qw).
+template <typename T, int E, int MASS>
+__device__ __forceinline__ void apply_minv(const T* Mi, int ld, int d, T* qw, int lane, const bool live[E],
+                                           const T minv[E], const T p[E], T mp[E]) {
+  if (MASS == HMC_MASS_FULL) {
+#pragma unroll
+    for (int k = 0; k < E; ++k)
+      if (live[k]) qw[lane + 32 * k] = p[k];
+    __syncwarp();
+    matvec<T, E>(Mi, ld, d, qw, lane, mp);
+    __syncwarp();
+  } else {
+#pragma unroll
+    for (int k = 0; k < E; ++k) mp[k] = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
+  }
+}
+
+// Shared-memory matrices of one block: GtG, and for a full mass its
+// inverse and Cholesky factor, each [d][ld]; then one q vector per warp.
+template <typename T>
+__device__ __forceinline__ void load_matrix(T* dst, const T* src, int d, int ld) {
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    const int r = e / d;
+    dst[r * ld + (e - r * d)] = src[e];
+  }
+}
+
 template <typename T, int E, int MASS, int PRIOR>
 __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Target<T> tg, hmc_schedule sch,
                                                                int64_t nprop, int dry) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int d = tg.d, ld = tg.ld;
-  T* A = (T*)smem_raw;  // [d][ld]
-  T* qbuf = A + d * ld;  // [warps][d]
-  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
-    const int r = e / d;
-    A[r * ld + (e - r * d)] = tg.GtG[e];
+  T* A = (T*)smem_raw;                                  // GtG [d][ld]
+  T* Mi = A + d * ld;                                   // M^-1 [d][ld] (FULL)
+  T* Lc = Mi + (MASS == HMC_MASS_FULL ? d * ld : 0);    // Cholesky factor [d][ld] (FULL)
+  T* qbuf = Lc + (MASS == HMC_MASS_FULL ? d * ld : 0);  // [warps][d]
+  load_matrix(A, tg.GtG, d, ld);
+  if (MASS == HMC_MASS_FULL) {
+    load_matrix(Mi, s.mfull_inv, d, ld);
+    load_matrix(Lc, s.mchol, d, ld);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -152,13 +185,27 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       p[k] = (T)0;
-      q[k] = qc[k];
       if (live[k]) {
         const T z = momentum_draw(s, d, lane + 32 * k, c, n);
         p[k] = MASS == HMC_MASS_DIAG ? msq[k] * z : z;
-        const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
-        k0 += (double)p[k] * (double)mp;
-        q[k] = qc[k] + ce * mp;
+      }
+    }
+    if (MASS == HMC_MASS_FULL) {  // p = L z
+#pragma unroll
+      for (int k = 0; k < E; ++k)
+        if (live[k]) qw[lane + 32 * k] = p[k];
+      __syncwarp();
+      matvec<T, E>(Lc, ld, d, qw, lane, p);
+      __syncwarp();
+    }
+    T mp[E];
+    apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      q[k] = qc[k];
+      if (live[k]) {
+        k0 += (double)p[k] * (double)mp[k];
+        q[k] = qc[k] + ce * mp[k];
       }
     }
     k0 = 0.5 * warp_sum(k0);
@@ -184,11 +231,9 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
       }
       if (sch.drift[st] != 0.0) {
         const T cd = (T)(sch.drift[st] * (double)e);
+        apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
 #pragma unroll
-        for (int k = 0; k < E; ++k) {
-          const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
-          q[k] = q[k] + cd * mp;
-        }
+        for (int k = 0; k < E; ++k) q[k] = q[k] + cd * mp[k];
       }
     }
 
@@ -200,6 +245,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
     T aq[E];
     matvec<T, E>(A, ld, d, qw, lane, aq);
     __syncwarp();
+    apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
     double lik = 0.0, pri = 0.0, k1 = 0.0;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
@@ -211,8 +257,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
         pri += (double)r * (double)(pw[k] * r);
       }
       if (PRIOR == PRIOR_LAPLACE) pri += (double)(fabs(q[k] - pm[k]) * pw[k]);
-      const T mp = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
-      k1 += (double)p[k] * (double)mp;
+      k1 += (double)p[k] * (double)mp[k];
     }
     lik = 0.5 * (warp_sum(lik) + tg.dtd);
     k1 = 0.5 * warp_sum(k1);
@@ -254,10 +299,16 @@ using namespace hmc::pers;
 
 namespace {
 
+template <typename T>
+size_t persistent_smem(int d, int mass_kind, int warps) {
+  const size_t ld = (size_t)(d | 1);
+  return ((mass_kind == HMC_MASS_FULL ? 3 : 1) * (size_t)d * ld + (size_t)warps * d) * sizeof(T);
+}
+
 template <typename T, int E, int MASS>
 int launch_prior(int prior, const State<T>& st, const Target<T>& tg, const hmc_schedule& sch, int64_t nprop,
                  int dry, int warps, cudaStream_t stream) {
-  const size_t smem = ((size_t)tg.d * tg.ld + (size_t)warps * tg.d) * sizeof(T);
+  const size_t smem = persistent_smem<T>(tg.d, MASS, warps);
   auto kern = prior == PRIOR_NORMAL    ? persistent_dense_kernel<T, E, MASS, PRIOR_NORMAL>
               : prior == PRIOR_LAPLACE ? persistent_dense_kernel<T, E, MASS, PRIOR_LAPLACE>
                                        : persistent_dense_kernel<T, E, MASS, PRIOR_NONE>;
@@ -278,8 +329,9 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
   HMC_REQUIRE(s->dims > 0 && s->dims <= MAX_D, "%s: dimension %lld outside 1..%d", who, (long long)s->dims, MAX_D);
   HMC_REQUIRE(s->chains > 0 && s->chains <= 0x7FFFFFFFll * 16, "%s: bad number of chains", who);
   HMC_REQUIRE(s->q_cur && s->x_cur && s->eps && s->accepted && s->proposal, "%s: missing state buffer", who);
-  HMC_REQUIRE(s->mass_kind == HMC_MASS_UNIT || s->mass_kind == HMC_MASS_DIAG, "%s: unit or diagonal mass only", who);
+  HMC_REQUIRE(s->mass_kind >= HMC_MASS_UNIT && s->mass_kind <= HMC_MASS_FULL, "%s: bad mass kind", who);
   if (s->mass_kind == HMC_MASS_DIAG) HMC_REQUIRE(s->mass_diag && s->mass_inv_diag, "%s: diagonal mass buffers", who);
+  if (s->mass_kind == HMC_MASS_FULL) HMC_REQUIRE(s->mass_chol && s->mass_inv, "%s: full mass buffers", who);
   HMC_REQUIRE(!s->lower && !s->upper, "%s: bounded targets use the launch-per-step path", who);
   HMC_REQUIRE(!s->autotune, "%s: autotuning uses the launch-per-step path", who);
   HMC_REQUIRE(!s->beta, "%s: tempered chains use the launch-per-step path", who);
@@ -294,6 +346,8 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
     HMC_REQUIRE(s->stream_z && s->stream_u && s->stream_len >= nprop && (s->stream_eps || !s->randomize_stepsize),
                 "%s: injected streams shorter than the launch", who);
   if (s->ring_q) HMC_REQUIRE(s->ring_x && s->ring_slots > 0 && s->thinning > 0, "%s: bad sample ring", who);
+  HMC_REQUIRE(persistent_smem<T>((int)s->dims, s->mass_kind, warps) <= 227 * 1024,
+              "%s: the matrices of d = %lld do not fit in shared memory", who, (long long)s->dims);
   if (nprop == 0) return HMC_OK;
   State<T> st;
   st.C = s->chains;
@@ -306,6 +360,8 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
   st.randomize = s->randomize_stepsize;
   st.mdiag = (const T*)s->mass_diag;
   st.minv = (const T*)s->mass_inv_diag;
+  st.mchol = (const T*)s->mass_chol;
+  st.mfull_inv = (const T*)s->mass_inv;
   st.sz = (const T*)s->stream_z;
   st.seps = (const T*)s->stream_eps;
   st.su = s->stream_u;
@@ -323,12 +379,13 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
   tg.pmean = (const T*)pmean;
   tg.pw = (const T*)pw;
   const int E = (tg.d + 31) / 32;
-  const bool diag = s->mass_kind == HMC_MASS_DIAG;
+  const int mk = s->mass_kind;
   int rc;
-#define HMC_PERSIST_CASE(EV)                                                                          \
-  case EV:                                                                                            \
-    rc = diag ? launch_prior<T, EV, HMC_MASS_DIAG>(prior, st, tg, *sch, nprop, dry, warps, stream)    \
-              : launch_prior<T, EV, HMC_MASS_UNIT>(prior, st, tg, *sch, nprop, dry, warps, stream);   \
+#define HMC_PERSIST_CASE(EV)                                                                               \
+  case EV:                                                                                                 \
+    rc = mk == HMC_MASS_DIAG   ? launch_prior<T, EV, HMC_MASS_DIAG>(prior, st, tg, *sch, nprop, dry, warps, stream) \
+         : mk == HMC_MASS_FULL ? launch_prior<T, EV, HMC_MASS_FULL>(prior, st, tg, *sch, nprop, dry, warps, stream) \
+                               : launch_prior<T, EV, HMC_MASS_UNIT>(prior, st, tg, *sch, nprop, dry, warps, stream); \
     break;
   switch (E) {
     HMC_PERSIST_CASE(1)

@@ -516,7 +516,9 @@ HMC_API int hmc_moments(int dtype, int64_t N, int64_t d, int64_t C,
  * 0.5 (m^T (GtG m - 2 Gtd0) + dtd)) with d <= 128, GtG held in shared
  * memory.  prior: 0 none, 1 Normal with diagonal inverse variances prior_w
  * (base.py:539-570), 2 Laplace with inverse dispersions prior_w
- * (base.py:689-710).  Unit or diagonal mass, no bounds, no autotuning, no
+ * (base.py:689-710).  Unit, diagonal or full mass (a full mass keeps M^-1
+ * and its Cholesky factor in shared memory too: 3 d (d|1) elements plus a
+ * vector per warp must fit in 227 KB), no bounds, no autotuning, no
  * temperatures.  The proposals are numbered from s->proposal[0] on, as
  * hmc_begin_trajectory / hmc_end_trajectory number them (same random draws,
  * injected streams included), and the counter is advanced by `proposals`.

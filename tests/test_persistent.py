@@ -37,6 +37,7 @@ def _problem(d, prior, seed):
 
 @pytest.mark.parametrize("d,prior,mass,integrator", [
     (24, "normal", "unit", "lf"), (50, "laplace", "diag", "lf"), (97, "none", "diag", "3s"), (128, "normal", "unit", "4s"),
+    (40, "normal", "full", "lf"), (80, "laplace", "full", "3s"),
 ])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_persistent_matches_launch_per_step(d, prior, mass, integrator, dtype):
@@ -46,7 +47,13 @@ def test_persistent_matches_launch_per_step(d, prior, mass, integrator, dtype):
     C, P = 96, 7
     rng = np.random.default_rng(1)
     q0 = m + 0.02 * rng.normal(size=(d, C))
-    mm = None if mass == "unit" else H.MassMatrices.Diagonal(rng.uniform(0.5, 2.0, size=(d, 1)))
+    if mass == "unit":
+        mm = None
+    elif mass == "diag":
+        mm = H.MassMatrices.Diagonal(rng.uniform(0.5, 2.0, size=(d, 1)))
+    else:
+        A = rng.normal(size=(d, d)) / np.sqrt(d)
+        mm = H.MassMatrices.Full(A @ A.T + np.eye(d))
     runs = []
     for persistent in (True, False):
         smp = H.Samplers.HMC(seed=11).sample(
