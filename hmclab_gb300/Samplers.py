@@ -713,3 +713,14 @@ class HMC:
         assert names is not None, "no samples file was written"
         with _Samples(names[chain], burn_in=burn_in) as s:
             return _numpy.array(s.numpy)
+
+
+def run_together(samplers, n_proposals, warps_per_block=None):
+    """Advance several prepared `HMC` samplers (`HMC.prepare`) whose targets
+    are small dense linear-Gaussian posteriors of different dimensions by
+    `n_proposals` proposals each, all of them in one persistent launch per
+    block of proposals; finish each with `finish()` afterwards.  Returns the
+    chains per block that were used."""
+    from hmclab_gb300._persistent import run_groups
+
+    return run_groups(samplers, n_proposals, warps_per_block)

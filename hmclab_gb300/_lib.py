@@ -121,6 +121,20 @@ class HmcSchedule(_ct.Structure):
     ]
 
 
+class HmcDenseGroup(_ct.Structure):
+    """Mirror of `hmc_dense_group` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("chains", c_void_p),
+        ("GtG", c_void_p),
+        ("Gtd0", c_void_p),
+        ("dtd", _ct.c_double),
+        ("prior", _ct.c_int),
+        ("prior_mean", c_void_p),
+        ("prior_w", c_void_p),
+    ]
+
+
 class HmcMlpOut(_ct.Structure):
     """Mirror of `hmc_mlp_out` in include/hmclab_gb300.h."""
 
@@ -179,6 +193,7 @@ SIGNATURES = {
     "hmc_gemm": [I, I64, I64, I64, D, P, P, P, P, I, S],
     "hmc_exchange": [P, I64, P, P, P, P, S],
     "hmc_persistent_dense": [P, P, P, D, I, P, P, P, I64, I, I, S],
+    "hmc_persistent_dense_groups": [P, I, P, I64, I, I, S],
     "hmc_gemm_splitk": [I, I64, I64, I64, D, P, P, P, I, P, I64, S],
     "hmc_split_bf16": [I64, I64, P, I64, P, P, S],
     "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],

@@ -132,3 +132,72 @@ class PersistentDense:
         if self.warps is None:
             self.autotune(h)
         self._call(n, self.warps, False, h)
+
+
+def run_groups(samplers, n_proposals, warps=None):
+    """Advance several prepared samplers — different targets, dimensions and
+    chain counts, each eligible for the persistent kernel — by n_proposals
+    each, with one launch per block of proposals for all of them (the
+    sampler of the first target provides the stream).  Returns the chains
+    per block used."""
+    import torch
+
+    ps = [s._persistent for s in samplers]
+    if any(p is None for p in ps):
+        raise ValueError("every sampler must run the persistent kernel (small dense linear-Gaussian target)")
+    s0 = samplers[0]
+    for s in samplers[1:]:
+        if (s.dtype, s.mass_matrix.kind, s._persistent.prior_kind) != (s0.dtype, s0.mass_matrix.kind, ps[0].prior_kind):
+            raise ValueError("grouped samplers must share dtype, mass kind and prior kind")
+        if s._schedule != s0._schedule:
+            raise ValueError("grouped samplers must share the integrator and its number of steps")
+    st = s0.stream
+    h = st.cuda_stream
+    for s in samplers[1:]:
+        st.wait_stream(s.stream)
+    groups = (_lib.HmcDenseGroup * len(samplers))()
+    for g, (s, p) in enumerate(zip(samplers, ps)):
+        groups[g].chains = _ct.addressof(s._state)
+        groups[g].GtG, groups[g].Gtd0, groups[g].dtd = p.GtG.data_ptr(), p.Gtd0.data_ptr(), p.dtd
+        groups[g].prior = p.prior_kind
+        groups[g].prior_mean = p.pmean.data_ptr() if p.pmean is not None else None
+        groups[g].prior_w = p.pw.data_ptr() if p.pw is not None else None
+    k = min(s.proposals_per_graph for s in samplers)
+
+    def call(n, w, dry):
+        _lib.call("hmc_persistent_dense_groups", groups, len(samplers), ps[0]._sched_ref, n, w, int(dry), h)
+
+    if warps is None:
+        full = s0.mass_matrix.kind == _lib.HMC_MASS_FULL
+        esize = 8 if s0.dtype == "float64" else 4
+        dmax = max(s.dimensions for s in samplers)
+        best = None
+        for w in _WARPS:
+            if _smem(dmax, full, w, esize) > _SMEM:
+                continue
+            call(1, w, True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            call(1, w, True)
+            e1.record(st)
+            st.synchronize()
+            if best is None or e0.elapsed_time(e1) < best[0]:
+                best = (e0.elapsed_time(e1), w)
+        warps = best[1]
+    done = 0
+    while done < n_proposals:
+        n = min(k, n_proposals - done, *(s.proposals - s._done for s in samplers))
+        if n <= 0:
+            break
+        for s in samplers:
+            s._load_streams(s._done, n)
+        for s in samplers[1:]:
+            st.wait_stream(s.stream)
+        call(n, warps, False)
+        for s in samplers[1:]:
+            s.stream.wait_stream(st)
+        for s in samplers:
+            s._drain(s._done, n)
+            s._done += n
+        done += n
+    return warps

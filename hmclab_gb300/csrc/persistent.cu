@@ -23,6 +23,7 @@ enum PriorKind { PRIOR_NONE = 0, PRIOR_NORMAL = 1, PRIOR_LAPLACE = 2 };
 template <typename T>
 struct Target {
   int d, ld;  // dimension, odd row stride of GtG in shared memory
+  int prior;  // PriorKind
   const T* GtG;
   const T* Gtd0;
   double dtd;
@@ -33,6 +34,7 @@ struct Target {
 template <typename T>
 struct State {
   int64_t C;
+  int mass;  // HMC_MASS_*
   T* q_cur;
   double* x_cur;
   const T* eps;
@@ -101,10 +103,10 @@ __device__ __forceinline__ void matvec(const T* A, int ld, int d, const T* qw, i
 
 // mp = M^-1 p for the lane's rows: unit, diagonal, or (FULL) the product
 // with the explicit inverse held in shared memory (p published in qw).
-template <typename T, int E, int MASS>
-__device__ __forceinline__ void apply_minv(const T* Mi, int ld, int d, T* qw, int lane, const bool live[E],
+template <typename T, int E>
+__device__ __forceinline__ void apply_minv(int mass, const T* Mi, int ld, int d, T* qw, int lane, const bool live[E],
                                            const T minv[E], const T p[E], T mp[E]) {
-  if (MASS == HMC_MASS_FULL) {
+  if (mass == HMC_MASS_FULL) {
 #pragma unroll
     for (int k = 0; k < E; ++k)
       if (live[k]) qw[lane + 32 * k] = p[k];
@@ -113,7 +115,7 @@ __device__ __forceinline__ void apply_minv(const T* Mi, int ld, int d, T* qw, in
     __syncwarp();
   } else {
 #pragma unroll
-    for (int k = 0; k < E; ++k) mp[k] = MASS == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
+    for (int k = 0; k < E; ++k) mp[k] = mass == HMC_MASS_DIAG ? minv[k] * p[k] : p[k];
   }
 }
 
@@ -127,11 +129,14 @@ __device__ __forceinline__ void load_matrix(T* dst, const T* src, int d, int ld)
   }
 }
 
-template <typename T, int E, int MASS, int PRIOR>
-__global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Target<T> tg, hmc_schedule sch,
-                                                               int64_t nprop, int dry) {
+// One block of chains of one target: `block` numbers the block within the
+// target's chains (warps of 32 lanes, one chain per warp).
+template <typename T, int E>
+__device__ __forceinline__ void run_block(const State<T>& s, const Target<T>& tg, const hmc_schedule& sch,
+                                          int64_t nprop, int dry, int64_t block) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int d = tg.d, ld = tg.ld;
+  const int MASS = s.mass, PRIOR = tg.prior;  // uniform over the block
   T* A = (T*)smem_raw;                                  // GtG [d][ld]
   T* Mi = A + d * ld;                                   // M^-1 [d][ld] (FULL)
   T* Lc = Mi + (MASS == HMC_MASS_FULL ? d * ld : 0);    // Cholesky factor [d][ld] (FULL)
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  const int64_t c = block * (blockDim.x >> 5) + warp;
   if (c >= s.C) return;  // whole warps only; no block barrier follows
   T* qw = qbuf + warp * d;
   const int64_t n0 = s.control[0];
@@ -199,7 +204,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
       __syncwarp();
     }
     T mp[E];
-    apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
+    apply_minv<T, E>(MASS, Mi, ld, d, qw, lane, live, minv, p, mp);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       q[k] = qc[k];
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
       }
       if (sch.drift[st] != 0.0) {
         const T cd = (T)(sch.drift[st] * (double)e);
-        apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
+        apply_minv<T, E>(MASS, Mi, ld, d, qw, lane, live, minv, p, mp);
 #pragma unroll
         for (int k = 0; k < E; ++k) q[k] = q[k] + cd * mp[k];
       }
@@ -245,7 +250,7 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
     T aq[E];
     matvec<T, E>(A, ld, d, qw, lane, aq);
     __syncwarp();
-    apply_minv<T, E, MASS>(Mi, ld, d, qw, lane, live, minv, p, mp);
+    apply_minv<T, E>(MASS, Mi, ld, d, qw, lane, live, minv, p, mp);
     double lik = 0.0, pri = 0.0, k1 = 0.0;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
@@ -289,6 +294,31 @@ __global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Targe
   }
 }
 
+template <typename T, int E>
+__global__ void __launch_bounds__(512) persistent_dense_kernel(State<T> s, Target<T> tg, hmc_schedule sch,
+                                                               int64_t nprop, int dry) {
+  run_block<T, E>(s, tg, sch, nprop, dry, blockIdx.x);
+}
+
+// Several targets of different dimensions (and chain counts) in one launch:
+// group g owns the blocks [block0, next group's block0).
+constexpr int MAX_GROUPS = 48;
+template <typename T>
+struct GroupTable {
+  int n;
+  int block0[MAX_GROUPS];
+  State<T> s[MAX_GROUPS];
+  Target<T> tg[MAX_GROUPS];
+};
+
+template <typename T, int E>
+__global__ void __launch_bounds__(512) persistent_groups_kernel(GroupTable<T> tab, hmc_schedule sch, int64_t nprop,
+                                                                int dry) {
+  int g = 0;
+  while (g + 1 < tab.n && tab.block0[g + 1] <= (int)blockIdx.x) ++g;
+  run_block<T, E>(tab.s[g], tab.tg[g], sch, nprop, dry, (int64_t)blockIdx.x - tab.block0[g]);
+}
+
 __global__ void advance_counter_kernel(int64_t* control, int64_t n) { control[0] += n; }
 
 }  // namespace pers
@@ -305,13 +335,11 @@ size_t persistent_smem(int d, int mass_kind, int warps) {
   return ((mass_kind == HMC_MASS_FULL ? 3 : 1) * (size_t)d * ld + (size_t)warps * d) * sizeof(T);
 }
 
-template <typename T, int E, int MASS>
-int launch_prior(int prior, const State<T>& st, const Target<T>& tg, const hmc_schedule& sch, int64_t nprop,
-                 int dry, int warps, cudaStream_t stream) {
-  const size_t smem = persistent_smem<T>(tg.d, MASS, warps);
-  auto kern = prior == PRIOR_NORMAL    ? persistent_dense_kernel<T, E, MASS, PRIOR_NORMAL>
-              : prior == PRIOR_LAPLACE ? persistent_dense_kernel<T, E, MASS, PRIOR_LAPLACE>
-                                       : persistent_dense_kernel<T, E, MASS, PRIOR_NONE>;
+template <typename T, int E>
+int launch_single(const State<T>& st, const Target<T>& tg, const hmc_schedule& sch, int64_t nprop, int dry,
+                  int warps, cudaStream_t stream) {
+  const size_t smem = persistent_smem<T>(tg.d, st.mass, warps);
+  auto kern = persistent_dense_kernel<T, E>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(persistent_dense_kernel)");
@@ -321,13 +349,13 @@ int launch_prior(int prior, const State<T>& st, const Target<T>& tg, const hmc_s
   return check_launch("persistent_dense_kernel");
 }
 
+// Checks one target's state and fills the kernel's views of it.
 template <typename T>
-int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, double dtd, int prior,
-                    const void* pmean, const void* pw, const hmc_schedule* sch, int64_t nprop, int warps, int dry,
-                    cudaStream_t stream) {
-  const char* who = "hmc_persistent_dense";
+int fill_target(const char* who, const hmc_chains* s, const void* GtG, const void* Gtd0, double dtd, int prior,
+                const void* pmean, const void* pw, int64_t nprop, int warps, State<T>& st, Target<T>& tg) {
+  HMC_REQUIRE(s != nullptr, "%s: null state", who);
   HMC_REQUIRE(s->dims > 0 && s->dims <= MAX_D, "%s: dimension %lld outside 1..%d", who, (long long)s->dims, MAX_D);
-  HMC_REQUIRE(s->chains > 0 && s->chains <= 0x7FFFFFFFll * 16, "%s: bad number of chains", who);
+  HMC_REQUIRE(s->chains > 0 && s->chains <= 0x7FFFFFFFll, "%s: bad number of chains", who);
   HMC_REQUIRE(s->q_cur && s->x_cur && s->eps && s->accepted && s->proposal, "%s: missing state buffer", who);
   HMC_REQUIRE(s->mass_kind >= HMC_MASS_UNIT && s->mass_kind <= HMC_MASS_FULL, "%s: bad mass kind", who);
   if (s->mass_kind == HMC_MASS_DIAG) HMC_REQUIRE(s->mass_diag && s->mass_inv_diag, "%s: diagonal mass buffers", who);
@@ -338,19 +366,14 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
   HMC_REQUIRE(GtG && Gtd0, "%s: null GtG or Gtd0", who);
   HMC_REQUIRE(prior >= PRIOR_NONE && prior <= PRIOR_LAPLACE, "%s: unknown prior kind %d", who, prior);
   HMC_REQUIRE(prior == PRIOR_NONE || (pmean && pw), "%s: prior parameters missing", who);
-  HMC_REQUIRE(sch && sch->steps >= 1 && sch->steps <= HMC_SCHEDULE_MAX, "%s: bad schedule", who);
-  HMC_REQUIRE(warps == 1 || warps == 2 || warps == 4 || warps == 8 || warps == 16, "%s: warps_per_block %d", who,
-              warps);
-  HMC_REQUIRE(nprop >= 0, "%s: negative proposal count", who);
   if (s->stream_z || s->stream_eps || s->stream_u)
     HMC_REQUIRE(s->stream_z && s->stream_u && s->stream_len >= nprop && (s->stream_eps || !s->randomize_stepsize),
                 "%s: injected streams shorter than the launch", who);
   if (s->ring_q) HMC_REQUIRE(s->ring_x && s->ring_slots > 0 && s->thinning > 0, "%s: bad sample ring", who);
   HMC_REQUIRE(persistent_smem<T>((int)s->dims, s->mass_kind, warps) <= 227 * 1024,
               "%s: the matrices of d = %lld do not fit in shared memory", who, (long long)s->dims);
-  if (nprop == 0) return HMC_OK;
-  State<T> st;
   st.C = s->chains;
+  st.mass = s->mass_kind;
   st.q_cur = (T*)s->q_cur;
   st.x_cur = s->x_cur;
   st.eps = (const T*)s->eps;
@@ -370,35 +393,103 @@ int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, doub
   st.ring_x = s->ring_x;
   st.ring_slots = s->ring_slots;
   st.thin = s->thinning;
-  Target<T> tg;
   tg.d = (int)s->dims;
   tg.ld = tg.d | 1;
+  tg.prior = prior;
   tg.GtG = (const T*)GtG;
   tg.Gtd0 = (const T*)Gtd0;
   tg.dtd = dtd;
   tg.pmean = (const T*)pmean;
   tg.pw = (const T*)pw;
+  return HMC_OK;
+}
+
+int check_common(const char* who, const hmc_schedule* sch, int64_t nprop, int warps) {
+  HMC_REQUIRE(sch && sch->steps >= 1 && sch->steps <= HMC_SCHEDULE_MAX, "%s: bad schedule", who);
+  HMC_REQUIRE(warps == 1 || warps == 2 || warps == 4 || warps == 8 || warps == 16, "%s: warps_per_block %d", who,
+              warps);
+  HMC_REQUIRE(nprop >= 0, "%s: negative proposal count", who);
+  return HMC_OK;
+}
+
+template <typename T>
+int persistent_impl(const hmc_chains* s, const void* GtG, const void* Gtd0, double dtd, int prior,
+                    const void* pmean, const void* pw, const hmc_schedule* sch, int64_t nprop, int warps, int dry,
+                    cudaStream_t stream) {
+  const char* who = "hmc_persistent_dense";
+  HMC_TRY(check_common(who, sch, nprop, warps));
+  State<T> st;
+  Target<T> tg;
+  HMC_TRY(fill_target<T>(who, s, GtG, Gtd0, dtd, prior, pmean, pw, nprop, warps, st, tg));
+  if (nprop == 0) return HMC_OK;
   const int E = (tg.d + 31) / 32;
-  const int mk = s->mass_kind;
   int rc;
-#define HMC_PERSIST_CASE(EV)                                                                               \
-  case EV:                                                                                                 \
-    rc = mk == HMC_MASS_DIAG   ? launch_prior<T, EV, HMC_MASS_DIAG>(prior, st, tg, *sch, nprop, dry, warps, stream) \
-         : mk == HMC_MASS_FULL ? launch_prior<T, EV, HMC_MASS_FULL>(prior, st, tg, *sch, nprop, dry, warps, stream) \
-                               : launch_prior<T, EV, HMC_MASS_UNIT>(prior, st, tg, *sch, nprop, dry, warps, stream); \
-    break;
   switch (E) {
-    HMC_PERSIST_CASE(1)
-    HMC_PERSIST_CASE(2)
-    HMC_PERSIST_CASE(3)
-    default:
-      HMC_PERSIST_CASE(4)
+    case 1: rc = launch_single<T, 1>(st, tg, *sch, nprop, dry, warps, stream); break;
+    case 2: rc = launch_single<T, 2>(st, tg, *sch, nprop, dry, warps, stream); break;
+    case 3: rc = launch_single<T, 3>(st, tg, *sch, nprop, dry, warps, stream); break;
+    default: rc = launch_single<T, 4>(st, tg, *sch, nprop, dry, warps, stream); break;
   }
-#undef HMC_PERSIST_CASE
   HMC_TRY(rc);
   if (dry) return HMC_OK;
   advance_counter_kernel<<<1, 1, 0, stream>>>(s->proposal, nprop);
   return check_launch("advance_counter_kernel");
+}
+
+template <typename T, int E>
+int launch_groups(const GroupTable<T>& tab, int blocks, size_t smem, const hmc_schedule& sch, int64_t nprop, int dry,
+                  int warps, cudaStream_t stream) {
+  auto kern = persistent_groups_kernel<T, E>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(persistent_groups_kernel)");
+  }
+  kern<<<(unsigned)blocks, 32 * warps, smem, stream>>>(tab, sch, nprop, dry);
+  return check_launch("persistent_groups_kernel");
+}
+
+template <typename T>
+int groups_impl(const hmc_dense_group* groups, int ngroups, const hmc_schedule* sch, int64_t nprop, int warps,
+                int dry, cudaStream_t stream) {
+  const char* who = "hmc_persistent_dense_groups";
+  HMC_TRY(check_common(who, sch, nprop, warps));
+  HMC_REQUIRE(groups && ngroups >= 1 && ngroups <= MAX_GROUPS, "%s: 1..%d groups", who, MAX_GROUPS);
+  GroupTable<T> tab;
+  tab.n = ngroups;
+  const int mk = groups[0].chains ? groups[0].chains->mass_kind : -1;
+  const int prior = groups[0].prior;
+  int64_t blocks = 0;
+  int dmax = 0;
+  size_t smem = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    const hmc_dense_group& G = groups[g];
+    HMC_REQUIRE(G.chains && G.chains->dtype == groups[0].chains->dtype, "%s: group %d has another dtype", who, g);
+    HMC_REQUIRE(G.chains->mass_kind == mk && G.prior == prior, "%s: group %d differs in mass or prior kind", who, g);
+    HMC_TRY(fill_target<T>(who, G.chains, G.GtG, G.Gtd0, G.dtd, G.prior, G.prior_mean, G.prior_w, nprop, warps,
+                           tab.s[g], tab.tg[g]));
+    tab.block0[g] = (int)blocks;
+    blocks += (G.chains->chains + warps - 1) / warps;
+    dmax = tab.tg[g].d > dmax ? tab.tg[g].d : dmax;
+    const size_t sm = persistent_smem<T>(tab.tg[g].d, mk, warps);
+    smem = sm > smem ? sm : smem;
+  }
+  HMC_REQUIRE(blocks <= 0x7FFFFFFF, "%s: too many blocks", who);
+  if (nprop == 0) return HMC_OK;
+  const int E = (dmax + 31) / 32;
+  int rc;
+  switch (E) {
+    case 1: rc = launch_groups<T, 1>(tab, (int)blocks, smem, *sch, nprop, dry, warps, stream); break;
+    case 2: rc = launch_groups<T, 2>(tab, (int)blocks, smem, *sch, nprop, dry, warps, stream); break;
+    case 3: rc = launch_groups<T, 3>(tab, (int)blocks, smem, *sch, nprop, dry, warps, stream); break;
+    default: rc = launch_groups<T, 4>(tab, (int)blocks, smem, *sch, nprop, dry, warps, stream); break;
+  }
+  HMC_TRY(rc);
+  if (dry) return HMC_OK;
+  for (int g = 0; g < ngroups; ++g) {
+    advance_counter_kernel<<<1, 1, 0, stream>>>(groups[g].chains->proposal, nprop);
+    HMC_TRY(check_launch("advance_counter_kernel"));
+  }
+  return HMC_OK;
 }
 
 }  // namespace
@@ -411,5 +502,15 @@ extern "C" HMC_API int hmc_persistent_dense(const hmc_chains* s, const void* GtG
   return HMC_DISPATCH(s->dtype, T, [&] {
     return persistent_impl<T>(s, GtG, Gtd0, dtd, prior, prior_mean, prior_w, schedule, proposals, warps_per_block,
                               dry, as_stream(stream));
+  });
+}
+
+extern "C" HMC_API int hmc_persistent_dense_groups(const hmc_dense_group* groups, int ngroups,
+                                                   const hmc_schedule* schedule, int64_t proposals,
+                                                   int warps_per_block, int dry, void* stream) {
+  if (!groups || ngroups < 1 || !groups[0].chains)
+    return fail(HMC_ERR_INVALID_ARG, "hmc_persistent_dense_groups: no groups");
+  return HMC_DISPATCH(groups[0].chains->dtype, T, [&] {
+    return groups_impl<T>(groups, ngroups, schedule, proposals, warps_per_block, dry, as_stream(stream));
   });
 }

@@ -540,6 +540,27 @@ HMC_API int hmc_persistent_dense(const hmc_chains* s, const void* GtG,
                                  int64_t proposals, int warps_per_block,
                                  int dry, void* stream);
 
+/* Several such targets of different dimensions and chain counts in one
+ * launch (one group per target, up to 48 groups; every group has its own
+ * chain state, data, step sizes and random draws).  All groups share the
+ * dtype, the mass kind, the prior kind and the integrator schedule; each
+ * group's proposal counter advances by `proposals`.                        */
+typedef struct hmc_dense_group {
+  const hmc_chains* chains;
+  const void* GtG;
+  const void* Gtd0;
+  double dtd;
+  int prior;
+  const void* prior_mean;
+  const void* prior_w;
+} hmc_dense_group;
+
+HMC_API int hmc_persistent_dense_groups(const hmc_dense_group* groups,
+                                        int ngroups,
+                                        const hmc_schedule* schedule,
+                                        int64_t proposals, int warps_per_block,
+                                        int dry, void* stream);
+
 /* ---- CUDA graphs of whole proposals --------------------------------------
  * Capture the work issued on `stream` between begin and end into an
  * executable graph; launch it any number of times.                          */

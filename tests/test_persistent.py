@@ -98,3 +98,35 @@ def test_persistent_counts_proposals_and_thins():
     assert out[0].shape == (64, 33, 8)
     assert np.max(np.abs(out[0] - out[1])) < 1e-10
     assert not np.allclose(out[0][:, :-1, 0], out[0][:, :-1, -1])
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_targets_of_uneven_dimension_in_one_launch(dtype):
+    """Three posteriors (d = 20, 50, 97; 64, 33 and 128 chains) advanced
+    together, one launch per block of proposals, give the chains each one
+    gives alone."""
+    import hmclab_gb300 as H
+
+    specs = [(20, 64, 1), (50, 33, 2), (97, 128, 3)]
+
+    def prepared(d, C, seed):
+        post, m, eps = _problem(d, "normal", seed=seed)
+        q0 = m + 0.02 * np.random.default_rng(seed).normal(size=(d, C))
+        return H.Samplers.HMC(seed=seed).prepare(None, post, stepsize=eps, amount_of_steps=5, initial_model=q0,
+                                                 proposals=12, chains=C, dtype=dtype, keep_samples=True,
+                                                 proposals_per_graph=6)
+
+    alone = []
+    for d, C, seed in specs:
+        smp = prepared(d, C, seed)
+        smp.run(12)
+        smp.finish()
+        alone.append(smp.samples_numpy())
+    group = [prepared(d, C, seed) for d, C, seed in specs]
+    H.Samplers.run_together(group, 12)
+    for smp, ref in zip(group, alone):
+        smp.finish()
+        assert smp.current_proposal == 11
+        got = smp.samples_numpy()
+        assert got.shape == ref.shape
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
