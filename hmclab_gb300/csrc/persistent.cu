@@ -170,23 +170,43 @@ __device__ __forceinline__ void run_block(const State<T>& s, const Target<T>& tg
   double xc = s.x_cur[c];
   const T eps0 = s.eps[c];
   int64_t n_acc = 0;
+  // which steps drift (the schedule's drift coefficient is nonzero)
+  const unsigned drift_lo = __ballot_sync(0xffffffffu, lane < sch.steps && sch.drift[lane] != 0.0);
+  const unsigned drift_hi = __ballot_sync(0xffffffffu, lane + 32 < sch.steps && sch.drift[lane + 32] != 0.0);
 
   for (int64_t t = 0; t < nprop; ++t) {
     const int64_t n = n0 + t;
-    // step size of this trajectory and the accept uniform
-    double ue = 0.0, ua = 0.0;
-    if (!s.seps || !s.su) philox_scalars(s.seed, (uint32_t)c, (uint64_t)n, &ue, &ua);
-    T e = eps0;
-    if (s.randomize) {
-      const T f = s.seps ? s.seps[(n % s.slen) * s.C + c] : (T)(0.5 + ue);
-      e = (T)((double)f * (double)e);
+    // Scalars of the proposal, each formed once per warp (FP64 issues at a
+    // small fraction of the FP32 rate, so lanes split this work and share
+    // the results by shuffles): the step size and accept uniform in lane 0,
+    // the kick / drift coefficients of step l in lane l % 32.
+    T e = eps0, ce = (T)0;
+    double u = 0.0;
+    if (lane == 0) {
+      double ue = 0.0, ua = 0.0;
+      if (!s.seps || !s.su) philox_scalars(s.seed, (uint32_t)c, (uint64_t)n, &ue, &ua);
+      if (s.randomize) {
+        const T f = s.seps ? s.seps[(n % s.slen) * s.C + c] : (T)(0.5 + ue);
+        e = (T)((double)f * (double)e);
+      }
+      u = s.su ? s.su[(n % s.slen) * s.C + c] : ua;
+      ce = (T)(sch.first_drift * (double)e);
     }
-    const double u = s.su ? s.su[(n % s.slen) * s.C + c] : ua;
+    e = __shfl_sync(0xffffffffu, e, 0);
+    ce = __shfl_sync(0xffffffffu, ce, 0);
+    T ck_lo = (T)0, cd_lo = (T)0, ck_hi = (T)0, cd_hi = (T)0;
+    if (lane < sch.steps) {
+      ck_lo = (T)(sch.kick[lane] * (double)e);
+      cd_lo = (T)(sch.drift[lane] * (double)e);
+    }
+    if (lane + 32 < sch.steps) {
+      ck_hi = (T)(sch.kick[lane + 32] * (double)e);
+      cd_hi = (T)(sch.drift[lane + 32] * (double)e);
+    }
 
     // momenta, K0, first drift
     T p[E], q[E];
     double k0 = 0.0;
-    const T ce = (T)(sch.first_drift * (double)e);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       p[k] = (T)0;
@@ -225,7 +245,7 @@ __device__ __forceinline__ void run_block(const State<T>& s, const Target<T>& tg
         T g[E];
         matvec<T, E>(A, ld, d, qw, lane, g);
         __syncwarp();
-        const T ck = (T)(sch.kick[st] * (double)e);
+        const T ck = __shfl_sync(0xffffffffu, st < 32 ? ck_lo : ck_hi, st & 31);
 #pragma unroll
         for (int k = 0; k < E; ++k) {
           T gk = g[k] - gtd[k];
@@ -234,8 +254,8 @@ __device__ __forceinline__ void run_block(const State<T>& s, const Target<T>& tg
           p[k] -= ck * gk;
         }
       }
-      if (sch.drift[st] != 0.0) {
-        const T cd = (T)(sch.drift[st] * (double)e);
+      if ((st < 32 ? drift_lo : drift_hi) >> (st & 31) & 1u) {
+        const T cd = __shfl_sync(0xffffffffu, st < 32 ? cd_lo : cd_hi, st & 31);
         apply_minv<T, E>(MASS, Mi, ld, d, qw, lane, live, minv, p, mp);
 #pragma unroll
         for (int k = 0; k < E; ++k) q[k] = q[k] + cd * mp[k];
@@ -269,8 +289,9 @@ __device__ __forceinline__ void run_block(const State<T>& s, const Target<T>& tg
     double x1 = lik;
     if (PRIOR == PRIOR_NORMAL) x1 = 0.5 * warp_sum(pri) + lik;
     if (PRIOR == PRIOR_LAPLACE) x1 = warp_sum(pri) + lik;
-    const double alpha = exp((xc + k0) - (x1 + k1));
-    if (alpha > u) {  // strict; NaN compares false
+    int accept = 0;
+    if (lane == 0) accept = exp((xc + k0) - (x1 + k1)) > u ? 1 : 0;  // strict; NaN compares false
+    if (__shfl_sync(0xffffffffu, accept, 0)) {
 #pragma unroll
       for (int k = 0; k < E; ++k) qc[k] = q[k];
       xc = x1;
