@@ -40,7 +40,11 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
 Each proposal is issued as: begin (momentum, K0, first drift) -> for every
 kick: gradient of the target on the device, then kick+drift -> misfit at the
 end point -> accept/record.  All of it runs on one CUDA stream; blocks of
-proposals are captured once and replayed as CUDA graphs.
+proposals are captured once and replayed as CUDA graphs.  Dense FP32 targets
+with d >= 64 fuse the gradient, kick and drift into one tensor-core launch
+per leapfrog step; small dense linear-Gaussian targets (d <= 128) run whole
+blocks of proposals in one persistent launch (`run_together` advances several
+such targets of different dimensions in the same launch).
 """
 import ctypes as _ct
 import os as _os
