@@ -124,6 +124,11 @@ class _AbstractDistribution:
         self._device_gradient(M, out, bool(accumulate), dtype, _dev.stream_handle(stream))
         return out
 
+    def check_device_status(self):
+        """Raise DeviceTimeoutError if one of this target's kernels gave up a
+        bounded wait since the last check (synchronises with the device).
+        Targets whose kernels never wait have nothing to check."""
+
     @_abstractmethod
     def _device_misfit(self, M, out, accumulate, dtype, stream):
         raise _AbstractMethodError()
@@ -393,6 +398,10 @@ class AdditiveDistribution(_AbstractDistribution):
     def _device_gradient(self, M, out, accumulate, dtype, stream):
         for k, dist in enumerate(self.separate_distributions):
             dist._device_gradient(M, out, accumulate or k > 0, dtype, stream)
+
+    def check_device_status(self):
+        for dist in self.separate_distributions:
+            dist.check_device_status()
 
     def collapse_bounds(self):
         for dist in self.separate_distributions:
@@ -670,6 +679,11 @@ class ElasticFullWaveform2D(_AbstractDistribution):
     single_dtype = "float32"
     # each shot is a CUDA graph of its own, replayed from the host
     graph_safe = False
+    # forward stencils read their neighbourhoods from shared-memory tiles
+    # staged by the tensor memory accelerator (chain counts that are a
+    # multiple of 32); False selects the direct-load kernels, which give the
+    # same records.  Set before the first evaluation.
+    staged_tiles: bool = True
 
     def __init__(self, _input, ux_obs=None, uz_obs=None, temperature=None, omp_threads_override=None,
                  free_parameter_grid=None, data_std=1.0, background=None, gradient_projection="chain_rule"):
@@ -760,6 +774,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
                                                  "sxx", "szz", "sxz")}
             ws["rec"] = z(cfg.n_shots * cfg.nt * cfg.n_rec * 2 * C)
             ws["partial"] = torch.zeros(64 * C, dtype=torch.float64, device=device)
+            ws["status"] = torch.zeros(1, dtype=torch.int32, device=device)
             cache[key] = ws
         if with_gradient and "store" not in ws:
             z = lambda *shape: torch.zeros(shape, dtype=torch.float32, device=device)  # noqa: E731
@@ -782,12 +797,14 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         d.taper, d.rec_map, d.obs = p["taper"].data_ptr(), p["rec_map"].data_ptr(), p["obs"].data_ptr()
         d.stf_host = p["stf_host"].ctypes.data
         for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec",
-                     "partial"):
+                     "partial", "status"):
             setattr(d, name, ws[name].data_ptr())
         for name in ("store", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam",
                      "g_muxz", "t1", "t2", "t3", "t4", "t5"):
             if name in ws:
                 setattr(d, name, ws[name].data_ptr())
+        if not self.staged_tiles:
+            d.status = None
         return d
 
     def _set_model(self, M, ws, stream):
@@ -846,6 +863,17 @@ class ElasticFullWaveform2D(_AbstractDistribution):
     def _check_dtype(self, dtype):
         if dtype != "float32":
             raise NotImplementedError("the elastic finite-difference kernels run in FP32 (float32 chains)")
+
+    def check_device_status(self):
+        """The forward stencils stage their tiles through bounded barrier
+        waits; a wait that ran out sets the workspace's status word."""
+        from hmclab_gb300.Helpers.CustomExceptions import DeviceTimeoutError
+
+        for key, ws in self.__dict__.get("_scratch_cache", {}).items():
+            st = ws.get("status") if isinstance(ws, dict) else None
+            if st is not None and int(st.cpu()[0]) != 0:
+                st.zero_()
+                raise DeviceTimeoutError("elastic stencil tile load timed out (bounded wait expired)")
 
     def _device_misfit(self, M, out, accumulate, dtype, stream):
         import ctypes

@@ -634,6 +634,9 @@ class HMC:
             self._graph = None
         if self._fused is not None:
             self._fused.ops.check_status()
+        check = getattr(self.distribution, "check_device_status", None)
+        if check is not None:
+            check()
         self._finalise(self._done)
         return self
 

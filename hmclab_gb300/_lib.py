@@ -103,7 +103,7 @@ class HmcFwi(_ct.Structure):
     ] + [(n, c_void_p) for n in (
         "taper", "stf_host", "rec_map", "rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx",
         "szz", "sxz", "store", "rec", "obs", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz",
-        "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial")]
+        "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial", "status")]
 
 
 HMC_SCHEDULE_MAX = 64

@@ -21,6 +21,11 @@
 // The adjoint runs the transpose of these maps backwards in time
 // ((Dx+)^T = -Dx-, (Dx-)^T = -Dx+, same in z), accumulating gradients with
 // respect to bx, bz, l+2m, l, muxz, which are then mapped to rho, vp, vs.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "common.cuh"
 
 namespace hmc {
@@ -173,6 +178,203 @@ __global__ void __launch_bounds__(TX* TY* TZ) stress_kernel(Grid g, Fields f, Pa
   f.szz[k] = szz * t;
   f.sxz[k] = sxz * t;
 }
+
+// ---- forward step with TMA-staged tiles --------------------------------------
+// A block owns 32 chains x TT_X cells along x x TT_Z rows.  The fields it
+// differentiates are copied into shared memory with their stencil halos by
+// three (velocity) or two (stress) tensor-memory-accelerator loads that
+// complete on one mbarrier; out-of-grid parts of a halo read as zero and are
+// never used (stencils are applied on interior cells only).  The block's own
+// fields and parameters are read directly.  The arithmetic is the same
+// expression for expression as velocity_kernel / stress_kernel.
+constexpr int TT_X = 8, TT_Z = 4;
+constexpr uint64_t TMA_WAIT_NS = 2000000000ull;  // bounded wait: 2 s
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool tile_barrier_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, P;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// One tile load (32 chains x cells x rows) that completes on `bar`.
+__device__ __forceinline__ void tile_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
+          "r"(smem_addr(dst)),
+      "l"((uint64_t)map), "r"(smem_addr(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+// Thread 0 arms the barrier and issues the tile loads; every thread then
+// waits (at most 2 s).  Returns false when the wait expired.
+__device__ __forceinline__ bool tile_wait(uint64_t* bar) {
+  if (tile_barrier_try(bar, 0)) return true;
+  const uint64_t t0 = now_ns();
+  while (!tile_barrier_try(bar, 0))
+    if (now_ns() - t0 > TMA_WAIT_NS) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tile_barrier_arm(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(1u) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+struct TileOrigin {
+  int c0, i0, j0;
+  int tx, lane;
+};
+__device__ __forceinline__ TileOrigin tile_of(const Grid& g) {
+  const int ctiles = (g.C + 31) / 32;
+  const int it = blockIdx.x / ctiles, ct = blockIdx.x - it * ctiles;
+  TileOrigin o;
+  o.c0 = ct * 32;
+  o.i0 = it * TT_X;
+  o.j0 = blockIdx.y * TT_Z;
+  o.tx = threadIdx.y;
+  o.lane = threadIdx.x;
+  return o;
+}
+inline dim3 tile_grid(int nx, int nz, int64_t C) {
+  return dim3((unsigned)(((nx + TT_X - 1) / TT_X) * ((C + 31) / 32)), (unsigned)((nz + TT_Z - 1) / TT_Z));
+}
+
+// staged differences: the same expressions as dxp / dxm on the tile
+#define HMC_DP(a, b, c, d) ((C1 * ((a) - (b)) + C2 * ((c) - (d))) * g.inv_h)
+
+__global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
+    const __grid_constant__ CUtensorMap m_sxx, const __grid_constant__ CUtensorMap m_sxz,
+    const __grid_constant__ CUtensorMap m_szz, Grid g, Fields f, Params p, const float* __restrict__ taper,
+    const int32_t* __restrict__ rec_map, float* rec_n, float* store_n, int* status) {
+  __shared__ __align__(128) float t_sxx[TT_Z][TT_X + 3][32];      // rows j0.., cells i0-1..
+  __shared__ __align__(128) float t_sxz[TT_Z + 3][TT_X + 3][32];  // rows j0-2.., cells i0-2..
+  __shared__ __align__(128) float t_szz[TT_Z + 3][TT_X][32];      // rows j0-1.., cells i0..
+  __shared__ __align__(8) uint64_t bar;
+  step_dependency_wait();
+  step_dependents_go();
+  const TileOrigin o = tile_of(g);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_sxx) + sizeof(t_sxz) + sizeof(t_szz)));
+    tile_load_3d(t_sxx, &m_sxx, &bar, o.c0, o.i0 - 1, o.j0);
+    tile_load_3d(t_sxz, &m_sxz, &bar, o.c0, o.i0 - 2, o.j0 - 2);
+    tile_load_3d(t_szz, &m_szz, &bar, o.c0, o.i0, o.j0 - 1);
+  }
+  __syncthreads();
+  if (!tile_wait(&bar)) {
+    // record the failure, give the copies in flight one more bounded wait
+    // so that none lands in a retired block's shared memory, and leave
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
+    tile_wait(&bar);
+    return;
+  }
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  if (c >= g.C || i >= g.nx) return;
+  const bool xin = i >= 2 && i < g.nx - 2;
+#pragma unroll
+  for (int zz = 0; zz < TT_Z; ++zz) {
+    const int j = o.j0 + zz;
+    if (j >= g.nz) break;
+    const int k = g.at(j, i) + c;
+    float vx = f.vx[k], vz = f.vz[k];
+    if (xin && j >= 2 && j < g.nz - 2) {
+      const float dsxx = HMC_DP(t_sxx[zz][tx + 2][l], t_sxx[zz][tx + 1][l], t_sxx[zz][tx + 3][l], t_sxx[zz][tx][l]);
+      const float dsxz_z =
+          HMC_DP(t_sxz[zz + 2][tx + 2][l], t_sxz[zz + 1][tx + 2][l], t_sxz[zz + 3][tx + 2][l], t_sxz[zz][tx + 2][l]);
+      vx += g.dt * p.bx[k] * (dsxx + dsxz_z);
+      const float dsxz_x =
+          HMC_DP(t_sxz[zz + 2][tx + 2][l], t_sxz[zz + 2][tx + 1][l], t_sxz[zz + 2][tx + 3][l], t_sxz[zz + 2][tx][l]);
+      const float dszz = HMC_DP(t_szz[zz + 2][tx][l], t_szz[zz + 1][tx][l], t_szz[zz + 3][tx][l], t_szz[zz][tx][l]);
+      vz += g.dt * p.bz[k] * (dsxz_x + dszz);
+    }
+    const int cell = j * g.nx + i;
+    const float t = taper[cell];
+    vx *= t;
+    vz *= t;
+    f.vx[k] = vx;
+    f.vz[k] = vz;
+    const int r = rec_map[cell];
+    if (r >= 0) {
+      rec_n[(r * 2 + 0) * g.C + c] = vx;
+      rec_n[(r * 2 + 1) * g.C + c] = vz;
+    }
+    if (store_n) {
+      store_n[k] = vx;
+      store_n[g.nx * g.nz * g.C + k] = vz;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_constant__ CUtensorMap m_vx,
+                                                               const __grid_constant__ CUtensorMap m_vz, Grid g,
+                                                               Fields f, Params p, const float* __restrict__ taper,
+                                                               int src_i, int src_j, float src_value, int* status) {
+  __shared__ __align__(128) float t_vx[TT_Z + 3][TT_X + 3][32];  // rows j0-1.., cells i0-2..
+  __shared__ __align__(128) float t_vz[TT_Z + 3][TT_X + 3][32];  // rows j0-2.., cells i0-1..
+  __shared__ __align__(8) uint64_t bar;
+  step_dependency_wait();
+  step_dependents_go();
+  const TileOrigin o = tile_of(g);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_vx) + sizeof(t_vz)));
+    tile_load_3d(t_vx, &m_vx, &bar, o.c0, o.i0 - 2, o.j0 - 1);
+    tile_load_3d(t_vz, &m_vz, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+  }
+  __syncthreads();
+  if (!tile_wait(&bar)) {
+    // record the failure, give the copies in flight one more bounded wait
+    // so that none lands in a retired block's shared memory, and leave
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
+    tile_wait(&bar);
+    return;
+  }
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  if (c >= g.C || i >= g.nx) return;
+  const bool xin = i >= 2 && i < g.nx - 2;
+#pragma unroll
+  for (int zz = 0; zz < TT_Z; ++zz) {
+    const int j = o.j0 + zz;
+    if (j >= g.nz) break;
+    const int k = g.at(j, i) + c;
+    float sxx = f.sxx[k], szz = f.szz[k], sxz = f.sxz[k];
+    if (xin && j >= 2 && j < g.nz - 2) {
+      const float exx = HMC_DP(t_vx[zz + 1][tx + 2][l], t_vx[zz + 1][tx + 1][l], t_vx[zz + 1][tx + 3][l],
+                               t_vx[zz + 1][tx][l]);
+      const float ezz = HMC_DP(t_vz[zz + 2][tx + 1][l], t_vz[zz + 1][tx + 1][l], t_vz[zz + 3][tx + 1][l],
+                               t_vz[zz][tx + 1][l]);
+      sxx += g.dt * (p.l2m[k] * exx + p.lam[k] * ezz);
+      szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
+      const float dvx = HMC_DP(t_vx[zz + 2][tx + 2][l], t_vx[zz + 1][tx + 2][l], t_vx[zz + 3][tx + 2][l],
+                               t_vx[zz][tx + 2][l]);
+      const float dvz = HMC_DP(t_vz[zz + 2][tx + 2][l], t_vz[zz + 2][tx + 1][l], t_vz[zz + 2][tx + 3][l],
+                               t_vz[zz + 2][tx][l]);
+      sxz += g.dt * p.muxz[k] * (dvx + dvz);
+    }
+    if (i == src_i && j == src_j) {
+      sxx += src_value;
+      szz += src_value;
+    }
+    const float t = taper[j * g.nx + i];
+    f.sxx[k] = sxx * t;
+    f.szz[k] = szz * t;
+    f.sxz[k] = sxz * t;
+  }
+}
+#undef HMC_DP
 
 // ---- adjoint ---------------------------------------------------------------
 struct Grads {
@@ -329,6 +531,36 @@ inline unsigned grid_for(int64_t n) {
   return b > 152u * 64u ? 152u * 64u : b;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tile_encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+// 3-D FP32 map of a [nz][nx][C] field with a box of 32 chains x bx cells x bz
+// rows; out-of-grid elements of a box read as zero.
+int field_map(CUtensorMap* m, const float* base, int nx, int nz, int64_t C, int bx, int bz) {
+  auto fn = tile_encode_fn();
+  if (!fn) return fail(HMC_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  cuuint64_t dims[3] = {(cuuint64_t)C, (cuuint64_t)nx, (cuuint64_t)nz};
+  cuuint64_t strides[2] = {(cuuint64_t)C * 4, (cuuint64_t)nx * C * 4};
+  cuuint32_t box[3] = {32u, (cuuint32_t)bx, (cuuint32_t)bz};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HMC_ERR_INVALID_ARG, "cuTensorMapEncodeTiled(field) failed (%d)", (int)r);
+  return HMC_OK;
+}
+
 }  // namespace fwi
 }  // namespace hmc
 
@@ -384,6 +616,31 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
   const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block = cell_block();
   const float src_scale = s->dt / (s->h * s->h);
   float* rec_shot = s->rec + (int64_t)shot * s->nt * s->nrec * 2 * s->chains;
+  // tiles staged by the tensor memory accelerator: whole 32-chain tiles and
+  // 16-byte row pitches (C a multiple of 32), and a status word for the
+  // bounded barrier wait
+  if (s->chains % 32 == 0 && s->status) {
+    CUtensorMap m_sxx, m_sxz, m_szz, m_vx, m_vz;
+    HMC_TRY(field_map(&m_sxx, s->sxx, s->nx, s->nz, s->chains, TT_X + 3, TT_Z));
+    HMC_TRY(field_map(&m_sxz, s->sxz, s->nx, s->nz, s->chains, TT_X + 3, TT_Z + 3));
+    HMC_TRY(field_map(&m_szz, s->szz, s->nx, s->nz, s->chains, TT_X, TT_Z + 3));
+    HMC_TRY(field_map(&m_vx, s->vx, s->nx, s->nz, s->chains, TT_X + 3, TT_Z + 3));
+    HMC_TRY(field_map(&m_vz, s->vz, s->nx, s->nz, s->chains, TT_X + 3, TT_Z + 3));
+    const dim3 tgrid = tile_grid(s->nx, s->nz, s->chains), tblock(32, TT_X);
+    for (int n = 0; n < s->nt; ++n) {
+      float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
+      float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
+      cudaError_t e = launch_step(n > 0, velocity_tma_kernel, tgrid, tblock, st, m_sxx, m_sxz, m_szz, g, f, p,
+                                  s->taper, s->rec_map, rec_n, store_n, s->status);
+      if (e != cudaSuccess) return cuda_fail(e, "launch velocity_tma_kernel");
+      HMC_TRY(check_launch("velocity_tma_kernel"));
+      e = launch_step(true, stress_tma_kernel, tgrid, tblock, st, m_vx, m_vz, g, f, p, s->taper, src_x, src_z,
+                      s->stf_host[n] * src_scale, s->status);
+      if (e != cudaSuccess) return cuda_fail(e, "launch stress_tma_kernel");
+      HMC_TRY(check_launch("stress_tma_kernel"));
+    }
+    return HMC_OK;
+  }
   // the source wavelet is read on the host: it is a handful of floats per step
   for (int n = 0; n < s->nt; ++n) {
     float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;

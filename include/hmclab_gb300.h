@@ -452,6 +452,8 @@ typedef struct hmc_fwi {
   float* t4;
   float* t5;
   double* partial;          /* [64][C] misfit partial sums (work)           */
+  int* status;              /* set to 1 when a tile load timed out (nullable:
+                               then the stencils read without staged tiles) */
 } hmc_fwi;
 
 /* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */
