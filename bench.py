@@ -350,9 +350,10 @@ class SrclocWorkload:
 # converts that cost into min-ESS/s with it.
 FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.241
 # DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
-# capture of velocity_kernel (59.1 + 0.4 MB) and stress_kernel (67.6 + 1.6 MB)
-# on a cold cache; in the time loop the fields stay in L2 and DRAM moves less
-FWI_STEP_DRAM_BYTES = 128.7e6
+# capture of velocity_tma_kernel (59.7 + 0.4 MB) and stress_tma_kernel
+# (67.8 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
+# DRAM moves less
+FWI_STEP_DRAM_BYTES = 129.1e6
 
 
 class FwiWorkload:
@@ -910,7 +911,7 @@ def run_fwi_arm(args, wl):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(q_start.size * 8 / K),
                 "d2h_bytes_per_step": int(d * C * 4 + C * 8), "seconds": t_e2e},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "fwi forward time step: velocity_kernel + stress_kernel (the exact misfit)",
+        "roofline": {"kernel": "fwi forward time step: velocity_tma_kernel + stress_tma_kernel (the exact misfit)",
                      "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": FWI_STEP_DRAM_BYTES, "traffic_source": "ncu capture of one velocity + one stress "
                      "launch at C = 64, default (cold) cache control", "peak_source": src, "step_s": t_step,
