@@ -274,6 +274,25 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
     tile_load_3d(t_sxz, &m_sxz, &bar, o.c0, o.i0 - 2, o.j0 - 2);
     tile_load_3d(t_szz, &m_szz, &bar, o.c0, o.i0, o.j0 - 1);
   }
+  // the block's own cells do not depend on the tiles: their loads are in
+  // flight while the tensor copies land
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  const bool active = c < g.C && i < g.nx;
+  float r_vx[TT_Z], r_vz[TT_Z], r_bx[TT_Z], r_bz[TT_Z], r_tp[TT_Z];
+  int r_rec[TT_Z];
+#pragma unroll
+  for (int zz = 0; zz < TT_Z; ++zz) {
+    const int j = o.j0 + zz;
+    if (active && j < g.nz) {
+      const int k = g.at(j, i) + c, cell = j * g.nx + i;
+      r_vx[zz] = f.vx[k];
+      r_vz[zz] = f.vz[k];
+      r_bx[zz] = p.bx[k];
+      r_bz[zz] = p.bz[k];
+      r_tp[zz] = taper[cell];
+      r_rec[zz] = rec_map[cell];
+    }
+  }
   __syncthreads();
   if (!tile_wait(&bar)) {
     // record the failure, give the copies in flight one more bounded wait
@@ -282,32 +301,30 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
     tile_wait(&bar);
     return;
   }
-  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
-  if (c >= g.C || i >= g.nx) return;
+  if (!active) return;
   const bool xin = i >= 2 && i < g.nx - 2;
 #pragma unroll
   for (int zz = 0; zz < TT_Z; ++zz) {
     const int j = o.j0 + zz;
     if (j >= g.nz) break;
     const int k = g.at(j, i) + c;
-    float vx = f.vx[k], vz = f.vz[k];
+    float vx = r_vx[zz], vz = r_vz[zz];
     if (xin && j >= 2 && j < g.nz - 2) {
       const float dsxx = HMC_DP(t_sxx[zz][tx + 2][l], t_sxx[zz][tx + 1][l], t_sxx[zz][tx + 3][l], t_sxx[zz][tx][l]);
       const float dsxz_z =
           HMC_DP(t_sxz[zz + 2][tx + 2][l], t_sxz[zz + 1][tx + 2][l], t_sxz[zz + 3][tx + 2][l], t_sxz[zz][tx + 2][l]);
-      vx += g.dt * p.bx[k] * (dsxx + dsxz_z);
+      vx += g.dt * r_bx[zz] * (dsxx + dsxz_z);
       const float dsxz_x =
           HMC_DP(t_sxz[zz + 2][tx + 2][l], t_sxz[zz + 2][tx + 1][l], t_sxz[zz + 2][tx + 3][l], t_sxz[zz + 2][tx][l]);
       const float dszz = HMC_DP(t_szz[zz + 2][tx][l], t_szz[zz + 1][tx][l], t_szz[zz + 3][tx][l], t_szz[zz][tx][l]);
-      vz += g.dt * p.bz[k] * (dsxz_x + dszz);
+      vz += g.dt * r_bz[zz] * (dsxz_x + dszz);
     }
-    const int cell = j * g.nx + i;
-    const float t = taper[cell];
+    const float t = r_tp[zz];
     vx *= t;
     vz *= t;
     f.vx[k] = vx;
     f.vz[k] = vz;
-    const int r = rec_map[cell];
+    const int r = r_rec[zz];
     if (r >= 0) {
       rec_n[(r * 2 + 0) * g.C + c] = vx;
       rec_n[(r * 2 + 1) * g.C + c] = vz;
@@ -334,6 +351,23 @@ __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_cons
     tile_load_3d(t_vx, &m_vx, &bar, o.c0, o.i0 - 2, o.j0 - 1);
     tile_load_3d(t_vz, &m_vz, &bar, o.c0, o.i0 - 1, o.j0 - 2);
   }
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  const bool active = c < g.C && i < g.nx;
+  float r_sxx[TT_Z], r_szz[TT_Z], r_sxz[TT_Z], r_l2m[TT_Z], r_lam[TT_Z], r_mu[TT_Z], r_tp[TT_Z];
+#pragma unroll
+  for (int zz = 0; zz < TT_Z; ++zz) {
+    const int j = o.j0 + zz;
+    if (active && j < g.nz) {
+      const int k = g.at(j, i) + c;
+      r_sxx[zz] = f.sxx[k];
+      r_szz[zz] = f.szz[k];
+      r_sxz[zz] = f.sxz[k];
+      r_l2m[zz] = p.l2m[k];
+      r_lam[zz] = p.lam[k];
+      r_mu[zz] = p.muxz[k];
+      r_tp[zz] = taper[j * g.nx + i];
+    }
+  }
   __syncthreads();
   if (!tile_wait(&bar)) {
     // record the failure, give the copies in flight one more bounded wait
@@ -342,33 +376,32 @@ __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_cons
     tile_wait(&bar);
     return;
   }
-  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
-  if (c >= g.C || i >= g.nx) return;
+  if (!active) return;
   const bool xin = i >= 2 && i < g.nx - 2;
 #pragma unroll
   for (int zz = 0; zz < TT_Z; ++zz) {
     const int j = o.j0 + zz;
     if (j >= g.nz) break;
     const int k = g.at(j, i) + c;
-    float sxx = f.sxx[k], szz = f.szz[k], sxz = f.sxz[k];
+    float sxx = r_sxx[zz], szz = r_szz[zz], sxz = r_sxz[zz];
     if (xin && j >= 2 && j < g.nz - 2) {
       const float exx = HMC_DP(t_vx[zz + 1][tx + 2][l], t_vx[zz + 1][tx + 1][l], t_vx[zz + 1][tx + 3][l],
                                t_vx[zz + 1][tx][l]);
       const float ezz = HMC_DP(t_vz[zz + 2][tx + 1][l], t_vz[zz + 1][tx + 1][l], t_vz[zz + 3][tx + 1][l],
                                t_vz[zz][tx + 1][l]);
-      sxx += g.dt * (p.l2m[k] * exx + p.lam[k] * ezz);
-      szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
+      sxx += g.dt * (r_l2m[zz] * exx + r_lam[zz] * ezz);
+      szz += g.dt * (r_lam[zz] * exx + r_l2m[zz] * ezz);
       const float dvx = HMC_DP(t_vx[zz + 2][tx + 2][l], t_vx[zz + 1][tx + 2][l], t_vx[zz + 3][tx + 2][l],
                                t_vx[zz][tx + 2][l]);
       const float dvz = HMC_DP(t_vz[zz + 2][tx + 2][l], t_vz[zz + 2][tx + 1][l], t_vz[zz + 2][tx + 3][l],
                                t_vz[zz + 2][tx][l]);
-      sxz += g.dt * p.muxz[k] * (dvx + dvz);
+      sxz += g.dt * r_mu[zz] * (dvx + dvz);
     }
     if (i == src_i && j == src_j) {
       sxx += src_value;
       szz += src_value;
     }
-    const float t = taper[j * g.nx + i];
+    const float t = r_tp[zz];
     f.sxx[k] = sxx * t;
     f.szz[k] = szz * t;
     f.sxz[k] = sxz * t;
@@ -402,34 +435,41 @@ __global__ void __launch_bounds__(TX* TY* TZ) adj_velocity_kernel(Grid g, Fields
   if (!e.in || !g.valid(e.i, e.j)) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C, plane = g.nx * g.nz * g.C;
   const float ih = g.inv_h;
-  // (Dx+)^T = -Dx-, etc.: -Dx+ t1 - Dz- t3 and -Dz+ t2 - Dx- t3
-  float ax = a.vx[k] - dxp(tm.t1, k, sx, ih) - dxm(tm.t3, k, sz, ih);
-  float az = a.vz[k] - dxp(tm.t2, k, sz, ih) - dxm(tm.t3, k, sx, ih);
+  const int cell = e.j * g.nx + e.i;
+  // every load first: the stores below may alias them as far as the
+  // compiler knows, and would otherwise hold later loads back
   const float* vxn = vn;
   const float* vzn = vn + plane;
+  const float avx = a.vx[k], avz = a.vz[k];
+  const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
+  const float g_l2m = gr.l2m[k], g_lam = gr.lam[k], g_mu = gr.muxz[k], g_bx = gr.bx[k], g_bz = gr.bz[k];
+  const float bx = p.bx[k], bz = p.bz[k];
+  const float tp = taper[cell];
+  const int r = rec_map[cell];
+  const float vxk = vxn[k], vzk = vzn[k];
+  const float vxp = vprev ? vprev[k] : 0.f, vzp = vprev ? vprev[plane + k] : 0.f;
+  // (Dx+)^T = -Dx-, etc.: -Dx+ t1 - Dz- t3 and -Dz+ t2 - Dx- t3
+  float ax = avx - dxp(tm.t1, k, sx, ih) - dxm(tm.t3, k, sz, ih);
+  float az = avz - dxp(tm.t2, k, sz, ih) - dxm(tm.t3, k, sx, ih);
   const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
   const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
-  const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
-  gr.l2m[k] += g.dt * (exx * asxx + ezz * aszz);
-  gr.lam[k] += g.dt * (ezz * asxx + exx * aszz);
-  gr.muxz[k] += g.dt * exz * asxz;
-  const int cell = e.j * g.nx + e.i;
-  const int r = rec_map[cell];
   if (r >= 0) {
     ax += resid_n[(r * 2 + 0) * g.C + e.c];
     az += resid_n[(r * 2 + 1) * g.C + e.c];
   }
-  const float tp = taper[cell];
   ax *= tp;
   az *= tp;
+  gr.l2m[k] = g_l2m + g.dt * (exx * asxx + ezz * aszz);
+  gr.lam[k] = g_lam + g.dt * (ezz * asxx + exx * aszz);
+  gr.muxz[k] = g_mu + g.dt * exz * asxz;
   a.vx[k] = ax;
   a.vz[k] = az;
-  const float dvx = vxn[k] / tp - (vprev ? vprev[k] : 0.f);
-  const float dvz = vzn[k] / tp - (vprev ? vprev[plane + k] : 0.f);
-  gr.bx[k] += dvx / p.bx[k] * ax;
-  gr.bz[k] += dvz / p.bz[k] * az;
-  tm.t4[k] = g.dt * p.bx[k] * ax;
-  tm.t5[k] = g.dt * p.bz[k] * az;
+  const float dvx = vxk / tp - vxp;
+  const float dvz = vzk / tp - vzp;
+  gr.bx[k] = g_bx + dvx / bx * ax;
+  gr.bz[k] = g_bz + dvz / bz * az;
+  tm.t4[k] = g.dt * bx * ax;
+  tm.t5[k] = g.dt * bz * az;
 }
 
 // Adjoint stress pass of step n (reverse of velocity step 1), then the taper
@@ -443,15 +483,16 @@ __global__ void __launch_bounds__(TX* TY* TZ) adj_stress_kernel(Grid g, Fields a
   const int k = e.k, sx = g.C, sz = g.nx * g.C;
   const float ih = g.inv_h;
   const float tp = taper[e.j * g.nx + e.i];
+  const float l2m = p.l2m[k], lam = p.lam[k], mu = p.muxz[k];
   const float asxx = (a.sxx[k] - dxm(tm.t4, k, sx, ih)) * tp;
   const float asxz = (a.sxz[k] - dxp(tm.t4, k, sz, ih) - dxp(tm.t5, k, sx, ih)) * tp;
   const float aszz = (a.szz[k] - dxm(tm.t5, k, sz, ih)) * tp;
   a.sxx[k] = asxx;
   a.sxz[k] = asxz;
   a.szz[k] = aszz;
-  tm.t1[k] = g.dt * (p.l2m[k] * asxx + p.lam[k] * aszz);
-  tm.t2[k] = g.dt * (p.lam[k] * asxx + p.l2m[k] * aszz);
-  tm.t3[k] = g.dt * p.muxz[k] * asxz;
+  tm.t1[k] = g.dt * (l2m * asxx + lam * aszz);
+  tm.t2[k] = g.dt * (lam * asxx + l2m * aszz);
+  tm.t3[k] = g.dt * mu * asxz;
 }
 
 // Weighted residuals w (rec - obs) of one shot, all steps: [nt][nrec][2][C];
