@@ -187,7 +187,16 @@ __global__ void __launch_bounds__(TX* TY* TZ) stress_kernel(Grid g, Fields f, Pa
 // never used (stencils are applied on interior cells only).  The block's own
 // fields and parameters are read directly.  The arithmetic is the same
 // expression for expression as velocity_kernel / stress_kernel.
-constexpr int TT_X = 8, TT_Z = 4;
+// Tile shape (overridable at build time): 8 x 4 measured fastest at 240 x 140
+// cells x 64 chains against 8 x 2, 8 x 8, 16 x 2 and 16 x 4 (117 ms per
+// 4-shot misfit against 120-128 ms).
+#ifndef HMC_FWI_TILE_X
+#define HMC_FWI_TILE_X 8
+#endif
+#ifndef HMC_FWI_TILE_Z
+#define HMC_FWI_TILE_Z 4
+#endif
+constexpr int TT_X = HMC_FWI_TILE_X, TT_Z = HMC_FWI_TILE_Z;
 constexpr uint64_t TMA_WAIT_NS = 2000000000ull;  // bounded wait: 2 s
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
