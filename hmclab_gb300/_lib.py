@@ -218,6 +218,7 @@ SIGNATURES = {
     "hmc_ess": [I, I64, I64, I64, P, I, P, P, P, S],
     "hmc_ess_work_size": [I64, I64, I],
     "hmc_moments": [I, I64, I64, I64, P, P, P, S],
+    "hmc_rank_normalize": [I, I64, I64, I64, P, P, S],
     "hmc_graph_begin": [S],
     "hmc_graph_end": [S, _ct.POINTER(c_void_p)],
     "hmc_graph_launch": [P, S],

@@ -221,3 +221,74 @@ extern "C" HMC_API int64_t hmc_ess_work_size(int64_t d, int64_t C, int lags) {
   const int64_t nblk = (2 * C + ESS_CH - 1) / ESS_CH;
   return d * nblk * (lags + 2) + d * nblk;
 }
+
+// ---- rank normalisation (Vehtari, Gelman, Simpson, Carpenter & Buerkner
+// 2021, "Rank-normalization, folding, and localization: an improved R-hat",
+// section 4.1): every draw of a parameter is replaced by the normal score of
+// its rank among all N x C draws of that parameter,
+//   z = Phi^-1((r - 3/8) / (S + 1/4)),  S = N C,
+// with tied draws given their average rank.  The split-R-hat and ESS of z are
+// the bulk diagnostics of that paper.
+namespace hmc {
+namespace {
+constexpr int RANK_TILE = 2048;
+
+// One thread per draw, blockIdx.y = parameter: the draw is compared with all
+// S draws of its parameter, staged through shared memory in tiles.
+template <typename T>
+__global__ void __launch_bounds__(256) rank_normal_kernel(const T* __restrict__ x, int64_t N, int64_t d, int64_t C,
+                                                          int64_t i0, double* __restrict__ z) {
+  __shared__ double tile[RANK_TILE];
+  const int64_t S = N * C;
+  const int64_t i = i0 + blockIdx.y;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool own = s < S;
+  const double v = own ? (double)x[((s / C) * d + i) * C + s % C] : 0.0;
+  int less = 0, equal = 0;
+  for (int64_t t0 = 0; t0 < S; t0 += RANK_TILE) {
+    const int m = (int)(S - t0 < RANK_TILE ? S - t0 : RANK_TILE);
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+      const int64_t u = t0 + q;
+      tile[q] = (double)x[((u / C) * d + i) * C + u % C];
+    }
+    __syncthreads();
+    if (own) {
+#pragma unroll 8
+      for (int q = 0; q < m; ++q) {
+        less += tile[q] < v;
+        equal += tile[q] == v;
+      }
+    }
+  }
+  if (own) {
+    const double r = (double)less + 0.5 * (double)(equal + 1);
+    z[((s / C) * d + i) * C + s % C] = normcdfinv((r - 0.375) / ((double)S + 0.25));
+  }
+}
+}  // namespace
+}  // namespace hmc
+
+extern "C" HMC_API int hmc_rank_normalize(int dtype, int64_t N, int64_t d, int64_t C, const void* samples, double* z,
+                                          void* stream) {
+  HMC_REQUIRE(N > 0 && d > 0 && C > 0, "hmc_rank_normalize: bad sizes");
+  HMC_REQUIRE(samples && z, "hmc_rank_normalize: null argument");
+  const int64_t S = N * C;
+  HMC_REQUIRE(S < (1ll << 31) / 2, "hmc_rank_normalize: too many draws per parameter");
+  // the comparison count is S^2 per parameter: refuse calls that would keep
+  // the device busy for more than tens of seconds
+  HMC_REQUIRE((double)S * (double)S * (double)d <= 1.1e12,
+              "hmc_rank_normalize: S^2 d = %.3g comparisons is beyond this estimator's budget (1.1e12)",
+              (double)S * (double)S * (double)d);
+  cudaStream_t st = as_stream(stream);
+  const unsigned bx = (unsigned)((S + 255) / 256);
+  for (int64_t i0 = 0; i0 < d; i0 += 65535) {
+    const unsigned dy = (unsigned)(d - i0 < 65535 ? d - i0 : 65535);
+    const int rc = HMC_DISPATCH(dtype, T, [&] {
+      rank_normal_kernel<T><<<dim3(bx, dy), 256, 0, st>>>((const T*)samples, N, d, C, i0, z);
+      return check_launch("rank_normal_kernel");
+    });
+    if (rc != HMC_OK) return rc;
+  }
+  return HMC_OK;
+}

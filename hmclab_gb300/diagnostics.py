@@ -1,7 +1,10 @@
 """Mixing diagnostics computed on the device from the sampler's sample ring.
 
 `ess(samples)`: split-chain multi-chain effective sample size per parameter
-(Gelman et al., BDA3 section 11.5, Geyer's initial monotone sequence);
+(Gelman et al., BDA3 section 11.5, Geyer's initial monotone sequence), with
+`rank_normalize=True` the rank-normalised bulk-ESS and split-R-hat of
+Vehtari et al. (2021, section 4.1), which do not change under monotone
+transformations of a parameter and stay finite for heavy-tailed draws;
 `moments(samples)`: per-parameter mean and standard deviation over all draws
 and chains; `moment_error(...)`: max over parameters of |mean - ref| / ref_std
 and |std - ref_std| / ref_std.  Samples are device tensors [N][d][C].
@@ -12,12 +15,28 @@ from hmclab_gb300 import _device as _dev
 from hmclab_gb300 import _lib
 
 
-def ess(samples, lags=None, stream=None, return_rhat=False):
+def rank_normalize(samples, stream=None):
+    """Normal scores of the pooled ranks of every parameter's draws (FP64
+    device tensor of the samples' shape [N][d][C])."""
+    N, d, C = samples.shape
+    z = _dev.empty((N, d, C), "float64", samples.device)
+    _lib.call("hmc_rank_normalize", _dev.dtype_code(_dev.normalise_dtype(samples.dtype)), N, d, C,
+              samples.data_ptr(), z.data_ptr(), _dev.stream_handle(stream))
+    return z
+
+
+_rank_normalize = rank_normalize  # the name ess() can reach under its keyword of the same name
+
+
+def ess(samples, lags=None, stream=None, return_rhat=False, rank_normalize=False):
     """ESS of every parameter (numpy float64 array of length d).
 
     Entries whose autocorrelation window `lags` was too short to truncate are
     returned as the (negative, flagged) value computed on that window; callers
-    wanting a lower bound take abs()."""
+    wanting a lower bound take abs().  `rank_normalize=True` computes both
+    on the normal scores of the pooled ranks (bulk-ESS, rank split-R-hat)."""
+    if rank_normalize:
+        samples = _rank_normalize(samples, stream)
     N, d, C = samples.shape
     n = N // 2
     if lags is None:

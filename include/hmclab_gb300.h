@@ -502,6 +502,13 @@ HMC_API int hmc_ess(int dtype, int64_t N, int64_t d, int64_t C,
                     const void* samples, int lags, double* work, double* ess,
                     double* rhat, void* stream);
 HMC_API int64_t hmc_ess_work_size(int64_t d, int64_t C, int lags);
+/* Rank normalisation (Vehtari et al. 2021, section 4.1): z[N][d][C] (FP64)
+ * receives, for every draw, Phi^-1((r - 3/8) / (S + 1/4)) with r its rank
+ * (ties averaged) among the S = N C draws of its parameter.  The split-R-hat
+ * and ESS of z (hmc_ess) are the rank-normalised bulk diagnostics.  Cost
+ * S^2 comparisons per parameter; calls with S^2 d > 1.1e12 are refused.    */
+HMC_API int hmc_rank_normalize(int dtype, int64_t N, int64_t d, int64_t C,
+                               const void* samples, double* z, void* stream);
 /* Mean and (population) variance over all draws and chains of every
  * parameter of an [N][d][C] sample array, in FP64.                          */
 HMC_API int hmc_moments(int dtype, int64_t N, int64_t d, int64_t C,

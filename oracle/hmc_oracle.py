@@ -512,6 +512,24 @@ def ess_split(x, lags):
     return out, np.sqrt(varp / W)
 
 
+def rank_normalize(x):
+    """Normal scores of pooled ranks per parameter (Vehtari, Gelman, Simpson,
+    Carpenter & Buerkner 2021, section 4.1): x [N][d][C] -> z of the same
+    shape, z = Phi^-1((r - 3/8) / (S + 1/4)) with r the average rank of a draw
+    among the S = N C draws of its parameter.  (No counterpart in the
+    reference, whose only mixing diagnostic is Helpers/Processing.py:6-13.)"""
+    from scipy.special import ndtri
+    from scipy.stats import rankdata
+
+    N, d, C = x.shape
+    S = N * C
+    z = np.empty((N, d, C))
+    for i in range(d):
+        r = rankdata(x[:, i, :].reshape(-1), method="average")
+        z[:, i, :] = ndtri((r - 0.375) / (S + 0.25)).reshape(N, C)
+    return z
+
+
 def ar1_ess(phi, n_total):
     """Asymptotic ESS of a stationary AR(1) chain: N (1 - phi) / (1 + phi)."""
     return n_total * (1 - phi) / (1 + phi)

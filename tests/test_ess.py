@@ -67,3 +67,53 @@ def test_device_ess_of_one_long_chain_matches_oracle():
     e = diagnostics.ess(t, lags=300)
     e_ref, _ = O.ess_split(t.double().cpu().numpy(), 300)
     np.testing.assert_allclose(e, e_ref, rtol=1e-6)
+
+
+def test_oracle_rank_normalised_ess():
+    """Rank-normalised bulk-ESS: close to the plain estimate for Gaussian
+    AR(1) chains, unchanged by a monotone transformation of the draws, and
+    finite for heavy-tailed draws whose variance does not exist."""
+    phi = [0.0, 0.5, 0.8]
+    x = ar1(400, 3, 64, phi, seed=5)
+    e_plain, _ = O.ess_split(x, 100)
+    e_rank, rh = O.ess_split(O.rank_normalize(x), 100)
+    np.testing.assert_allclose(np.abs(e_rank), np.abs(e_plain), rtol=0.1)
+    assert np.all(np.abs(rh - 1) < 0.06)
+    e_mono, _ = O.ess_split(O.rank_normalize(np.exp(3 * x) + x**3), 100)
+    np.testing.assert_array_equal(e_mono, e_rank)
+    # Cauchy draws: independent, so the bulk-ESS is close to N C
+    rng = np.random.default_rng(6)
+    c = rng.standard_cauchy(size=(400, 2, 64))
+    e_c, _ = O.ess_split(O.rank_normalize(c), 100)
+    assert np.all(np.abs(e_c) > 0.8 * 400 * 64)
+    # ties get their average rank: a constant parameter maps to z = 0
+    z = O.rank_normalize(np.ones((10, 1, 4)))
+    np.testing.assert_allclose(z, 0.0, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_device_rank_normalisation_matches_oracle():
+    """Normal scores and rank-normalised ESS / split-R-hat of the device
+    against the oracle (FP64 and FP32 draws, with ties), and the invariance
+    of the device estimate under a monotone transformation."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from hmclab_gb300 import diagnostics
+
+    x = ar1(300, 4, 96, [0.0, 0.3, 0.6, 0.9], seed=7)
+    x[:, 3] = np.round(x[:, 3] * 4) / 4  # many ties
+    for dtype in (torch.float64, torch.float32):
+        t = torch.from_numpy(x).to("cuda", dtype)
+        xr = t.double().cpu().numpy()
+        z = diagnostics.rank_normalize(t).cpu().numpy()
+        z_ref = O.rank_normalize(xr)
+        np.testing.assert_allclose(z, z_ref, rtol=0, atol=1e-12)
+        e, rh = diagnostics.ess(t, lags=80, return_rhat=True, rank_normalize=True)
+        e_ref, rh_ref = O.ess_split(z_ref, 80)
+        np.testing.assert_allclose(e, e_ref, rtol=1e-9)
+        np.testing.assert_allclose(rh, rh_ref, rtol=1e-9)
+    t = torch.from_numpy(x).to("cuda", torch.float64)
+    e1 = diagnostics.ess(t, lags=80, rank_normalize=True)
+    e2 = diagnostics.ess(torch.exp(2 * t) + t, lags=80, rank_normalize=True)
+    np.testing.assert_array_equal(e1, e2)
