@@ -350,10 +350,10 @@ class SrclocWorkload:
 # converts that cost into min-ESS/s with it.
 FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.241
 # DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
-# capture of velocity_tma_kernel (59.7 + 0.4 MB) and stress_tma_kernel
-# (67.8 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
+# capture of velocity_tma_kernel (60.5 + 0.4 MB) and stress_tma_kernel
+# (69.0 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
 # DRAM moves less
-FWI_STEP_DRAM_BYTES = 129.1e6
+FWI_STEP_DRAM_BYTES = 131.0e6
 
 
 class FwiWorkload:
