@@ -156,6 +156,7 @@ class HmcMlpOut(_ct.Structure):
 
 
 HMC_MLP_HIDDEN, HMC_MLP_OUT, HMC_MLP_BACK, HMC_MLP_WGRAD = 0, 1, 2, 3
+HMC_POT_DELTA2, HMC_POT_DELTA1, HMC_POT_DBAR1, HMC_POT_DBAR2, HMC_POT_ZBAR1 = 0, 1, 2, 3, 4
 
 P = c_void_p
 I = c_int
@@ -209,6 +210,10 @@ SIGNATURES = {
     "hmc_mlp_adam": [I64, P, P, P, P, _ct.c_float, _ct.c_float, _ct.c_float, _ct.c_float, I64, S],
     "hmc_mlp_cast": [I64, I64, P, P, I64, P, I64, S],
     "hmc_mlp_record": [I64, I64, P, P, I64, S],
+    "hmc_pot_elementwise": [I, I64, I64, P, I64, P, I64, P, I64, P, P, I64, P, I64, P, I64, S],
+    "hmc_pot_w3_grad": [I64, I64, P, I64, P, I64, P, S],
+    "hmc_pot_loss": [I64, I64, P, I64, P, I64, P, P, I64, P, I64, P, S],
+    "hmc_pot_scaled_cast": [I64, I64, P, I64, I, P, P, I64, I64, S],
     "hmc_fwi_prepare": [P, S],
     "hmc_fwi_forward_shot": [P, I, I, I, I, S],
     "hmc_fwi_misfit": [P, I, P, I, S],

@@ -3,6 +3,7 @@
     python -m hmclab_gb300.profile_cases fwi-gradient [--nt 100] [--chains 64] [--repeat 2]
     python -m hmclab_gb300.profile_cases fwi-misfit   [--nt 100] [--chains 64] [--repeat 2]
     python -m hmclab_gb300.profile_cases mlp          [--chains 64] [--repeat 3]
+    python -m hmclab_gb300.profile_cases potential    [--chains 64] [--repeat 3]
     python -m hmclab_gb300.profile_cases persistent   [--chains 4096] [--repeat 2]
     python -m hmclab_gb300.profile_cases tomo         [--chains 1024] [--repeat 2]
     python -m hmclab_gb300.profile_cases srcloc       [--chains 8192] [--repeat 2]
@@ -12,7 +13,9 @@ Each case builds the workload's full spatial grid (200x100 cells plus the
 record (`--nt` time steps) so that a profiler capture of every launch of one
 gradient stays small, runs the evaluation `--repeat` times on the current
 stream and synchronises.  `mlp` runs the surrogate's training step (batch
-256) and its sampler-side prediction for 600 parameters.  `persistent` runs
+256) and its sampler-side prediction for 600 parameters; `potential` the same
+for the scalar-potential surrogate (gradient pass and double
+backpropagation).  `persistent` runs
 blocks of 10 proposals of a d = 50 dense linear-Gaussian posterior (FP32,
 10 leapfrog steps) through the persistent kernel; `tomo` and `srcloc` evaluate
 the gradient of the tomography (64 x 64 cells, 2000 rays) and source-location
@@ -40,7 +43,7 @@ def main(argv=None):
     import torch
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["fwi-gradient", "fwi-misfit", "mlp", "persistent", "tomo", "srcloc"])
+    ap.add_argument("case", choices=["fwi-gradient", "fwi-misfit", "mlp", "potential", "persistent", "tomo", "srcloc"])
     ap.add_argument("--nt", type=int, default=100)
     ap.add_argument("--chains", type=int, default=64)
     ap.add_argument("--repeat", type=int, default=2)
@@ -104,7 +107,8 @@ def main(argv=None):
         from hmclab_gb300 import surrogate as S
 
         d = 600
-        net = S.MLPSurrogate(d, hidden=(512, 512), seed=0)
+        kind = S.PotentialSurrogate if a.case == "potential" else S.MLPSurrogate
+        net = kind(d, hidden=(512, 512), seed=0)
         data = S.TrainingSet(d, 4096)
         rng = np.random.default_rng(0)
         st = torch.cuda.current_stream().cuda_stream
@@ -122,7 +126,7 @@ def main(argv=None):
             net.predict_into(q, g, st)
         torch.cuda.synchronize()
         net.check_status()
-        print(f"mlp: d={d} hidden=512x512 batch=256 chains={a.chains} repeat={a.repeat} ok")
+        print(f"{a.case}: d={d} hidden=512x512 batch=256 chains={a.chains} repeat={a.repeat} ok")
 
 
 if __name__ == "__main__":

@@ -54,7 +54,101 @@ class TrainingSet:
         return True
 
 
-class MLPSurrogate:
+class _Surrogate:
+    """Training loop, validation and status checks shared by the surrogates.
+    Subclasses provide fit_normalization, train_step, predict_into, _cast,
+    _snapshot / _restore (copies of the trainable FP32 parameters) and the
+    `status` word of their contractions."""
+
+    frozen = False
+
+    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
+        """Fit the network with Adam on the first `rows` pairs of data (all by
+        default); returns the loss history (host)."""
+        rng = _np.random.default_rng(seed)
+        n = data.count if rows is None else min(int(rows), data.count)
+        assert n >= batch, "not enough training pairs"
+        history = []
+        for s in range(steps):
+            rate = lr * (0.5 * (1 + _np.cos(_np.pi * s / steps)) if lr_decay else 1.0)
+            idx = rng.integers(0, n, size=batch)
+            loss = self.train_step(data, idx, lr=float(rate), stream=stream)
+            if s % 50 == 0 or s == steps - 1:
+                history.append((s, float(loss[0].item())))
+        self.check_status()
+        return history
+
+    def fit(self, data: TrainingSet, steps=3000, batch=256, lr=1e-3, holdout_fraction=0.1, check_every=200,
+            seed=0, stream=None):
+        """Train with early stopping: a random `holdout_fraction` of the stored
+        pairs is held out, and every `check_every` steps its relative error
+        is measured; the weights with the lowest one are kept.  Returns a
+        dict with the loss history, the held-out errors (step 0 is the
+        least-squares linear start) and the best step."""
+        import torch
+
+        n = data.count
+        rng = _np.random.default_rng(seed)
+        perm = rng.permutation(n)
+        n_hold = max(1, int(round(holdout_fraction * n)))
+        held = torch.from_numpy(_np.sort(perm[:n_hold])).to(self.device)
+        train_rows = _np.sort(perm[n_hold:])
+        assert len(train_rows) >= batch, "not enough training pairs"
+        self.fit_normalization(data, rows=train_rows)
+        err0 = self.relative_error(data, held, stream=stream)
+        best = (err0, 0, self._snapshot())
+        errors = [(0, err0)]
+        history = []
+        done = 0
+        while done < steps:
+            chunk = min(check_every, steps - done)
+            for s in range(chunk):
+                k = done + s
+                rate = lr * 0.5 * (1 + _np.cos(_np.pi * k / steps))
+                idx = train_rows[rng.integers(0, len(train_rows), size=batch)]
+                loss = self.train_step(data, idx, lr=float(rate), stream=stream)
+                if k % 50 == 0:
+                    history.append((k, float(loss[0].item())))
+            done += chunk
+            e = self.relative_error(data, held, stream=stream)
+            errors.append((done, e))
+            if e < best[0]:
+                best = (e, done, self._snapshot())
+        self.check_status()
+        self._restore(best[2])
+        self._cast(_dev.stream_handle(stream))
+        torch.cuda.synchronize(self.device)
+        return {"history": history, "heldout": errors, "best_step": best[1], "best_heldout": best[0],
+                "train_pairs": len(train_rows), "heldout_pairs": n_hold}
+
+    def freeze(self):
+        self.frozen = True
+        return self
+
+    def relative_error(self, data: TrainingSet, rows, stop=None, stream=None):
+        """|f(q) - g| / |g| (Frobenius norms) over stored pairs of data: the
+        rows [rows, stop) when `stop` is given, else the index tensor `rows`.
+        The held-out error when those pairs were not trained on."""
+        import torch
+
+        sel = slice(rows, stop) if stop is not None else rows
+        q = data.q[sel].t().contiguous()
+        g = data.g[sel].t().contiguous()
+        out = torch.empty_like(g)
+        self.predict_into(q, out, _dev.stream_handle(stream))
+        torch.cuda.synchronize(self.device)
+        return float(torch.linalg.norm((out - g).double()) / torch.linalg.norm(g.double()))
+
+    def check_status(self):
+        from hmclab_gb300.Helpers.CustomExceptions import DeviceTimeoutError
+
+        s = int(self.status.cpu()[0])
+        if s:
+            self.status.zero_()
+            raise DeviceTimeoutError(f"surrogate contraction reported status {s}")
+
+
+class MLPSurrogate(_Surrogate):
     def __init__(self, dimensions, hidden=(512, 512), seed=0, device=None):
         import torch
 
@@ -241,71 +335,6 @@ class MLPSurrogate:
         _lib.call("hmc_tc_mlp", _lib.HMC_MLP_WGRAD, n_in, n_out, B, act_t.data_ptr(), ld_act_t, delta_t.data_ptr(),
                   delta_t.shape[1], None, ctypes.byref(o), self.status.data_ptr(), stream)
 
-    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
-        """Fit the network with Adam on the first `rows` pairs of data (all by
-        default); returns the loss history (host)."""
-        rng = _np.random.default_rng(seed)
-        n = data.count if rows is None else min(int(rows), data.count)
-        assert n >= batch, "not enough training pairs"
-        history = []
-        for s in range(steps):
-            rate = lr * (0.5 * (1 + _np.cos(_np.pi * s / steps)) if lr_decay else 1.0)
-            idx = rng.integers(0, n, size=batch)
-            loss = self.train_step(data, idx, lr=float(rate), stream=stream)
-            if s % 50 == 0 or s == steps - 1:
-                history.append((s, float(loss[0].item())))
-        self.check_status()
-        return history
-
-    def fit(self, data: TrainingSet, steps=3000, batch=256, lr=1e-3, holdout_fraction=0.1, check_every=200,
-            seed=0, stream=None):
-        """Train with early stopping: a random `holdout_fraction` of the stored
-        pairs is held out, and every `check_every` steps its relative error
-        is measured; the weights with the lowest one are kept.  Returns a
-        dict with the loss history, the held-out errors (step 0 is the
-        least-squares linear start) and the best step."""
-        import torch
-
-        n = data.count
-        rng = _np.random.default_rng(seed)
-        perm = rng.permutation(n)
-        n_hold = max(1, int(round(holdout_fraction * n)))
-        held = torch.from_numpy(_np.sort(perm[:n_hold])).to(self.device)
-        train_rows = _np.sort(perm[n_hold:])
-        assert len(train_rows) >= batch, "not enough training pairs"
-        self.fit_normalization(data, rows=train_rows)
-        err0 = self.relative_error(data, held, stream=stream)
-        best = (err0, 0, [w.clone() for w in self.W], [b.clone() for b in self.b])
-        errors = [(0, err0)]
-        history = []
-        done = 0
-        while done < steps:
-            chunk = min(check_every, steps - done)
-            for s in range(chunk):
-                k = done + s
-                rate = lr * 0.5 * (1 + _np.cos(_np.pi * k / steps))
-                idx = train_rows[rng.integers(0, len(train_rows), size=batch)]
-                loss = self.train_step(data, idx, lr=float(rate), stream=stream)
-                if k % 50 == 0:
-                    history.append((k, float(loss[0].item())))
-            done += chunk
-            e = self.relative_error(data, held, stream=stream)
-            errors.append((done, e))
-            if e < best[0]:
-                best = (e, done, [w.clone() for w in self.W], [b.clone() for b in self.b])
-        self.check_status()
-        for l in range(3):
-            self.W[l].copy_(best[2][l])
-            self.b[l].copy_(best[3][l])
-        self._cast(_dev.stream_handle(stream))
-        torch.cuda.synchronize(self.device)
-        return {"history": history, "heldout": errors, "best_step": best[1], "best_heldout": best[0],
-                "train_pairs": len(train_rows), "heldout_pairs": n_hold}
-
-    def freeze(self):
-        self.frozen = True
-        return self
-
     # ---- inference for the sampler -----------------------------------------
     def predict_into(self, q, g, stream):
         """g [d][C] = surrogate gradient at the chain positions q [d][C]."""
@@ -315,24 +344,278 @@ class MLPSurrogate:
                   b["X"].data_ptr(), b["A2"].shape[1], stream)
         self._forward(b, C, stream, g_state=g)
 
-    def relative_error(self, data: TrainingSet, rows, stop=None, stream=None):
-        """|f(q) - g| / |g| (Frobenius norms) over stored pairs of data: the
-        rows [rows, stop) when `stop` is given, else the index tensor `rows`.
-        The held-out error when those pairs were not trained on."""
+    def _snapshot(self):
+        return [w.clone() for w in self.W] + [b.clone() for b in self.b]
+
+    def _restore(self, snap):
+        for l in range(3):
+            self.W[l].copy_(snap[l])
+            self.b[l].copy_(snap[3 + l])
+
+
+
+class PotentialSurrogate(_Surrogate):
+    """Scalar-potential surrogate: f(x) = w3 . GELU(W2 GELU(W1 x + b1) + b2)
+    + x^T A x / 2 + beta . x of x = (q - mu_q) / s_q, with the leapfrog driven
+    by grad_q f = grad_x f / s_q.
+
+    A network that outputs a gradient directly defines a force field with a
+    curl: along a trajectory it pumps energy in or out, and the acceptance of
+    the exact test decays with the trajectory length.  The gradient of a
+    scalar is curl-free, so the surrogate dynamics conserve the surrogate
+    Hamiltonian up to the integrator's error, and only the potential's own
+    error enters the acceptance.  A and beta are the symmetrised ridge fit of
+    the training gradients (the quadratic part of U); the network learns the
+    rest by matching its gradient to the exact gradients
+    (loss 0.5 mean |(grad_q f - g) / sigma_g|^2), which the project's kernels
+    differentiate with respect to the weights by double backpropagation
+    (csrc/potential.cu).  Same interface as MLPSurrogate."""
+
+    def __init__(self, dimensions, hidden=(512, 512), seed=0, device=None):
         import torch
 
-        sel = slice(rows, stop) if stop is not None else rows
-        q = data.q[sel].t().contiguous()
-        g = data.g[sel].t().contiguous()
-        out = torch.empty_like(g)
-        self.predict_into(q, out, _dev.stream_handle(stream))
+        self.device = device or _dev.require_cuda()
+        d, h1, h2 = int(dimensions), int(hidden[0]), int(hidden[1])
+        assert h1 % 16 == 0 and h2 % 16 == 0, "hidden widths must be multiples of 16"
+        self.d = d
+        self.sizes = [d, h1, h2]
+        self.kg = h1 + d  # the output contraction reads [delta1 | x]
+        rng = _np.random.default_rng(seed)
+        f32 = dict(dtype=torch.float32, device=self.device)
+        bf = dict(dtype=torch.bfloat16, device=self.device)
+
+        def uniform(bound, shape):
+            return torch.from_numpy(rng.uniform(-bound, bound, size=shape)).to(**f32).contiguous()
+
+        # uniform +-1/sqrt(fan_in); the output weights 10x smaller, so training
+        # starts from the quadratic fit
+        self.params = {
+            "W1": uniform(d**-0.5, (h1, d)), "b1": uniform(d**-0.5, (h1,)),
+            "W2": uniform(h1**-0.5, (h2, h1)), "b2": uniform(h1**-0.5, (h2,)),
+            "w3": uniform(0.1 * h2**-0.5, (h2,)),
+        }
+        self.grads = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.m1 = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.m2 = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.A = torch.zeros((d, d), **f32)
+        self.beta = torch.zeros(d, **f32)
+        self.mu_q = torch.zeros(d, **f32)
+        self.inv_q = torch.ones(d, **f32)
+        self.mu_g = torch.zeros(d, **f32)
+        self.sig_g = torch.ones(d, **f32)
+        self.inv_g = torch.ones(d, **f32)
+        self.scale = torch.ones(d, **f32)  # 1 / (s_q sigma_g): grad_x f -> normalised gradient
+        self.bias_out = torch.zeros(d, **f32)  # scale * beta - mu_g / sigma_g
+        self.zero_h1 = torch.zeros(h1, **f32)
+        self.zero_h2 = torch.zeros(h2, **f32)
+        self.W1_16 = torch.zeros((h1, _pad(d)), **bf)
+        self.W1t_16 = torch.zeros((d, _pad(h1)), **bf)
+        self.W2_16 = torch.zeros((h2, _pad(h1)), **bf)
+        self.W2t_16 = torch.zeros((h1, _pad(h2)), **bf)
+        self.Wg = torch.zeros((d, _pad(self.kg)), **bf)  # [scale W1^T | scale A]
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.loss_buf = torch.zeros(1025, dtype=torch.float64, device=self.device)
+        self.steps = 0
+        self._bufs = {}
+        h = _dev.stream_handle()
+        self._cast(h)
+        self._cast_quadratic(h)
+        self.frozen = False
+
+    # ---- buffers and weights -------------------------------------------------
+    def _buffers(self, B, training):
+        import torch
+
+        key = (int(B), bool(training))
+        if key in self._bufs:
+            return self._bufs[key]
+        bf, f32 = torch.bfloat16, torch.float32
+        d, h1, h2 = self.sizes
+        pB = _pad(B)
+        z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=self.device)  # noqa: E731
+        Ag = z((B, _pad(self.kg)), bf)
+        b = {
+            "Ag": Ag, "X": Ag[:, h1:],
+            "Z1": z((B, h1), f32), "A1": z((B, _pad(h1)), bf), "A1t": z((h1, pB), bf),
+            "Z2": z((B, h2), f32), "A2": z((B, _pad(h2)), bf), "A2t": z((h2, pB), bf),
+            "D2": z((B, _pad(h2)), bf), "U1": z((B, h1), f32),
+        }
+        if training:
+            b.update({
+                "idx": z((B,), torch.int32), "Xt": z((d, pB), bf), "T": z((B, d), f32), "Y": z((B, d), f32),
+                "D2t": z((h2, pB), bf), "D1t": z((h1, pB), bf),
+                "E": z((B, _pad(d)), bf), "Et": z((d, pB), bf),
+                "DB1": z((B, h1), f32), "UB1": z((B, _pad(h1)), bf), "UB1t": z((h1, pB), bf),
+                "ZB1p": z((B, h1), f32), "DB2": z((B, h2), f32),
+                "ZB2": z((B, _pad(h2)), bf), "ZB2t": z((h2, pB), bf),
+                "AB1": z((B, h1), f32), "ZB1": z((B, _pad(h1)), bf), "ZB1t": z((h1, pB), bf),
+            })
+        self._bufs[key] = b
+        return b
+
+    def _cast(self, stream):
+        d, h1, h2 = self.sizes
+        P = self.params
+        _lib.call("hmc_mlp_cast", h1, d, P["W1"].data_ptr(), self.W1_16.data_ptr(), _pad(d), self.W1t_16.data_ptr(),
+                  _pad(h1), stream)
+        _lib.call("hmc_mlp_cast", h2, h1, P["W2"].data_ptr(), self.W2_16.data_ptr(), _pad(h1),
+                  self.W2t_16.data_ptr(), _pad(h2), stream)
+        _lib.call("hmc_pot_scaled_cast", d, h1, P["W1"].data_ptr(), d, 1, self.scale.data_ptr(), self.Wg.data_ptr(),
+                  self.Wg.shape[1], 0, stream)
+
+    def _cast_quadratic(self, stream):
+        d, h1, _ = self.sizes
+        _lib.call("hmc_pot_scaled_cast", d, d, self.A.data_ptr(), d, 0, self.scale.data_ptr(), self.Wg.data_ptr(),
+                  self.Wg.shape[1], h1, stream)
+
+    def _out(self, **kw):
+        o = _lib.HmcMlpOut()
+        for k, v in kw.items():
+            setattr(o, k, v.data_ptr() if hasattr(v, "data_ptr") else v)
+        return o
+
+    def _mm(self, mode, M, N, K, x, ldx, w, bias, out, stream):
+        import ctypes
+
+        _lib.call("hmc_tc_mlp", mode, M, N, K, x.data_ptr(), ldx, w.data_ptr(), w.shape[1],
+                  bias.data_ptr() if bias is not None else None, ctypes.byref(out), self.status.data_ptr(), stream)
+
+    def _ew(self, mode, B, n, stream, z, out_bf, out_t=None, inp=None, aux=None, vec=None, out_f=None):
+        _lib.call("hmc_pot_elementwise", mode, B, n, _dev.ptr(inp), inp.shape[1] if inp is not None else 0,
+                  z.data_ptr(), z.shape[1], _dev.ptr(aux), aux.shape[1] if aux is not None else 0, _dev.ptr(vec),
+                  out_bf.data_ptr(), out_bf.stride(0), _dev.ptr(out_t), out_t.shape[1] if out_t is not None else 0,
+                  _dev.ptr(out_f), out_f.shape[1] if out_f is not None else 0, stream)
+
+    def _gradient_pass(self, b, B, stream, training, g_state=None):
+        """grad_x f of the rows of b["X"], normalised (y = scale grad_x f +
+        bias_out) into b["Y"], or as grad_q f into g_state [d][B]."""
+        d, h1, h2 = self.sizes
+        P = self.params
+        pB = _pad(B)
+        ldg = b["Ag"].shape[1]
+        o = self._out(z=b["Z1"], ldz=h1, act=b["A1"], ld_act=_pad(h1), act_t=b["A1t"], ld_act_t=pB)
+        self._mm(_lib.HMC_MLP_HIDDEN, B, h1, d, b["X"], ldg, self.W1_16, P["b1"], o, stream)
+        o = self._out(z=b["Z2"], ldz=h2, act=b["A2"], ld_act=_pad(h2), act_t=b["A2t"], ld_act_t=pB)
+        self._mm(_lib.HMC_MLP_HIDDEN, B, h2, h1, b["A1"], _pad(h1), self.W2_16, P["b2"], o, stream)
+        self._ew(_lib.HMC_POT_DELTA2, B, h2, stream, b["Z2"], b["D2"], b.get("D2t") if training else None,
+                 vec=P["w3"])
+        self._mm(_lib.HMC_MLP_OUT, B, h1, h2, b["D2"], _pad(h2), self.W2t_16, self.zero_h1,
+                 self._out(y=b["U1"], ldy=h1), stream)
+        self._ew(_lib.HMC_POT_DELTA1, B, h1, stream, b["Z1"], b["Ag"], b.get("D1t") if training else None,
+                 inp=b["U1"])
+        if g_state is None:
+            o = self._out(y=b["Y"], ldy=d)
+        else:
+            o = self._out(g_state=g_state, out_scale=self.sig_g, out_shift=self.mu_g)
+        self._mm(_lib.HMC_MLP_OUT, B, d, self.kg, b["Ag"], ldg, self.Wg, self.bias_out, o, stream)
+
+    # ---- normalisation and the quadratic part --------------------------------
+    def fit_normalization(self, data: TrainingSet, rows=None):
+        """Per-coordinate scales and the quadratic part A, beta: the ridge
+        least-squares fit grad_x U ~ A x + beta on the stored pairs (or the
+        given rows), symmetrised."""
+        import torch
+
+        n = data.count
+        if rows is None:
+            q = data.q[:n].double()
+            g = data.g[:n].double()
+        else:
+            r = torch.as_tensor(_np.asarray(rows), device=self.device)
+            q = data.q[r].double()
+            g = data.g[r].double()
+            n = len(rows)
+        sq = q.std(dim=0).clamp_min(1e-12)
+        sg = g.std(dim=0).clamp_min(1e-12)
+        self.mu_q.copy_(q.mean(dim=0).float())
+        self.inv_q.copy_((1.0 / sq).float())
+        self.mu_g.copy_(g.mean(dim=0).float())
+        self.sig_g.copy_(sg.float())
+        self.inv_g.copy_((1.0 / sg).float())
+        scale = 1.0 / (sq * sg)
+        self.scale.copy_(scale.float())
+        x = ((q - q.mean(dim=0)) / sq).cpu().numpy()
+        y = (g * sq).cpu().numpy()  # grad_x U
+        x1 = _np.c_[x, _np.ones((n, 1))]
+        reg = 1e-3 * n * _np.eye(self.d + 1)
+        reg[-1, -1] = 0.0
+        sol = _np.linalg.solve(x1.T @ x1 + reg, x1.T @ y)  # y ~ x A^T + beta
+        A = sol[: self.d].T
+        self.A.copy_(torch.from_numpy(0.5 * (A + A.T)).float())
+        self.beta.copy_(torch.from_numpy(sol[self.d]).float())
+        self.bias_out.copy_((scale * self.beta.double() - g.mean(dim=0) / sg).float())
+        h = _dev.stream_handle()
+        self._cast(h)
+        self._cast_quadratic(h)
         torch.cuda.synchronize(self.device)
-        return float(torch.linalg.norm((out - g).double()) / torch.linalg.norm(g.double()))
 
-    def check_status(self):
-        from hmclab_gb300.Helpers.CustomExceptions import DeviceTimeoutError
+    # ---- training --------------------------------------------------------------
+    def train_step(self, data: TrainingSet, idx_host, lr=1e-3, stream=None, beta1=0.9, beta2=0.999, eps=1e-8):
+        """One Adam step of gradient matching on the minibatch rows idx_host;
+        returns the device loss buffer (loss_buf[0])."""
+        import torch
 
-        s = int(self.status.cpu()[0])
-        if s:
-            self.status.zero_()
-            raise DeviceTimeoutError(f"surrogate contraction reported status {s}")
+        assert not self.frozen, "the surrogate is frozen"
+        h = _dev.stream_handle(stream)
+        B = len(idx_host)
+        b = self._buffers(B, True)
+        d, h1, h2 = self.sizes
+        P, G = self.params, self.grads
+        pB = _pad(B)
+        b["idx"].copy_(torch.from_numpy(_np.asarray(idx_host, _np.int32)), non_blocking=False)
+        _lib.call("hmc_mlp_gather", B, d, b["idx"].data_ptr(), data.q.data_ptr(), data.g.data_ptr(),
+                  self.mu_q.data_ptr(), self.inv_q.data_ptr(), self.mu_g.data_ptr(), self.inv_g.data_ptr(),
+                  b["X"].data_ptr(), b["Ag"].shape[1], b["Xt"].data_ptr(), pB, b["T"].data_ptr(), d, h)
+        self._gradient_pass(b, B, h, True)
+        _lib.call("hmc_pot_loss", B, d, b["Y"].data_ptr(), d, b["T"].data_ptr(), d, self.scale.data_ptr(),
+                  b["E"].data_ptr(), _pad(d), b["Et"].data_ptr(), pB, self.loss_buf.data_ptr(), h)
+        # dW1 = delta1^T e; dbar1 = e W1^T -> ubar1, zbar1 (partial)
+        self._wgrad(d, h1, B, b["Et"], b["D1t"], G["W1"], 0, h)
+        self._mm(_lib.HMC_MLP_OUT, B, h1, d, b["E"], _pad(d), self.W1_16, self.zero_h1,
+                 self._out(y=b["DB1"], ldy=h1), h)
+        self._ew(_lib.HMC_POT_DBAR1, B, h1, h, b["Z1"], b["UB1"], b["UB1t"], inp=b["DB1"], aux=b["U1"],
+                 out_f=b["ZB1p"])
+        # dW2 = delta2^T ubar1; dbar2 = ubar1 W2^T -> dw3, zbar2
+        self._wgrad(h1, h2, B, b["UB1t"], b["D2t"], G["W2"], 0, h)
+        self._mm(_lib.HMC_MLP_OUT, B, h2, h1, b["UB1"], _pad(h1), self.W2_16, self.zero_h2,
+                 self._out(y=b["DB2"], ldy=h2), h)
+        _lib.call("hmc_pot_w3_grad", B, h2, b["DB2"].data_ptr(), h2, b["Z2"].data_ptr(), h2, G["w3"].data_ptr(), h)
+        self._ew(_lib.HMC_POT_DBAR2, B, h2, h, b["Z2"], b["ZB2"], b["ZB2t"], inp=b["DB2"], vec=P["w3"])
+        # abar1 = zbar2 W2 -> zbar1; the forward pass's weight and bias gradients
+        self._mm(_lib.HMC_MLP_OUT, B, h1, h2, b["ZB2"], _pad(h2), self.W2t_16, self.zero_h1,
+                 self._out(y=b["AB1"], ldy=h1), h)
+        self._ew(_lib.HMC_POT_ZBAR1, B, h1, h, b["Z1"], b["ZB1"], b["ZB1t"], inp=b["AB1"], aux=b["ZB1p"])
+        self._wgrad(h1, h2, B, b["A1t"], b["ZB2t"], G["W2"], 1, h)
+        _lib.call("hmc_mlp_bias_grad", h2, B, b["ZB2t"].data_ptr(), pB, G["b2"].data_ptr(), h)
+        self._wgrad(d, h1, B, b["Xt"], b["ZB1t"], G["W1"], 1, h)
+        _lib.call("hmc_mlp_bias_grad", h1, B, b["ZB1t"].data_ptr(), pB, G["b1"].data_ptr(), h)
+        self.steps += 1
+        for k in P:
+            _lib.call("hmc_mlp_adam", P[k].numel(), P[k].data_ptr(), G[k].data_ptr(), self.m1[k].data_ptr(),
+                      self.m2[k].data_ptr(), lr, beta1, beta2, eps, self.steps, h)
+        self._cast(h)
+        return self.loss_buf
+
+    def _wgrad(self, n_in, n_out, B, act_t, delta_t, g, accumulate, stream):
+        """g [n_out][n_in] (+)= sum_b delta[b][out] act[b][in] (K = batch)."""
+        import ctypes
+
+        o = self._out(g=g, accumulate=int(accumulate))
+        _lib.call("hmc_tc_mlp", _lib.HMC_MLP_WGRAD, n_in, n_out, B, act_t.data_ptr(), act_t.shape[1],
+                  delta_t.data_ptr(), delta_t.shape[1], None, ctypes.byref(o), self.status.data_ptr(), stream)
+
+    def _snapshot(self):
+        return {k: v.clone() for k, v in self.params.items()}
+
+    def _restore(self, snap):
+        for k, v in snap.items():
+            self.params[k].copy_(v)
+
+    # ---- inference for the sampler ---------------------------------------------
+    def predict_into(self, q, g, stream):
+        """g [d][C] = grad_q f at the chain positions q [d][C]."""
+        C = q.shape[1]
+        b = self._buffers(C, False)
+        _lib.call("hmc_mlp_input", self.d, C, q.data_ptr(), self.mu_q.data_ptr(), self.inv_q.data_ptr(),
+                  b["X"].data_ptr(), b["Ag"].shape[1], stream)
+        self._gradient_pass(b, C, stream, False, g_state=g)

@@ -404,6 +404,47 @@ HMC_API int hmc_mlp_cast(int64_t rows, int64_t cols, const float* w,
 HMC_API int hmc_mlp_record(int64_t d, int64_t C, const float* src, float* dst,
                            int64_t base, void* stream);
 
+/* ---- scalar-potential surrogate (no counterpart in the reference; like the
+ * MLP surrogate it stands in for distribution.gradient in the leapfrog,
+ * Samplers.py:1562,1573).  f(x) = w3 . GELU(W2 GELU(W1 x + b1) + b2)
+ * + x^T A x / 2 + beta . x; the leapfrog uses grad_q f, a conservative field.
+ * Its contractions run through hmc_tc_mlp; these are the element-wise steps
+ * of the gradient pass and of the double backpropagation that trains it.
+ * hmc_pot_elementwise: for every (b < B, j < n), with z [B][ldz]:
+ *   HMC_POT_DELTA2  v = vec[j] GELU'(z)
+ *   HMC_POT_DELTA1  v = in GELU'(z)
+ *   HMC_POT_DBAR1   v = in GELU'(z), and out_f = in aux GELU''(z)
+ *   HMC_POT_DBAR2   v = in vec[j] GELU''(z)
+ *   HMC_POT_ZBAR1   v = aux + in GELU'(z)
+ * v -> out_bf [B][ld_bf] and (nullable) out_t [n][ld_t], both BF16.          */
+#define HMC_POT_DELTA2 0
+#define HMC_POT_DELTA1 1
+#define HMC_POT_DBAR1 2
+#define HMC_POT_DBAR2 3
+#define HMC_POT_ZBAR1 4
+HMC_API int hmc_pot_elementwise(int mode, int64_t B, int64_t n, const float* in,
+                                int64_t ldi, const float* z, int64_t ldz,
+                                const float* aux, int64_t ldaux,
+                                const float* vec, void* out_bf, int64_t ld_bf,
+                                void* out_t, int64_t ld_t, float* out_f,
+                                int64_t ldf, void* stream);
+/* g[j] = sum_b in[b][j] GELU'(z[b][j]) (the gradient of w3).                 */
+HMC_API int hmc_pot_w3_grad(int64_t B, int64_t n, const float* in, int64_t ldi,
+                            const float* z, int64_t ldz, float* g,
+                            void* stream);
+/* Loss 0.5/B sum (y - t)^2 -> loss[0] (loss points to 1025 device doubles,
+ * loss[1..] hold block partials) and e = scale[j] (y - t) / B as BF16
+ * e [B][lde] and e_t [n][ldet].                                             */
+HMC_API int hmc_pot_loss(int64_t B, int64_t n, const float* y, int64_t ldy,
+                         const float* t, int64_t ldt, const float* scale,
+                         void* e, int64_t lde, void* e_t, int64_t ldet,
+                         double* loss, void* stream);
+/* dst[r][k0 + k] = bf16(scale[r] src(r, k)) for r < rows, k < cols, where
+ * src(r, k) = src[k][r] if transposed else src[r][k] (pitch lds).           */
+HMC_API int hmc_pot_scaled_cast(int64_t rows, int64_t cols, const float* src,
+                                int64_t lds, int transposed, const float* scale,
+                                void* dst, int64_t ldd, int64_t k0, void* stream);
+
 /* ---- 2-D elastic P-SV full-waveform misfit and gradient ------------------
  * Replaces psvWave's forward_simulate / calculate_l2_misfit / adjoint_simulate
  * / map_kernels_to_velocity as called by ElasticFullWaveform2D.misfit and

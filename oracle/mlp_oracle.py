@@ -51,3 +51,75 @@ def predict(q, mu_q, inv_q, mu_g, sig_g, W, b):
     _, a2 = hidden(a1, w16[1], b[1])
     y = np.c_[a2, x] @ w16[2].T + b[2]
     return (y * sig_g + mu_g).T
+
+
+# ---- scalar-potential surrogate ---------------------------------------------
+# f(x) = w3 . gelu(W2 gelu(W1 x + b1) + b2) + x^T A x / 2 + beta . x, with the
+# leapfrog driven by grad_q f = grad_x f / s.  Two forms: exact FP64 (for
+# finite-difference checks) and the device's rounding points (BF16 inputs,
+# weights, activations and deltas; FP32-or-wider accumulation).
+
+
+def gelu_grad2(z):
+    return np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi) * (2.0 - z * z)
+
+
+def potential_value(x, W1, b1, W2, b2, w3, A, beta):
+    """f at rows of x [B][d] (FP64, no rounding)."""
+    a2 = gelu(gelu(x @ W1.T + b1) @ W2.T + b2)
+    return a2 @ w3 + 0.5 * np.sum((x @ A) * x, axis=1) + x @ beta
+
+
+def potential_grad(x, W1, b1, W2, b2, w3, A, beta):
+    """grad_x f at rows of x [B][d] (FP64, no rounding)."""
+    z1 = x @ W1.T + b1
+    z2 = gelu(z1) @ W2.T + b2
+    delta2 = w3 * gelu_grad(z2)
+    delta1 = (delta2 @ W2) * gelu_grad(z1)
+    return delta1 @ W1 + x @ A + beta
+
+
+def potential_loss_grads(x, t, scale, shift, W1, b1, W2, b2, w3, A, beta):
+    """Loss 0.5/B sum |y - t|^2 of y = scale * grad_x f + shift and its
+    gradients with respect to W1, b1, W2, b2, w3 (FP64, no rounding), by the
+    double backpropagation the device runs."""
+    B = x.shape[0]
+    z1 = x @ W1.T + b1
+    a1 = gelu(z1)
+    z2 = a1 @ W2.T + b2
+    delta2 = w3 * gelu_grad(z2)
+    u1 = delta2 @ W2
+    delta1 = u1 * gelu_grad(z1)
+    gx = delta1 @ W1 + x @ A + beta
+    y = scale * gx + shift
+    loss = 0.5 * np.sum((y - t) ** 2) / B
+    e = scale * (y - t) / B
+    dbar1 = e @ W1.T
+    ubar1 = dbar1 * gelu_grad(z1)
+    zbar1 = dbar1 * u1 * gelu_grad2(z1)
+    dbar2 = ubar1 @ W2.T
+    gw3 = np.sum(dbar2 * gelu_grad(z2), axis=0)
+    zbar2 = dbar2 * w3 * gelu_grad2(z2)
+    abar1 = zbar2 @ W2
+    zbar1 = zbar1 + abar1 * gelu_grad(z1)
+    gW1 = delta1.T @ e + zbar1.T @ x
+    gW2 = delta2.T @ ubar1 + zbar2.T @ a1
+    return loss, {"W1": gW1, "b1": zbar1.sum(0), "W2": gW2, "b2": zbar2.sum(0), "w3": gw3}
+
+
+def potential_predict(q, mu_q, s_q, mu_g, sig_g, W1, b1, W2, b2, w3, A, beta):
+    """Surrogate gradient grad_q f at positions q [d][C] with the device's
+    rounding points: x, W1, W2 and the scaled output matrix [W1^T | A] / (s
+    sig_g) in BF16, activations and deltas in BF16."""
+    x = bf16(((q.T - mu_q) / s_q).astype(np.float32))
+    D = 1.0 / (s_q * sig_g)
+    w1, w2 = bf16(W1), bf16(W2)
+    z1 = x @ w1.T + b1
+    a1 = bf16(gelu(z1))
+    z2 = a1 @ w2.T + b2
+    delta2 = bf16(w3 * gelu_grad(z2))
+    delta1 = bf16((delta2 @ bf16(W2.T).T) * gelu_grad(z1))
+    wg = bf16(np.c_[(D[:, None] * W1.T), D[:, None] * A])  # [d][h1 + d]
+    bias = D * beta - mu_g / sig_g
+    y = np.c_[delta1, x] @ wg.T + bias
+    return (y * sig_g + mu_g).T
