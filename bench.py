@@ -348,7 +348,7 @@ class SrclocWorkload:
 # bench's GPU arm (the `plain.ess_per_chain_proposal` field of its line); the
 # reference arm, which can only afford to time the CPU cost of a proposal,
 # converts that cost into min-ESS/s with it.
-FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.241
+FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.318
 # DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
 # capture of velocity_tma_kernel (60.5 + 0.4 MB) and stress_tma_kernel
 # (69.0 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and

@@ -75,12 +75,13 @@ __global__ void loss_kernel(int64_t B, int64_t n, const float* __restrict__ y, i
   if (threadIdx.x == 0) loss_partial[blockIdx.x] = sh[0];
 }
 
+// One warp: lane l adds partials l, l + 32, ...; the lanes' sums are combined
+// by a fixed shuffle tree (deterministic).
 __global__ void sum_partials_kernel(int n, const double* __restrict__ p, double scale, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < n; ++k) s += p[k];
-    *out = s * scale;
-  }
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += 32) s += p[k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) *out = s * scale;
 }
 
 // One warp per row: db[r] = sum_c delta_t[r][c].

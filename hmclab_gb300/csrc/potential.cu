@@ -83,15 +83,23 @@ __global__ void elementwise_kernel(int mode, int64_t B, int64_t n, const float* 
   }
 }
 
-// dw3[j] = sum_b dbar2[b][j] GELU'(z2[b][j]): one thread per column, rows in
-// order (deterministic).
+// dw3[j] = sum_b dbar2[b][j] GELU'(z2[b][j]): a block takes 32 columns, its
+// 16 thread rows take every 16th batch row, and the 16 partial sums of a
+// column are added in a fixed order (deterministic).
 __global__ void w3_grad_kernel(int64_t B, int64_t n, const float* __restrict__ in, int64_t ldi,
                                const float* __restrict__ z, int64_t ldz, float* g) {
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (j >= n) return;
+  __shared__ float part[16][33];
+  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
   float s = 0.f;
-  for (int64_t b = 0; b < B; ++b) s += in[b * ldi + j] * gelu_d1(z[b * ldz + j]);
-  g[j] = s;
+  if (j < n)
+    for (int64_t b = threadIdx.y; b < B; b += 16) s += in[b * ldi + j] * gelu_d1(z[b * ldz + j]);
+  part[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && j < n) {
+    float t = 0.f;
+    for (int y = 0; y < 16; ++y) t += part[y][threadIdx.x];
+    g[j] = t;
+  }
 }
 
 // Loss 0.5 sum_b |y_b - t_b|^2 (partials per block) and e = scale * (y - t) / B
@@ -119,12 +127,13 @@ __global__ void loss_kernel(int64_t B, int64_t n, const float* __restrict__ y, i
   if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
+// One warp: lane l adds partials l, l + 32, ...; the lanes' sums are combined
+// by a fixed shuffle tree (deterministic).
 __global__ void sum_kernel(int n, const double* __restrict__ p, double scale, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < n; ++k) s += p[k];
-    *out = s * scale;
-  }
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += 32) s += p[k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) *out = s * scale;
 }
 
 // dst[r][k0 + k] = bf16(scale[r] * src(r, k)) for r < rows, k < cols, with
@@ -196,7 +205,7 @@ HMC_API int hmc_pot_elementwise(int mode, int64_t B, int64_t n, const float* in,
 HMC_API int hmc_pot_w3_grad(int64_t B, int64_t n, const float* in, int64_t ldi, const float* z, int64_t ldz,
                             float* g, void* stream) {
   HMC_REQUIRE(B > 0 && n > 0 && in && z && g && ldi >= n && ldz >= n, "hmc_pot_w3_grad: bad arguments");
-  w3_grad_kernel<<<blocks_for(n, 128), 128, 0, as_stream(stream)>>>(B, n, in, ldi, z, ldz, g);
+  w3_grad_kernel<<<(unsigned)((n + 31) / 32), dim3(32, 16), 0, as_stream(stream)>>>(B, n, in, ldi, z, ldz, g);
   return check_launch("pot w3_grad_kernel");
 }
 
