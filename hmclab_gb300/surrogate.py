@@ -62,16 +62,28 @@ class _Surrogate:
 
     frozen = False
 
+    @staticmethod
+    def _finite_rows(data: TrainingSet, n):
+        """Indices (host) of the first n stored pairs whose position and
+        gradient are finite: trajectories that diverged record non-finite
+        gradients, which must not reach the normalisation or the loss."""
+        import torch
+
+        ok = torch.isfinite(data.q[:n]).all(dim=1) & torch.isfinite(data.g[:n]).all(dim=1)
+        return _np.flatnonzero(ok.cpu().numpy())
+
     def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
         """Fit the network with Adam on the first `rows` pairs of data (all by
-        default); returns the loss history (host)."""
+        default; pairs with non-finite entries are skipped); returns the loss
+        history (host)."""
         rng = _np.random.default_rng(seed)
         n = data.count if rows is None else min(int(rows), data.count)
-        assert n >= batch, "not enough training pairs"
+        usable = self._finite_rows(data, n)
+        assert len(usable) >= batch, "not enough (finite) training pairs"
         history = []
         for s in range(steps):
             rate = lr * (0.5 * (1 + _np.cos(_np.pi * s / steps)) if lr_decay else 1.0)
-            idx = rng.integers(0, n, size=batch)
+            idx = usable[rng.integers(0, len(usable), size=batch)]
             loss = self.train_step(data, idx, lr=float(rate), stream=stream)
             if s % 50 == 0 or s == steps - 1:
                 history.append((s, float(loss[0].item())))
@@ -84,12 +96,14 @@ class _Surrogate:
         pairs is held out, and every `check_every` steps its relative error
         is measured; the weights with the lowest one are kept.  Returns a
         dict with the loss history, the held-out errors (step 0 is the
-        least-squares linear start) and the best step."""
+        least-squares linear start) and the best step.  Pairs with non-finite
+        entries are left out of both sets."""
         import torch
 
-        n = data.count
+        usable = self._finite_rows(data, data.count)
+        n = len(usable)
         rng = _np.random.default_rng(seed)
-        perm = rng.permutation(n)
+        perm = usable[rng.permutation(n)]
         n_hold = max(1, int(round(holdout_fraction * n)))
         held = torch.from_numpy(_np.sort(perm[:n_hold])).to(self.device)
         train_rows = _np.sort(perm[n_hold:])
@@ -119,7 +133,7 @@ class _Surrogate:
         self._cast(_dev.stream_handle(stream))
         torch.cuda.synchronize(self.device)
         return {"history": history, "heldout": errors, "best_step": best[1], "best_heldout": best[0],
-                "train_pairs": len(train_rows), "heldout_pairs": n_hold}
+                "train_pairs": len(train_rows), "heldout_pairs": n_hold, "skipped_pairs": data.count - n}
 
     def freeze(self):
         self.frozen = True

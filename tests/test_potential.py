@@ -200,3 +200,37 @@ def test_potential_surrogate_keeps_the_exact_posterior():
           f"{var_ratio.min():.3f}..{var_ratio.max():.3f}")
     assert z_mean.max() < 5.0
     assert np.all(np.abs(var_ratio - 1.0) < 5.0 * np.sqrt(2.0 / C))
+
+
+@pytest.mark.gpu
+def test_fit_skips_non_finite_pairs():
+    """Pairs recorded from diverged trajectories (non-finite gradient) are
+    left out of the normalisation, the ridge start and the loss."""
+    torch = _torch()
+    from hmclab_gb300 import surrogate as S
+
+    d = 32
+
+    def grad(q):
+        return 2.0 * q + np.sin(q)
+
+    for kind in (S.PotentialSurrogate, S.MLPSurrogate):
+        data = S.TrainingSet(d, 2048)
+        rng = np.random.default_rng(9)
+        for k in range(8):
+            q = rng.normal(size=(d, 256))
+            g = grad(q)
+            if k == 3:
+                g[:, :40] = np.nan
+                g[0, 40:50] = np.inf
+            data.record(torch.from_numpy(q).float().cuda(), torch.from_numpy(g).float().cuda(),
+                        torch.cuda.current_stream().cuda_stream)
+        net = kind(d, hidden=(64, 64), seed=1)
+        fit = net.fit(data, steps=200, batch=128)
+        assert fit["skipped_pairs"] == 50
+        assert np.isfinite(fit["best_heldout"]) and fit["best_heldout"] < fit["heldout"][0][1] + 1e-12
+        qt = torch.from_numpy(rng.normal(size=(d, 64))).float().cuda()
+        out = torch.empty_like(qt)
+        net.freeze().predict_into(qt, out, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert torch.isfinite(out).all()
