@@ -359,7 +359,7 @@ FWI_STEP_DRAM_BYTES = 131.0e6
 class FwiWorkload:
     name = ("elastic P-SV FWI 200x100 cells (+20-cell sponge), h=5 m, dt=0.5 ms, nt=1500, 4 shots x 20 receivers, "
             "25 Hz Ricker, blobs 20x10 x (vp,vs,rho) = 600 params, Normal prior 10%, 64 chains, FP32 stencils, "
-            "MLP 600-512-512-600 surrogate vs plain HMC")
+            "scalar-potential network surrogate 600-512-512-1 vs plain HMC")
     kind = "fwi"
     chains, L = 64, 10
     stepsize = 0.12  # prior-whitened units: the mass matrix is the prior precision
