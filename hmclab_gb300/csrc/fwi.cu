@@ -248,19 +248,19 @@ struct TileOrigin {
   int c0, i0, j0;
   int tx, lane;
 };
-__device__ __forceinline__ TileOrigin tile_of(const Grid& g) {
+__device__ __forceinline__ TileOrigin tile_of(const Grid& g, int rows = TT_Z) {
   const int ctiles = (g.C + 31) / 32;
   const int it = blockIdx.x / ctiles, ct = blockIdx.x - it * ctiles;
   TileOrigin o;
   o.c0 = ct * 32;
   o.i0 = it * TT_X;
-  o.j0 = blockIdx.y * TT_Z;
+  o.j0 = blockIdx.y * rows;
   o.tx = threadIdx.y;
   o.lane = threadIdx.x;
   return o;
 }
-inline dim3 tile_grid(int nx, int nz, int64_t C) {
-  return dim3((unsigned)(((nx + TT_X - 1) / TT_X) * ((C + 31) / 32)), (unsigned)((nz + TT_Z - 1) / TT_Z));
+inline dim3 tile_grid(int nx, int nz, int64_t C, int rows = TT_Z) {
+  return dim3((unsigned)(((nx + TT_X - 1) / TT_X) * ((C + 31) / 32)), (unsigned)((nz + rows - 1) / rows));
 }
 
 // staged differences: the same expressions as dxp / dxm on the tile
@@ -504,6 +504,199 @@ __global__ void __launch_bounds__(TX* TY* TZ) adj_stress_kernel(Grid g, Fields a
   tm.t3[k] = g.dt * mu * asxz;
 }
 
+// ---- adjoint passes with TMA-staged tiles ----------------------------------
+// Same tiling, barrier and bounded wait as the forward pair, R rows per
+// thread, every own-cell operand loaded before the wait; the arithmetic is
+// the same expression for expression as adj_velocity_kernel /
+// adj_stress_kernel.  The stored forward velocities of step n come through
+// one map over all stored planes ([2 nt x nz] rows of nx cells): halo rows
+// that fall into a neighbouring plane are never used, because only interior
+// cells are updated.
+// Rows per thread (overridable at build time): velocity 1 / stress 4 measured
+// fastest at 240 x 140 cells x 64 chains (gradient 454 ms against 455-470 ms
+// for 2 / 4, 2 / 2 and 4 / 4, and 535 ms with direct loads); it is also the
+// variant whose results are bitwise equal to the direct-load kernels.
+#ifndef HMC_FWI_ADJ_ROWS_V
+#define HMC_FWI_ADJ_ROWS_V 1
+#endif
+#ifndef HMC_FWI_ADJ_ROWS_S
+#define HMC_FWI_ADJ_ROWS_S 4
+#endif
+constexpr int AR_V = HMC_FWI_ADJ_ROWS_V, AR_S = HMC_FWI_ADJ_ROWS_S;
+#define HMC_DP(a, b, c, d) ((C1 * ((a) - (b)) + C2 * ((c) - (d))) * g.inv_h)
+
+template <int R>
+__global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
+    const __grid_constant__ CUtensorMap m_t1, const __grid_constant__ CUtensorMap m_t2,
+    const __grid_constant__ CUtensorMap m_t3, const __grid_constant__ CUtensorMap m_store, int row_vx, int row_vz,
+    Grid g, Fields a, Params p, Grads gr, Temps tm, const float* __restrict__ taper,
+    const int32_t* __restrict__ rec_map, const float* __restrict__ resid_n, const float* __restrict__ vprev,
+    int* status) {
+  __shared__ __align__(128) float t_t1[R][TT_X + 3][32];      // rows j0.., cells i0-1..
+  __shared__ __align__(128) float t_t3[R + 3][TT_X + 3][32];  // rows j0-2.., cells i0-2..
+  __shared__ __align__(128) float t_t2[R + 3][TT_X][32];      // rows j0-1.., cells i0..
+  __shared__ __align__(128) float t_vx[R + 3][TT_X + 3][32];  // rows j0-1.., cells i0-2..
+  __shared__ __align__(128) float t_vz[R + 3][TT_X + 3][32];  // rows j0-2.., cells i0-1..
+  __shared__ __align__(8) uint64_t bar;
+  step_dependency_wait();
+  step_dependents_go();
+  const TileOrigin o = tile_of(g, R);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t1) + sizeof(t_t3) + sizeof(t_t2) + sizeof(t_vx) + sizeof(t_vz)));
+    tile_load_3d(t_t1, &m_t1, &bar, o.c0, o.i0 - 1, o.j0);
+    tile_load_3d(t_t3, &m_t3, &bar, o.c0, o.i0 - 2, o.j0 - 2);
+    tile_load_3d(t_t2, &m_t2, &bar, o.c0, o.i0, o.j0 - 1);
+    tile_load_3d(t_vx, &m_store, &bar, o.c0, o.i0 - 2, row_vx + o.j0 - 1);
+    tile_load_3d(t_vz, &m_store, &bar, o.c0, o.i0 - 1, row_vz + o.j0 - 2);
+  }
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  const bool active = c < g.C && i >= 2 && i < g.nx - 2;
+  const int plane = g.nx * g.nz * g.C;
+  float r_avx[R], r_avz[R], r_sxx[R], r_szz[R], r_sxz[R], r_gl2m[R], r_glam[R], r_gmu[R], r_gbx[R], r_gbz[R];
+  float r_bx[R], r_bz[R], r_tp[R], r_vxp[R], r_vzp[R];
+  int r_rec[R];
+#pragma unroll
+  for (int zz = 0; zz < R; ++zz) {
+    const int j = o.j0 + zz;
+    if (active && j >= 2 && j < g.nz - 2) {
+      const int k = g.at(j, i) + c, cell = j * g.nx + i;
+      r_avx[zz] = a.vx[k];
+      r_avz[zz] = a.vz[k];
+      r_sxx[zz] = a.sxx[k];
+      r_szz[zz] = a.szz[k];
+      r_sxz[zz] = a.sxz[k];
+      r_gl2m[zz] = gr.l2m[k];
+      r_glam[zz] = gr.lam[k];
+      r_gmu[zz] = gr.muxz[k];
+      r_gbx[zz] = gr.bx[k];
+      r_gbz[zz] = gr.bz[k];
+      r_bx[zz] = p.bx[k];
+      r_bz[zz] = p.bz[k];
+      r_tp[zz] = taper[cell];
+      r_rec[zz] = rec_map[cell];
+      r_vxp[zz] = vprev ? vprev[k] : 0.f;
+      r_vzp[zz] = vprev ? vprev[plane + k] : 0.f;
+    }
+  }
+  __syncthreads();
+  if (!tile_wait(&bar)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
+    tile_wait(&bar);
+    return;
+  }
+  if (!active) return;
+#pragma unroll
+  for (int zz = 0; zz < R; ++zz) {
+    const int j = o.j0 + zz;
+    if (j < 2 || j >= g.nz - 2) continue;
+    const int k = g.at(j, i) + c;
+    float ax = r_avx[zz] -
+               HMC_DP(t_t1[zz][tx + 2][l], t_t1[zz][tx + 1][l], t_t1[zz][tx + 3][l], t_t1[zz][tx][l]) -
+               HMC_DP(t_t3[zz + 2][tx + 2][l], t_t3[zz + 1][tx + 2][l], t_t3[zz + 3][tx + 2][l], t_t3[zz][tx + 2][l]);
+    float az = r_avz[zz] -
+               HMC_DP(t_t2[zz + 2][tx][l], t_t2[zz + 1][tx][l], t_t2[zz + 3][tx][l], t_t2[zz][tx][l]) -
+               HMC_DP(t_t3[zz + 2][tx + 2][l], t_t3[zz + 2][tx + 1][l], t_t3[zz + 2][tx + 3][l], t_t3[zz + 2][tx][l]);
+    const float exx = HMC_DP(t_vx[zz + 1][tx + 2][l], t_vx[zz + 1][tx + 1][l], t_vx[zz + 1][tx + 3][l],
+                             t_vx[zz + 1][tx][l]);
+    const float ezz = HMC_DP(t_vz[zz + 2][tx + 1][l], t_vz[zz + 1][tx + 1][l], t_vz[zz + 3][tx + 1][l],
+                             t_vz[zz][tx + 1][l]);
+    const float exz = HMC_DP(t_vx[zz + 2][tx + 2][l], t_vx[zz + 1][tx + 2][l], t_vx[zz + 3][tx + 2][l],
+                             t_vx[zz][tx + 2][l]) +
+                      HMC_DP(t_vz[zz + 2][tx + 2][l], t_vz[zz + 2][tx + 1][l], t_vz[zz + 2][tx + 3][l],
+                             t_vz[zz + 2][tx][l]);
+    const int r = r_rec[zz];
+    if (r >= 0) {
+      ax += resid_n[(r * 2 + 0) * g.C + c];
+      az += resid_n[(r * 2 + 1) * g.C + c];
+    }
+    const float tp = r_tp[zz];
+    ax *= tp;
+    az *= tp;
+    const float asxx = r_sxx[zz], aszz = r_szz[zz], asxz = r_sxz[zz];
+    gr.l2m[k] = r_gl2m[zz] + g.dt * (exx * asxx + ezz * aszz);
+    gr.lam[k] = r_glam[zz] + g.dt * (ezz * asxx + exx * aszz);
+    gr.muxz[k] = r_gmu[zz] + g.dt * exz * asxz;
+    a.vx[k] = ax;
+    a.vz[k] = az;
+    const float dvx = t_vx[zz + 1][tx + 2][l] / tp - r_vxp[zz];
+    const float dvz = t_vz[zz + 2][tx + 1][l] / tp - r_vzp[zz];
+    const float bx = r_bx[zz], bz = r_bz[zz];
+    gr.bx[k] = r_gbx[zz] + dvx / bx * ax;
+    gr.bz[k] = r_gbz[zz] + dvz / bz * az;
+    tm.t4[k] = g.dt * bx * ax;
+    tm.t5[k] = g.dt * bz * az;
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(32 * TT_X) adj_stress_tma_kernel(const __grid_constant__ CUtensorMap m_t4,
+                                                                   const __grid_constant__ CUtensorMap m_t5, Grid g,
+                                                                   Fields a, Params p, Temps tm,
+                                                                   const float* __restrict__ taper, int* status) {
+  __shared__ __align__(128) float t_t4[R + 3][TT_X + 3][32];  // rows j0-1.., cells i0-2..
+  __shared__ __align__(128) float t_t5[R + 3][TT_X + 3][32];  // rows j0-2.., cells i0-1..
+  __shared__ __align__(8) uint64_t bar;
+  step_dependency_wait();
+  step_dependents_go();
+  const TileOrigin o = tile_of(g, R);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t4) + sizeof(t_t5)));
+    tile_load_3d(t_t4, &m_t4, &bar, o.c0, o.i0 - 2, o.j0 - 1);
+    tile_load_3d(t_t5, &m_t5, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+  }
+  const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
+  const bool active = c < g.C && i >= 2 && i < g.nx - 2;
+  float r_sxx[R], r_sxz[R], r_szz[R], r_l2m[R], r_lam[R], r_mu[R], r_tp[R];
+#pragma unroll
+  for (int zz = 0; zz < R; ++zz) {
+    const int j = o.j0 + zz;
+    if (active && j >= 2 && j < g.nz - 2) {
+      const int k = g.at(j, i) + c;
+      r_sxx[zz] = a.sxx[k];
+      r_sxz[zz] = a.sxz[k];
+      r_szz[zz] = a.szz[k];
+      r_l2m[zz] = p.l2m[k];
+      r_lam[zz] = p.lam[k];
+      r_mu[zz] = p.muxz[k];
+      r_tp[zz] = taper[j * g.nx + i];
+    }
+  }
+  __syncthreads();
+  if (!tile_wait(&bar)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
+    tile_wait(&bar);
+    return;
+  }
+  if (!active) return;
+#pragma unroll
+  for (int zz = 0; zz < R; ++zz) {
+    const int j = o.j0 + zz;
+    if (j < 2 || j >= g.nz - 2) continue;
+    const int k = g.at(j, i) + c;
+    const float tp = r_tp[zz];
+    const float asxx =
+        (r_sxx[zz] - HMC_DP(t_t4[zz + 1][tx + 2][l], t_t4[zz + 1][tx + 1][l], t_t4[zz + 1][tx + 3][l],
+                            t_t4[zz + 1][tx][l])) *
+        tp;
+    const float asxz =
+        (r_sxz[zz] -
+         HMC_DP(t_t4[zz + 2][tx + 2][l], t_t4[zz + 1][tx + 2][l], t_t4[zz + 3][tx + 2][l], t_t4[zz][tx + 2][l]) -
+         HMC_DP(t_t5[zz + 2][tx + 2][l], t_t5[zz + 2][tx + 1][l], t_t5[zz + 2][tx + 3][l], t_t5[zz + 2][tx][l])) *
+        tp;
+    const float aszz =
+        (r_szz[zz] -
+         HMC_DP(t_t5[zz + 2][tx + 1][l], t_t5[zz + 1][tx + 1][l], t_t5[zz + 3][tx + 1][l], t_t5[zz][tx + 1][l])) *
+        tp;
+    a.sxx[k] = asxx;
+    a.sxz[k] = asxz;
+    a.szz[k] = aszz;
+    tm.t1[k] = g.dt * (r_l2m[zz] * asxx + r_lam[zz] * aszz);
+    tm.t2[k] = g.dt * (r_lam[zz] * asxx + r_l2m[zz] * aszz);
+    tm.t3[k] = g.dt * r_mu[zz] * asxz;
+  }
+}
+#undef HMC_DP
+
 // Weighted residuals w (rec - obs) of one shot, all steps: [nt][nrec][2][C];
 // obs is shared by all chains: [nt][nrec][2].
 __global__ void residual_kernel(int64_t n_rows, int64_t C, const float* __restrict__ rec,
@@ -744,6 +937,34 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
   Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
   Temps tm{s->t1, s->t2, s->t3, s->t4, s->t5};
+  // staged tiles, as in the forward pass (C a multiple of 32, a status word)
+  if (s->chains % 32 == 0 && s->status) {
+    HMC_REQUIRE((int64_t)s->nt * 2 * s->nz < INT32_MAX, "hmc_fwi_adjoint_shot: too many stored rows");
+    CUtensorMap m_t1, m_t2, m_t3, m_t4, m_t5, m_store;
+    HMC_TRY(field_map(&m_t1, s->t1, s->nx, s->nz, s->chains, TT_X + 3, AR_V));
+    HMC_TRY(field_map(&m_t2, s->t2, s->nx, s->nz, s->chains, TT_X, AR_V + 3));
+    HMC_TRY(field_map(&m_t3, s->t3, s->nx, s->nz, s->chains, TT_X + 3, AR_V + 3));
+    HMC_TRY(field_map(&m_store, s->store, s->nx, s->nt * 2 * s->nz, s->chains, TT_X + 3, AR_V + 3));
+    HMC_TRY(field_map(&m_t4, s->t4, s->nx, s->nz, s->chains, TT_X + 3, AR_S + 3));
+    HMC_TRY(field_map(&m_t5, s->t5, s->nx, s->nz, s->chains, TT_X + 3, AR_S + 3));
+    const dim3 gv = tile_grid(s->nx, s->nz, s->chains, AR_V), gs = tile_grid(s->nx, s->nz, s->chains, AR_S);
+    const dim3 tblock(32, TT_X);
+    for (int n = s->nt - 1; n >= 0; --n) {
+      const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
+      // the first launch follows the residual kernel and memsets: ordinary stream order
+      cudaError_t e = launch_step(n < s->nt - 1, adj_velocity_tma_kernel<AR_V>, gv, tblock, st, m_t1, m_t2, m_t3,
+                                  m_store, 2 * n * s->nz, (2 * n + 1) * s->nz, g, a, p, gr, tm, s->taper,
+                                  s->rec_map, (const float*)(s->resid + (int64_t)n * s->nrec * 2 * s->chains), vp,
+                                  s->status);
+      if (e != cudaSuccess) return cuda_fail(e, "launch adj_velocity_tma_kernel");
+      HMC_TRY(check_launch("adj_velocity_tma_kernel"));
+      e = launch_step(true, adj_stress_tma_kernel<AR_S>, gs, tblock, st, m_t4, m_t5, g, a, p, tm, s->taper,
+                      s->status);
+      if (e != cudaSuccess) return cuda_fail(e, "launch adj_stress_tma_kernel");
+      HMC_TRY(check_launch("adj_stress_tma_kernel"));
+    }
+    return HMC_OK;
+  }
   const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block = cell_block();
   for (int n = s->nt - 1; n >= 0; --n) {
     const float* vn = s->store + (int64_t)n * 2 * cells;
