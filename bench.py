@@ -348,7 +348,7 @@ class SrclocWorkload:
 # bench's GPU arm (the `plain.ess_per_chain_proposal` field of its line); the
 # reference arm, which can only afford to time the CPU cost of a proposal,
 # converts that cost into min-ESS/s with it.
-FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.318
+FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.203
 # DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
 # capture of velocity_tma_kernel (60.5 + 0.4 MB) and stress_tma_kernel
 # (69.0 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
@@ -965,7 +965,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
-    ap.add_argument("--plain-steps", type=int, default=10, help="fwi: timed proposals of plain HMC")
+    ap.add_argument("--plain-steps", type=int, default=16, help="fwi: timed proposals of plain HMC")
     ap.add_argument("--train-steps", type=int, default=10000, help="fwi: Adam steps of the surrogate")
     ap.add_argument("--surrogate", default="potential", choices=["potential", "gradient"],
                     help="fwi: scalar-potential network (conservative field) or a network that outputs the gradient")
