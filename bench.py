@@ -1,6 +1,7 @@
 """Benchmark of the batched HMC hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload fwi|dense]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload fwi|dense|tomo|srcloc|cfg1]
 
 A "step" is one HMC proposal (a full leapfrog trajectory plus the accept test)
 for every chain of the workload.  Prints one JSON line.
@@ -8,12 +9,15 @@ for every chain of the workload.  Prints one JSON line.
 Workload `fwi` (default; the metric's configuration): 2-D elastic P-SV
 waveform inversion, 200x100 cells plus a 20-cell sponge, 1500 time steps, 4
 shots, 20 receivers, 600 blob parameters, Normal prior of 10%, 64 chains.
-W exact-gradient burn-in proposals record (position, gradient) pairs; the MLP
-surrogate is trained on them on the device; then K surrogate-driven proposals
-(interior gradients from the network, exact misfit for the accept test) and
---plain-steps plain proposals (exact gradients) are timed from the same
-start.  `value` is the surrogate run's min-ESS/s; `plain` and
-`speedup_vs_plain` give the comparison.
+W exact-gradient burn-in proposals record (position, gradient) pairs; the
+surrogate (--surrogate potential: a scalar network whose gradient is used;
+gradient: a network that outputs the gradient) is trained on them on the
+device; then K surrogate-driven proposals (interior gradients from the
+network, exact misfit for the accept test) and --plain-steps plain proposals
+(exact gradients) are timed from the same start.  `value` is the surrogate
+run's min-ESS/s; `plain` and `speedup_vs_plain` give the comparison, and
+`ess_window_not_truncated` the fraction of parameters whose ESS lag window
+ended before the autocorrelation sum was truncated (an upper estimate).
 
 Workload `dense`: G 2000x1000 with N(0, 1/1000) entries, m_true ~ N(0, I),
 noise sigma 0.05, Normal prior N(0, I), diagonal mass drawn U[0.5, 2], 20
