@@ -20,7 +20,8 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
                 targets whose `graph_safe` is False, e.g. the elastic FWI
                 misfit with its own per-shot graphs, run uncaptured)
   keep_samples  keep every thinned sample on the device (`samples_device`)
-  surrogate     a frozen `surrogate.MLPSurrogate`: it supplies every gradient
+  surrogate     a frozen `surrogate.PotentialSurrogate` or
+                `surrogate.MLPSurrogate`: it supplies every gradient
                 of the leapfrog; the exact misfit at the trajectory end still
                 decides acceptance, so the chain targets the exact posterior
   training_set  a `surrogate.TrainingSet` that receives every exact

@@ -1,7 +1,16 @@
-"""Learned gradient surrogate for HMC: a d-512-512-d GELU MLP with BF16
-weights and activations and FP32 accumulation, trained on the GPU by the
-project's own kernels (tensor-core contractions in csrc/dense_tc.cu, Adam and
-data movement in csrc/mlp.cu).
+"""Learned gradient surrogates for HMC, with BF16 weights and activations and
+FP32 accumulation, trained on the GPU by the project's own kernels
+(tensor-core contractions in csrc/dense_tc.cu; Adam and data movement in
+csrc/mlp.cu; the potential network's element-wise passes in
+csrc/potential.cu):
+
+  PotentialSurrogate  a scalar network f(q) whose gradient drives the
+                      leapfrog (a curl-free field), trained by matching its
+                      gradient to the exact gradients;
+  MLPSurrogate        a d-512-512-d network that outputs the gradient.
+
+The rest of this note describes MLPSurrogate; PotentialSurrogate documents
+its own architecture.
 
 Exactness: the sampler uses the surrogate only for the interior kicks of the
 leapfrog (the `distribution.gradient` calls of Samplers.py:1562,1573 in the

@@ -1,4 +1,5 @@
-"""FP64 numpy oracle of the MLP surrogate's forward, backward and Adam step —
+"""FP64 numpy oracle of the surrogates (the MLP's forward, backward and Adam
+step; the scalar potential's gradient pass and double backpropagation) —
 TEST INFRASTRUCTURE ONLY.  BF16 rounding (round to nearest even on the upper
 16 bits of an IEEE float32) is applied at the same points as the device:
 inputs, weights, activations and backward deltas are BF16, accumulation and
