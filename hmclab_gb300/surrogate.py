@@ -377,6 +377,20 @@ class MLPSurrogate(_Surrogate):
 
 
 
+def quadratic_fit(x, y, ridge=1e-3):
+    """Gradient of the quadratic x^T A x / 2 + beta . x closest to the pairs
+    (x_k, y_k) (rows of x, y): the ridge least-squares affine map
+    y ~ x A^T + beta (penalty ridge * n on A, none on beta), with A then
+    replaced by its symmetric part, the Hessian of a potential.  Host FP64."""
+    n, d = x.shape
+    x1 = _np.c_[x, _np.ones((n, 1))]
+    reg = ridge * n * _np.eye(d + 1)
+    reg[-1, -1] = 0.0
+    sol = _np.linalg.solve(x1.T @ x1 + reg, x1.T @ y)
+    A = sol[:d].T
+    return 0.5 * (A + A.T), sol[d]
+
+
 class PotentialSurrogate(_Surrogate):
     """Scalar-potential surrogate: f(x) = w3 . GELU(W2 GELU(W1 x + b1) + b2)
     + x^T A x / 2 + beta . x of x = (q - mu_q) / s_q, with the leapfrog driven
@@ -559,13 +573,9 @@ class PotentialSurrogate(_Surrogate):
         self.scale.copy_(scale.float())
         x = ((q - q.mean(dim=0)) / sq).cpu().numpy()
         y = (g * sq).cpu().numpy()  # grad_x U
-        x1 = _np.c_[x, _np.ones((n, 1))]
-        reg = 1e-3 * n * _np.eye(self.d + 1)
-        reg[-1, -1] = 0.0
-        sol = _np.linalg.solve(x1.T @ x1 + reg, x1.T @ y)  # y ~ x A^T + beta
-        A = sol[: self.d].T
-        self.A.copy_(torch.from_numpy(0.5 * (A + A.T)).float())
-        self.beta.copy_(torch.from_numpy(sol[self.d]).float())
+        A, beta = quadratic_fit(x, y)
+        self.A.copy_(torch.from_numpy(A).float())
+        self.beta.copy_(torch.from_numpy(beta).float())
         self.bias_out.copy_((scale * self.beta.double() - g.mean(dim=0) / sg).float())
         h = _dev.stream_handle()
         self._cast(h)

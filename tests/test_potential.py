@@ -234,3 +234,24 @@ def test_fit_skips_non_finite_pairs():
         net.freeze().predict_into(qt, out, torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         assert torch.isfinite(out).all()
+
+
+def test_quadratic_fit_recovers_a_quadratic_potential():
+    """The fixed part of the potential surrogate: the symmetrised ridge fit
+    of gradients recovers the Hessian and linear term of a quadratic (host,
+    no device)."""
+    from hmclab_gb300.surrogate import quadratic_fit
+
+    rng = np.random.default_rng(4)
+    d, n = 12, 4000
+    L = rng.normal(size=(d, d))
+    H = L @ L.T / d + np.eye(d)
+    b = rng.normal(size=d)
+    x = rng.normal(size=(n, d))
+    A, beta = quadratic_fit(x, x @ H + b, ridge=1e-9)
+    np.testing.assert_allclose(A, H, atol=1e-6)
+    np.testing.assert_allclose(beta, b, atol=1e-6)
+    # a non-symmetric linear field is projected onto its symmetric part
+    M = rng.normal(size=(d, d))
+    A2, _ = quadratic_fit(x, x @ M.T, ridge=1e-9)
+    np.testing.assert_allclose(A2, 0.5 * (M + M.T), atol=1e-6)
