@@ -40,7 +40,7 @@ extern "C" {
 #define HMC_ERR_CUDA 2        /* CUDA runtime error (launch or execution)    */
 #define HMC_ERR_TIMEOUT 3     /* a bounded device wait ran out               */
 #define HMC_ERR_NONFINITE 4   /* non-finite state where it is not allowed    */
-#define HMC_ERR_UNSUPPORTED 5 /* valid request this build does not provide   */
+#define HMC_ERR_UNSUPPORTED 5 /* valid request the library does not provide */
 
 #define HMC_F32 0
 #define HMC_F64 1
