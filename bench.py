@@ -772,6 +772,16 @@ def forward_step_timing(lik, smp, n_iter=2):
     return ev0.elapsed_time(ev1) / 1e3 / n_iter / (lik.config.n_shots * lik.config.nt)
 
 
+def choose_trajectory(pilot, min_acceptance=0.25):
+    """(L, stepsize) of the pilot entry (gain, L, stepsize, acceptance) with
+    the largest gain among those that accepted at least `min_acceptance` of
+    their proposals (a lower acceptance estimated from a few proposals is too
+    noisy to trust); among all entries when none did."""
+    usable = [x for x in pilot if x[3] >= min_acceptance] or pilot
+    _, L_best, eps_best, _ = max(usable)
+    return L_best, eps_best
+
+
 def run_fwi_arm(args, wl):
     import torch
 
@@ -831,10 +841,7 @@ def run_fwi_arm(args, wl):
                     **dict(kw, amount_of_steps=L_s, stepsize=eps_s))
                 a = float(np.mean(p_smp.accepted_proposals) / 4)
                 pilot.append((a * (L_s * eps_s) ** 2, L_s, eps_s, a))
-        # settings that kept at least a quarter of the pilot proposals: the
-        # estimate of a lower acceptance from 4 proposals is too noisy to trust
-        usable = [x for x in pilot if x[3] >= 0.25] or pilot
-        _, L_best, eps_best, _ = max(usable)
+        L_best, eps_best = choose_trajectory(pilot)
     else:
         L_best, eps_best = args.surrogate_L, args.surrogate_stepsize
 

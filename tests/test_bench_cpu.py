@@ -1,0 +1,55 @@
+"""Host logic of bench.py (no GPU): peaks with and without the measured
+file, the clock record's parsing, the surrogate trajectory choice and the
+FWI workload's algorithmic bytes."""
+import json
+import os
+
+import pytest
+
+import bench
+
+
+def test_peaks_measured_and_fallback(tmp_path, monkeypatch):
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.peaks() == (6800.0, 1900.0, 1700.0, "fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6791.0, "bf16_tflops": 1935.3}))
+    assert bench.peaks() == (6791.0, 1935.3, 1935.3, "measured")
+
+
+class _FakeProc:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_sampler_parses_nvidia_smi_lines():
+    c = bench.ClockSampler(0)
+    c.proc = _FakeProc()
+    c.lines = [
+        "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1000.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    r = c.stop()
+    assert r == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.ClockSampler(0).stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_choose_trajectory():
+    pilot = [(0.8 * 0.24**2, 2, 0.12, 0.8), (0.3 * 0.48**2, 8, 0.06, 0.3), (0.1 * 0.96**2, 8, 0.12, 0.1)]
+    # the last entry has the largest gain but an untrustworthy acceptance
+    assert bench.choose_trajectory(pilot) == (8, 0.06)
+    assert bench.choose_trajectory(pilot, min_acceptance=0.5) == (2, 0.12)
+    assert bench.choose_trajectory([(0.0, 4, 0.03, 0.0), (0.01, 2, 0.06, 0.1)]) == (2, 0.06)
+
+
+def test_fwi_workload_algorithmic_bytes():
+    wl = bench.FwiWorkload()
+    assert (wl.cfg.nxc, wl.cfg.nzc) == (240, 140)
+    # 20 FP32 words per cell and chain per forward step (velocity + stress)
+    assert wl.stencil_bytes_per_step() == 80.0 * 240 * 140 * 64
+    cfg = wl.config()
+    assert cfg["chains"] == 64 and cfg["nt"] == 1500 and cfg["params"] == 600
