@@ -148,3 +148,70 @@ def test_tomography_problem_shape():
     assert nnz.min() > 0 and 20 < nnz.mean() < 64 * 2
     bg = t["background"]
     assert bg.min() >= 0.2 - 1e-12 and bg.max() <= 0.5 + 1e-12
+
+
+class _FakeSurrogate:
+    def __init__(self, d, frozen=True):
+        self.d, self.frozen = d, frozen
+
+
+def _parsed(d=3, chains=4, dtype="float32"):
+    smp = Samplers.HMC(seed=1)
+    smp._parse(None, _normal(d), 0.1, True, 10, None, "lf", None, 10, 1, False, False, None, False, 0.65, 0.75,
+               chains, dtype, None, True, None, False)
+    return smp
+
+
+@pytest.mark.parametrize(
+    "make,msg",
+    [
+        (lambda: (_parsed(dtype="float64"), _FakeSurrogate(3)), "float32"),
+        (lambda: (_parsed(), _FakeSurrogate(5)), "dimensions"),
+        (lambda: (_parsed(), _FakeSurrogate(3, frozen=False)), "freeze"),
+    ],
+)
+def test_surrogate_argument_validation(make, msg):
+    """A surrogate must be frozen, match the target's dimension and drive
+    float32 chains; checked on the host before any device work."""
+    smp, sur = make()
+    with pytest.raises(AssertionError, match=msg):
+        smp._parse_surrogate(sur, None)
+
+
+def test_training_set_disables_graph_capture():
+    """Recording exact gradients needs the host between launches, so the
+    sampler runs uncaptured; a frozen surrogate alone keeps the graphs."""
+    smp = _parsed()
+    smp._parse_surrogate(_FakeSurrogate(3), None)
+    assert smp.use_graph is True
+    smp = _parsed()
+    smp._parse_surrogate(None, _FakeSurrogate(3))
+    assert smp.use_graph is False
+
+
+@pytest.mark.parametrize(
+    "temps,interval,msg",
+    [
+        ([1.0, 2.0, 4.0], None, "one temperature per chain"),
+        ([1.0, 2.0, 0.0, 4.0], None, "positive"),
+        ([1.0, 2.0, np.inf, 4.0], None, "finite"),
+        ([1.0, 2.0, 3.0, 4.0], 0, "positive int"),
+        ([1.0, 2.0, 3.0, 4.0], 2.5, "positive int"),
+    ],
+)
+def test_tempering_argument_validation(temps, interval, msg):
+    smp = _parsed(chains=4)
+    with pytest.raises(AssertionError, match=msg):
+        smp._parse_tempering(temps, interval)
+
+
+def test_replica_exchange_needs_two_chains_and_a_thinning_multiple():
+    with pytest.raises(AssertionError, match="two chains"):
+        _parsed(chains=1)._parse_tempering(None, 5)
+    smp = Samplers.HMC(seed=1)
+    smp._parse(None, _normal(3), 0.1, True, 10, None, "lf", None, 12, 3, False, False, None, False, 0.65, 0.75,
+               4, "float32", None, True, None, False)
+    with pytest.raises(AssertionError, match="multiple of online_thinning"):
+        smp._parse_tempering(None, 4)
+    smp._parse_tempering([1.0, 1.5, 2.0, 3.0], 6)
+    assert smp.exchange_interval == 6 and np.allclose(smp._temperatures, [1.0, 1.5, 2.0, 3.0])
