@@ -215,3 +215,72 @@ def test_replica_exchange_needs_two_chains_and_a_thinning_multiple():
         smp._parse_tempering(None, 4)
     smp._parse_tempering([1.0, 1.5, 2.0, 3.0], 6)
     assert smp.exchange_interval == 6 and np.allclose(smp._temperatures, [1.0, 1.5, 2.0, 3.0])
+
+
+def _linear_post(d=6, n=12, prior="normal", sparse=False):
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(0)
+    G = rng.normal(size=(n, d))
+    if sparse:
+        G = sp.csr_matrix(G)
+    lik = H.Distributions.LinearMatrix(G, rng.normal(size=(n, 1)), 0.1)
+    if prior is None:
+        return lik
+    pr = _normal(d) if prior == "normal" else H.Distributions.Laplace(np.zeros((d, 1)), np.ones((d, 1)))
+    return H.Distributions.BayesRule([pr, lik])
+
+
+def _parsed_for(post, chains=8, dtype="float32", proposals=10, autotuning=False):
+    smp = Samplers.HMC(seed=1)
+    smp._parse(None, post, 0.1, True, 10, None, "lf", None, proposals, 1, False, False, None, autotuning, 0.65,
+               0.75, chains, dtype, None, True, None, False)
+    smp._parse_surrogate(None, None)
+    smp._parse_tempering(None, None)
+    # the device set-up uploads the bounds; these targets have none
+    smp.lower = smp.upper = None
+    return smp
+
+
+@pytest.mark.parametrize(
+    "case",
+    ["too_large", "autotuning", "surrogate", "sparse", "no_linear", "two_priors", "opted_out"],
+)
+def test_persistent_kernel_declines_unsupported_runs(case):
+    """The persistent path applies only to small dense linear-Gaussian (or
+    Laplace-prior) targets without bounds, autotuning, tempering or a
+    surrogate; every other run keeps the launch-per-step path.  Host logic,
+    no device allocation."""
+    from hmclab_gb300._persistent import PersistentDense
+
+    if case == "too_large":
+        smp = _parsed_for(_linear_post(d=200, n=300))
+    elif case == "autotuning":
+        smp = _parsed_for(_linear_post(), autotuning=True)
+    elif case == "surrogate":
+        smp = _parsed_for(_linear_post())
+        smp.surrogate = _FakeSurrogate(6)
+    elif case == "sparse":
+        smp = _parsed_for(_linear_post(sparse=True))
+    elif case == "no_linear":
+        smp = _parsed_for(_normal(6))
+    elif case == "two_priors":
+        post = H.Distributions.BayesRule([_normal(6), _normal(6), _linear_post(prior=None)])
+        smp = _parsed_for(post)
+    else:
+        smp = _parsed_for(_linear_post())
+        smp.use_persistent = False
+    assert PersistentDense.applies(smp) is None
+
+
+def test_persistent_shared_memory_budget():
+    from hmclab_gb300._persistent import MAX_D, _SMEM, _smem
+
+    # GtG with an odd row stride plus one vector per warp; a full mass adds
+    # its inverse and Cholesky factor
+    assert _smem(50, False, 4, 4) == (50 * 51 + 4 * 50) * 4
+    assert _smem(64, True, 2, 8) == (3 * 64 * 65 + 2 * 64) * 8
+    # the largest supported dimension fits in FP32 with a unit or diagonal
+    # mass; in FP64 with a full mass it does not, and the path declines it
+    assert _smem(MAX_D, False, 16, 4) <= _SMEM
+    assert _smem(MAX_D, True, 1, 8) > _SMEM
