@@ -284,3 +284,38 @@ def test_persistent_shared_memory_budget():
     # mass; in FP64 with a full mass it does not, and the path declines it
     assert _smem(MAX_D, False, 16, 4) <= _SMEM
     assert _smem(MAX_D, True, 1, 8) > _SMEM
+
+
+@pytest.mark.parametrize("case", ["float64", "full_mass", "small", "sparse", "tempered", "two_priors"])
+def test_fused_tensor_core_step_declines_unsupported_runs(case):
+    """The fused tensor-core leapfrog step applies to FP32 chains of a dense
+    premultiplied LinearMatrix with d >= 64 and at most one diagonal Normal
+    or Laplace prior, under a unit or diagonal mass and no tempering."""
+    from hmclab_gb300._dense_tc import FusedDenseStep
+
+    d = 16 if case == "small" else 80
+    post = _linear_post(d=d, n=2 * d, sparse=case == "sparse")
+    if case == "two_priors":
+        post = H.Distributions.BayesRule([_normal(d), _normal(d), _linear_post(d=d, n=2 * d, prior=None)])
+    smp = _parsed_for(post, dtype="float64" if case == "float64" else "float32")
+    if case == "full_mass":
+        smp.mass_matrix = H.MassMatrices.Full(np.eye(d))
+    if case == "tempered":
+        smp.beta = object()
+    assert FusedDenseStep.applies(smp) is None
+
+
+def test_moment_error():
+    from hmclab_gb300 import diagnostics
+
+    me, se = diagnostics.moment_error(np.array([1.0, 2.0]), np.array([1.0, 4.0]), [[1.1], [2.0]], [[2.0], [5.0]])
+    assert me == pytest.approx(0.05) and se == pytest.approx(0.5)
+
+
+def test_batched_calls_reject_host_arrays_and_wrong_shapes():
+    torch = pytest.importorskip("torch")
+    dist = _normal(4)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        dist.misfit_batch(torch.zeros(4, 3))
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        dist.gradient_batch(np.zeros((4, 3)))
