@@ -238,6 +238,11 @@ class HMC:
         self.amount_of_steps = amount_of_steps
         if mass_matrix is None:
             mass_matrix = _Unit(self.dimensions)
+        if mass_matrix.kind is None:
+            raise NotImplementedError(
+                f"{type(mass_matrix).__name__} updates the mass inside the trajectory, which the batched device "
+                "sampler does not do (it would make the chain inexact); learn it on the host and pass "
+                "freeze(cast=True), a Full mass matrix")
         mass_matrix.rng = self.rng
         assert isinstance(mass_matrix, _AbstractMassMatrix), (
             "The passed mass matrix (mass_matrix) should be a class derived from _AbstractMassMatrix."
