@@ -85,3 +85,29 @@ def test_struct_layout_matches_c(tmp_path, cname, cls):
     assert out[0] == ctypes.sizeof(cls)
     for f, off in zip(fields, out[1:]):
         assert getattr(cls, f).offset == off, f
+
+
+def test_new_entry_points_reject_bad_arguments_on_the_host(lib):
+    """Argument checks of the potential-surrogate, rank-normalisation and
+    FWI entry points run before any CUDA call (no GPU here)."""
+    E = _lib.HMC_ERR_INVALID_ARG
+    # unknown element-wise mode, missing buffers, bad pitches
+    assert lib.hmc_pot_elementwise(9, 4, 4, None, 0, ctypes.c_void_p(8), 4, None, 0, None, ctypes.c_void_p(8), 4,
+                                   None, 0, None, 0, None) == E
+    assert b"unknown mode" in lib.hmc_last_error()
+    assert lib.hmc_pot_elementwise(_lib.HMC_POT_DELTA2, 4, 4, None, 0, ctypes.c_void_p(8), 4, None, 0, None,
+                                   ctypes.c_void_p(8), 4, None, 0, None, 0, None) == E
+    assert lib.hmc_pot_elementwise(_lib.HMC_POT_DELTA1, 4, 8, ctypes.c_void_p(8), 8, ctypes.c_void_p(8), 4, None, 0,
+                                   None, ctypes.c_void_p(8), 8, None, 0, None, 0, None) == E
+    assert lib.hmc_pot_loss(4, 8, ctypes.c_void_p(8), 4, ctypes.c_void_p(8), 8, ctypes.c_void_p(8),
+                            ctypes.c_void_p(8), 8, ctypes.c_void_p(8), 4, ctypes.c_void_p(8), None) == E
+    assert lib.hmc_pot_w3_grad(0, 8, None, 8, None, 8, None, None) == E
+    assert lib.hmc_pot_scaled_cast(4, 4, ctypes.c_void_p(8), 4, 0, ctypes.c_void_p(8), ctypes.c_void_p(8), 6, 4,
+                                   None) == E
+    # the S^2 d comparison budget of the rank normalisation
+    assert lib.hmc_rank_normalize(_lib.HMC_F32, 100000, 200, 64, ctypes.c_void_p(8), ctypes.c_void_p(8), None) == E
+    assert b"budget" in lib.hmc_last_error()
+    assert lib.hmc_rank_normalize(_lib.HMC_F32, 10, 2, 4, None, ctypes.c_void_p(8), None) == E
+    # FWI entry points with no descriptor
+    assert lib.hmc_fwi_forward_shot(None, 0, 0, 0, 0, None) == E
+    assert lib.hmc_fwi_adjoint_shot(None, 0, None) == E
