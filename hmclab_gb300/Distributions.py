@@ -530,6 +530,25 @@ class LinearMatrix(_AbstractDistribution):
             cache[key] = _dense_tc.DenseOperands(self, C, device)
         return cache[key]
 
+    def check_device_status(self):
+        """The tensor-core contractions wait on tensor-copy barriers with a
+        bound; raise DeviceTimeoutError if one of them ran out since the last
+        check (synchronises with the device)."""
+        for key, ops in list(self.__dict__.get("_scratch_cache", {}).items()):
+            if isinstance(key, tuple) and key[0] == "tc":
+                ops.check_status()
+
+    def _csr_plan(self, C, device, stream):
+        """Slab-staged FP32 products of the sparse G for C chains, with the
+        launch shapes the autotuner picked (timed on the first call)."""
+        from hmclab_gb300 import _csr
+
+        cache = self.__dict__.setdefault("_scratch_cache", {})
+        key = ("csr_slab", int(C))
+        if key not in cache:
+            cache[key] = _csr.CsrSlabPlan(self, C, device, stream)
+        return cache[key]
+
     def _use_tc(self, dtype, C):
         from hmclab_gb300 import _dense_tc
 
@@ -551,6 +570,8 @@ class LinearMatrix(_AbstractDistribution):
         if self.dense:
             _lib.call("hmc_dense_resid_misfit", code, self.n_data, d, C, M.data_ptr(), p["G"].data_ptr(),
                       p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(), int(accumulate), stream)
+        elif dtype == "float32":
+            self._csr_plan(C, M.device, stream).misfit(M, resid, out, accumulate, stream)
         else:
             _lib.call("hmc_csr_misfit", code, self.n_data, d, C, M.data_ptr(), p["rp"].data_ptr(), p["col"].data_ptr(),
                       p["val"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(),
@@ -572,6 +593,8 @@ class LinearMatrix(_AbstractDistribution):
             _lib.call("hmc_dense_resid_gradient", code, self.n_data, d, C, M.data_ptr(), p["G"].data_ptr(),
                       p["Gt"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), out.data_ptr(),
                       int(accumulate), stream)
+        elif dtype == "float32":
+            self._csr_plan(C, M.device, stream).gradient(M, resid, out, accumulate, stream)
         else:
             _lib.call("hmc_csr_gradient", code, self.n_data, d, C, M.data_ptr(), p["rp"].data_ptr(),
                       p["col"].data_ptr(), p["val"].data_ptr(), p["trp"].data_ptr(), p["tcol"].data_ptr(),

@@ -121,6 +121,20 @@ class HmcSchedule(_ct.Structure):
     ]
 
 
+class HmcCsrSlabs(_ct.Structure):
+    """Mirror of `hmc_csr_slabs` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("col", c_void_p),
+        ("val", c_void_p),
+        ("slab_ptr", c_void_p),
+        ("rows", c_int64),
+        ("cols", c_int64),
+        ("slab", c_int32),
+        ("rows_per_warp", c_int32),
+    ]
+
+
 class HmcDenseGroup(_ct.Structure):
     """Mirror of `hmc_dense_group` in include/hmclab_gb300.h."""
 
@@ -169,6 +183,10 @@ SIGNATURES = {
     "hmc_version": [],
     "hmc_last_error": [],
     "hmc_launch_count": [],
+    "hmc_set_wait_limits": [c_uint64, I],
+    "hmc_stream_capturing": [S, P],
+    "hmc_csr_slab_misfit": [P, I64, P, P, P, P, P, P, I, S],
+    "hmc_csr_slab_gradient": [P, P, I64, P, P, P, P, P, P, I, S],
     "hmc_philox_normal": [I, I64, I64, c_uint64, c_uint64, c_uint32, P, S],
     "hmc_philox_raw": [I64, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, P, S],
     "hmc_begin_trajectory": [P, D, S],
@@ -293,3 +311,24 @@ def call(name, *args):
 
 def launch_count():
     return int(load().hmc_launch_count())
+
+
+class wait_limits:
+    """Context manager around hmc_set_wait_limits (a test hook): inside it,
+    bounded device waits give up after `wait_ns`, and with `withhold` block 0
+    of every launch that stages tiles through tensor-copy barriers skips its
+    arrival, so its wait runs out and the kernel reports a time-out.  The
+    production limits (2 s, nothing withheld) are restored on exit."""
+
+    DEFAULT_NS = 2_000_000_000
+
+    def __init__(self, wait_ns, withhold=False):
+        self.wait_ns, self.withhold = int(wait_ns), int(bool(withhold))
+
+    def __enter__(self):
+        call("hmc_set_wait_limits", self.wait_ns, self.withhold)
+        return self
+
+    def __exit__(self, *exc):
+        call("hmc_set_wait_limits", self.DEFAULT_NS, 0)
+        return False

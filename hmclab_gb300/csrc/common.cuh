@@ -20,6 +20,17 @@ void count_launch(int n = 1);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Limits of the bounded device waits, read by the launchers of the kernels
+// that wait on tensor-copy barriers.  Production: 2 s, nothing withheld.
+// hmc_set_wait_limits shortens the limit and makes block 0 of those kernels
+// withhold its first barrier arrival, so a test can make a wait run out and
+// check the status path without faulting or hanging the GPU.
+struct WaitLimits {
+  uint64_t ns;
+  int withhold;
+};
+WaitLimits wait_limits();
+
 // Check the launch that was just issued.
 inline int check_launch(const char* where) {
   count_launch();

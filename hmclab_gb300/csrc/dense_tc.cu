@@ -20,7 +20,8 @@
 //                            q += drift*eps*M^-1 p; reflect; write p, q and
 //                            the next step's Q hi/lo operand
 //             EPI_MISFIT     partial[tile][c] = sum_r (D - data[r])^2 inv_var[r]
-// Every mbarrier wait is bounded (2 s of %globaltimer); on expiry the CTA sets
+// Every mbarrier wait is bounded (2 s of %globaltimer by default, see
+// hmc_set_wait_limits); on expiry the CTA sets
 // *status = HMC_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
 // copies and MMAs, frees its TMEM and returns.
 #include <cuda.h>
@@ -55,7 +56,6 @@ struct Stage {
 };
 constexpr int THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t TMEM_COLS = 256;
-constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
 
 enum Epi { EPI_GRAD = 0, EPI_STEP = 1, EPI_MISFIT = 2, EPI_MLP_HIDDEN = 3, EPI_MLP_OUT = 4, EPI_MLP_BACK = 5 };
 enum Prior { PRIOR_NONE = 0, PRIOR_NORMAL = 1, PRIOR_LAPLACE = 2 };
@@ -99,6 +99,8 @@ struct EpiParams {
   const float* out_scale;
   const float* out_shift;
   int* status;
+  uint64_t wait_ns;  // bounded-wait limit (filled by the launcher)
+  int withhold;      // test hook: block (0, 0) skips its first stage's copies
 };
 
 // GELU(z) = z Phi(z) and its derivative Phi(z) + z phi(z), with
@@ -139,14 +141,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait; false when the 2 s limit expired or another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+// Bounded wait; false when the limit (2 s in production) expired or another
+// role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (globaltimer() - t0 > WAIT_NS) return false;
+    if (globaltimer() - t0 > limit_ns) return false;
   }
 }
 
@@ -251,10 +255,16 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int kb = 0; kb < num_kb; ++kb) {
       const int s = kb % STAGES;
       if (kb >= STAGES) {
-        if (!mbar_wait(&empty[s], ((kb / STAGES) & 1) ^ 1, abort_flag)) {
+        if (!mbar_wait(&empty[s], ((kb / STAGES) & 1) ^ 1, abort_flag, ep.wait_ns)) {
           *abort_flag = 1;
           break;
         }
+      }
+      if (ep.withhold && kb == 0 && blockIdx.x == 0 && blockIdx.y == 0) {
+        // test hook: this stage is never armed, so the MMA issuer's wait on
+        // it runs out; nothing is in flight for it
+        ++tma_issued_stage_uses;
+        continue;
       }
       unsigned char* st = smem + s * S::bytes;
       mbar_expect_tx(&full[s], S::bytes);
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     bool ok = true;
     for (int kb = 0; kb < num_kb; ++kb) {
       const int s = kb % STAGES;
-      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag)) {
+      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag, ep.wait_ns)) {
         *abort_flag = 1;
         ok = false;
         break;
@@ -325,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
     }
     // warp-uniform: the TMEM loads below are warp-collective
-    const bool ready = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort_flag) ? 1 : 0) != 0;
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort_flag, ep.wait_ns) ? 1 : 0) != 0;
     tc_fence_after();
     const bool live_c = ready && c < C;
     const uint32_t tbase = tmem + ((uint32_t)lane_base << 16);
@@ -483,14 +493,14 @@ __global__ void __launch_bounds__(THREADS, 1)
     // Drain what this CTA put in flight before releasing TMEM and smem.
     if (warp == 1 && lane == 0) {
       const uint64_t t0 = globaltimer();
-      while (!mbar_try_wait(accum, 0) && globaltimer() - t0 < WAIT_NS) {
+      while (!mbar_try_wait(accum, 0) && globaltimer() - t0 < ep.wait_ns) {
       }
     }
     if (warp == 0 && lane == 0) {
       for (int u = 0; u < tma_issued_stage_uses && u < num_kb; ++u) {
         const int s = u % STAGES;
         const uint64_t t0 = globaltimer();
-        while (!mbar_try_wait(&full[s], (u / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+        while (!mbar_try_wait(&full[s], (u / STAGES) & 1) && globaltimer() - t0 < ep.wait_ns) {
         }
       }
       atomicExch(ep.status, HMC_ERR_TIMEOUT);
@@ -611,7 +621,11 @@ int launch(int64_t C, int64_t rows, int64_t K, const void* q_hi, const void* q_l
   const int num_kb = (int)((K + BK - 1) / BK);
   const dim3 grid((unsigned)((C + BM - 1) / BM), (unsigned)((rows + BN - 1) / BN));
   HMC_REQUIRE(grid.y <= 65535, "tensor-core contraction: too many rows");
-  chain_gemm_kernel<EPI, NPROD><<<grid, THREADS, smem, st>>>(mq_hi, mq_lo, ma_hi, ma_lo, num_kb, ep);
+  EpiParams e = ep;
+  const WaitLimits wl = wait_limits();
+  e.wait_ns = wl.ns;
+  e.withhold = wl.withhold;
+  chain_gemm_kernel<EPI, NPROD><<<grid, THREADS, smem, st>>>(mq_hi, mq_lo, ma_hi, ma_lo, num_kb, e);
   return check_launch("chain_gemm_kernel");
 }
 

@@ -196,6 +196,208 @@ int csr_spmm(int64_t rows, int64_t C, const int32_t* rp, const int32_t* col, con
   return HMC_OK;
 }
 
+// ---- CSR times a chain block through shared-memory column slabs (FP32) ------
+// out[r][c] = (sum_k val[k] X[col[k]][c] - bias[r]) * rs[r] (+ out), as
+// csr_spmm_kernel, for a CSR whose columns are sorted within each row.
+//
+// Each nonzero of the tomography operator multiplies a whole row of the chain
+// block, and every column is shared by tens of rows, so gathering X rows from
+// L2 once per nonzero moves nnz * C * 4 bytes.  Here a block owns 32 chains
+// (one per lane) and a group of CSR_WARPS * RPW rows (warp w: rows
+// r0 + w + CSR_WARPS * i).  The columns are walked in slabs of `slab`: X[slab
+// columns][the block's 32 chains] is copied into shared memory by
+// asynchronous copies (cp.async), double-buffered so that the next slab is in
+// flight while the warps add the current slab's nonzeros of their rows
+// (slab_ptr[r][s] .. slab_ptr[r][s + 1]) into register accumulators.  Each X
+// element is read from L2 once per row group instead of once per nonzero,
+// and a shared-memory read is one 128-byte row per nonzero and warp, free of
+// bank conflicts.  Nonzeros are added in CSR order with fused multiply-adds,
+// so the sums equal csr_spmm_kernel's bit for bit.
+constexpr int CSR_WARPS = 16;
+constexpr int CSR_THREADS = 32 * CSR_WARPS;
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+  // a chain past C copies nothing and zero-fills (src-size 0)
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src), "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Issue the copies of slab s (columns s*slab ..) into buffer `buf`.  VEC4:
+// C is a multiple of 4 and X 16-byte aligned, so every chain quad of a row is
+// one 16-byte copy (the block's 32 chains are 8 quads; quads past C are
+// skipped, their lanes never store results).
+template <bool VEC4>
+__device__ __forceinline__ void csr_slab_fill(float* buf, const float* __restrict__ X, int C, int c0, int cols,
+                                              int slab, int s) {
+  const int k0 = s * slab;
+  const int kn = cols - k0 < slab ? cols - k0 : slab;
+  if (VEC4) {
+    for (int t = threadIdx.x; t < kn * 8; t += CSR_THREADS) {
+      const int row = t >> 3, q = t & 7, cc = c0 + 4 * q;
+      if (cc < C) cp_async16(buf + row * 32 + 4 * q, X + (int64_t)(k0 + row) * C + cc);
+    }
+  } else {
+    for (int t = threadIdx.x; t < kn * 32; t += CSR_THREADS) {
+      const int row = t >> 5, cc = c0 + (t & 31);
+      const bool ok = cc < C;
+      cp_async4(buf + t, ok ? X + (int64_t)(k0 + row) * C + cc : X, ok);
+    }
+  }
+  cp_async_commit();
+}
+
+// Subtract center[column] from the elements of slab s this thread copied (its
+// own copies are complete once it has waited for them).
+template <bool VEC4>
+__device__ __forceinline__ void csr_slab_centre(float* buf, const float* __restrict__ center, int C, int c0,
+                                                int cols, int slab, int s) {
+  const int k0 = s * slab;
+  const int kn = cols - k0 < slab ? cols - k0 : slab;
+  if (VEC4) {
+    for (int t = threadIdx.x; t < kn * 8; t += CSR_THREADS) {
+      const int row = t >> 3, q = t & 7;
+      if (c0 + 4 * q < C) {
+        float4* v = (float4*)(buf + row * 32 + 4 * q);
+        const float cv = center[k0 + row];
+        float4 x = *v;
+        x.x -= cv;
+        x.y -= cv;
+        x.z -= cv;
+        x.w -= cv;
+        *v = x;
+      }
+    }
+  } else {
+    for (int t = threadIdx.x; t < kn * 32; t += CSR_THREADS) buf[t] -= center[k0 + (t >> 5)];
+  }
+}
+
+template <int RPW, bool VEC4>
+__global__ void __launch_bounds__(CSR_THREADS, 2)
+    csr_slab_kernel(int rows, int cols, int C, const int32_t* __restrict__ col, const float* __restrict__ val,
+                    const int32_t* __restrict__ slab_ptr, int n_slabs, int slab, const float* __restrict__ X,
+                    const float* __restrict__ center, const float* __restrict__ bias, const float* __restrict__ rs,
+                    float* out, int accumulate) {
+  extern __shared__ __align__(16) float sx[];  // two buffers of [slab][32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c0 = blockIdx.x * 32, c = c0 + lane;
+  const int r0 = blockIdx.y * (CSR_WARPS * RPW);
+  float acc[RPW];
+#pragma unroll
+  for (int i = 0; i < RPW; ++i) acc[i] = 0.f;
+  csr_slab_fill<VEC4>(sx, X, C, c0, cols, slab, 0);
+  for (int s = 0; s < n_slabs; ++s) {
+    float* cur = sx + (s & 1) * slab * 32;
+    if (s + 1 < n_slabs) {
+      // the other buffer was released by the barrier at the end of slab s - 1
+      csr_slab_fill<VEC4>(sx + ((s + 1) & 1) * slab * 32, X, C, c0, cols, slab, s + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    if (center) csr_slab_centre<VEC4>(cur, center, C, c0, cols, slab, s);
+    __syncthreads();  // slab s has landed (and is centred) for every thread's copies
+    const int k0 = s * slab;
+#pragma unroll
+    for (int i = 0; i < RPW; ++i) {
+      const int r = r0 + warp + CSR_WARPS * i;
+      if (r >= rows) break;  // warp-uniform
+      const int64_t sp = (int64_t)r * (n_slabs + 1) + s;
+      const int b = slab_ptr[sp], e = slab_ptr[sp + 1];
+      float a = acc[i];
+      int k = b;
+      for (; k + 4 <= e; k += 4) {
+        const int j0 = col[k] - k0, j1 = col[k + 1] - k0, j2 = col[k + 2] - k0, j3 = col[k + 3] - k0;
+        const float v0 = val[k], v1 = val[k + 1], v2 = val[k + 2], v3 = val[k + 3];
+        const float x0 = cur[j0 * 32 + lane], x1 = cur[j1 * 32 + lane], x2 = cur[j2 * 32 + lane],
+                    x3 = cur[j3 * 32 + lane];
+        a = fmaf(v0, x0, a);
+        a = fmaf(v1, x1, a);
+        a = fmaf(v2, x2, a);
+        a = fmaf(v3, x3, a);
+      }
+      for (; k < e; ++k) a = fmaf(val[k], cur[(col[k] - k0) * 32 + lane], a);
+      acc[i] = a;
+    }
+    __syncthreads();  // every warp is done with this buffer before it is refilled
+  }
+  if (c >= C) return;
+#pragma unroll
+  for (int i = 0; i < RPW; ++i) {
+    const int r = r0 + warp + CSR_WARPS * i;
+    if (r >= rows) break;
+    float v = acc[i];
+    if (bias) v -= bias[r];
+    if (rs) v *= rs[r];
+    const int64_t o = (int64_t)r * C + c;
+    out[o] = accumulate ? out[o] + v : v;
+  }
+}
+
+int csr_slab_check(const hmc_csr_slabs* A, const char* who) {
+  HMC_REQUIRE(A != nullptr, "%s: null CSR descriptor", who);
+  HMC_REQUIRE(A->col && A->val && A->slab_ptr, "%s: CSR descriptor has a null array", who);
+  HMC_REQUIRE(A->rows > 0 && A->cols > 0 && A->rows < (1ll << 31) && A->cols < (1ll << 31), "%s: bad CSR shape",
+              who);
+  HMC_REQUIRE(A->slab >= 32 && A->slab <= 448,
+              "%s: slab of %d columns outside 32 .. 448 (two double-buffered blocks per SM)", who, (int)A->slab);
+  HMC_REQUIRE(A->rows_per_warp == 4 || A->rows_per_warp == 8 || A->rows_per_warp == 16,
+              "%s: rows_per_warp must be 4, 8 or 16", who);
+  return HMC_OK;
+}
+
+template <int RPW, bool VEC4>
+int csr_slab_launch(const hmc_csr_slabs* A, int64_t C, const float* X, const float* center, const float* bias,
+                    const float* rs, float* out, int accumulate, cudaStream_t st) {
+  const int smem = 2 * A->slab * 32 * (int)sizeof(float);  // double buffer
+  static int attr_bytes = 0;  // per instantiation: the largest size enabled so far
+  if (smem > 48 * 1024 && smem > attr_bytes) {
+    cudaError_t e =
+        cudaFuncSetAttribute(csr_slab_kernel<RPW, VEC4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(csr_slab_kernel)");
+    attr_bytes = smem;
+  }
+  const int n_slabs = (int)((A->cols + A->slab - 1) / A->slab);
+  const int64_t groups = (A->rows + CSR_WARPS * RPW - 1) / (CSR_WARPS * RPW);
+  HMC_REQUIRE(groups <= 65535, "csr slab product: too many rows");
+  const dim3 grid((unsigned)((C + 31) / 32), (unsigned)groups);
+  csr_slab_kernel<RPW, VEC4><<<grid, CSR_THREADS, smem, st>>>((int)A->rows, (int)A->cols, (int)C, A->col, A->val,
+                                                              A->slab_ptr, n_slabs, A->slab, X, center, bias, rs,
+                                                              out, accumulate);
+  return check_launch("csr_slab_kernel");
+}
+
+template <int RPW>
+int csr_slab_launch(const hmc_csr_slabs* A, int64_t C, const float* X, const float* center, const float* bias,
+                    const float* rs, float* out, int accumulate, cudaStream_t st) {
+  const bool vec4 = C % 4 == 0 && ((uintptr_t)X & 15) == 0;
+  return vec4 ? csr_slab_launch<RPW, true>(A, C, X, center, bias, rs, out, accumulate, st)
+              : csr_slab_launch<RPW, false>(A, C, X, center, bias, rs, out, accumulate, st);
+}
+
+int csr_slab(const hmc_csr_slabs* A, int64_t C, const float* X, const float* center, const float* bias,
+             const float* rs, float* out, int accumulate, cudaStream_t st) {
+  HMC_REQUIRE(C < (1ll << 31) && (C + 31) / 32 <= 0x7fffffff, "csr slab product: too many chains");
+  switch (A->rows_per_warp) {
+    case 4:
+      return csr_slab_launch<4>(A, C, X, center, bias, rs, out, accumulate, st);
+    case 8:
+      return csr_slab_launch<8>(A, C, X, center, bias, rs, out, accumulate, st);
+    default:
+      return csr_slab_launch<16>(A, C, X, center, bias, rs, out, accumulate, st);
+  }
+}
+
 // ---- 3-D source location ----------------------------------------------------
 // One thread per (chain, event); stations are staged in shared memory.  The
 // per-pair terms mirror SourceLocation.py:495-540, including nansum's skipping
@@ -475,6 +677,32 @@ int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C, const void* M, 
     HMC_TRY(csr_spmm<T>(n, C, row_ptr, col, val, M, data, inv_var, resid, 0, st));
     return csr_spmm<T>(d, C, t_row_ptr, t_col, t_val, resid, nullptr, nullptr, out_g, accumulate, st);
   });
+}
+
+int hmc_csr_slab_misfit(const hmc_csr_slabs* G, int64_t C, const float* M, const float* center, const float* data,
+                        const float* inv_var, float* resid, double* out_x, int accumulate, void* stream) {
+  HMC_TRY(csr_slab_check(G, "hmc_csr_slab_misfit"));
+  HMC_REQUIRE(C >= 0, "hmc_csr_slab_misfit: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && data && inv_var && resid && out_x, "hmc_csr_slab_misfit: null argument");
+  cudaStream_t st = as_stream(stream);
+  HMC_TRY(csr_slab(G, C, M, center, data, nullptr, resid, 0, st));
+  weighted_sq_kernel<float><<<red_grid(C), red_block(), 0, st>>>(G->rows, C, resid, inv_var, out_x, accumulate);
+  return check_launch("weighted_sq_kernel");
+}
+
+int hmc_csr_slab_gradient(const hmc_csr_slabs* G, const hmc_csr_slabs* Gt, int64_t C, const float* M,
+                          const float* center, const float* data, const float* inv_var, float* resid, float* out_g,
+                          int accumulate, void* stream) {
+  HMC_TRY(csr_slab_check(G, "hmc_csr_slab_gradient"));
+  HMC_TRY(csr_slab_check(Gt, "hmc_csr_slab_gradient"));
+  HMC_REQUIRE(Gt->rows == G->cols && Gt->cols == G->rows, "hmc_csr_slab_gradient: G^T shape does not match G");
+  HMC_REQUIRE(C >= 0, "hmc_csr_slab_gradient: bad sizes");
+  if (C == 0) return HMC_OK;
+  HMC_REQUIRE(M && data && inv_var && resid && out_g, "hmc_csr_slab_gradient: null argument");
+  cudaStream_t st = as_stream(stream);
+  HMC_TRY(csr_slab(G, C, M, center, data, inv_var, resid, 0, st));
+  return csr_slab(Gt, C, resid, nullptr, nullptr, nullptr, out_g, accumulate, st);
 }
 
 int hmc_srcloc3d_misfit(int dtype, int64_t E, int64_t S, int64_t C, const void* M, const void* rx, const void* ry,

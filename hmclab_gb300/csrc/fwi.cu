@@ -39,6 +39,8 @@ struct Grid {
   int C;
   float inv_h;
   float dt;
+  uint64_t wait_ns;  // limit of the tile-barrier waits (2 s in production)
+  int withhold;      // test hook: block (0, 0) of the staged kernels never arms its barrier
   __device__ __forceinline__ int at(int j, int i) const { return (j * nx + i) * C; }
   __device__ __forceinline__ bool valid(int i, int j) const { return i >= 2 && i < nx - 2 && j >= 2 && j < nz - 2; }
 };
@@ -197,7 +199,6 @@ __global__ void __launch_bounds__(TX* TY* TZ) stress_kernel(Grid g, Fields f, Pa
 #define HMC_FWI_TILE_Z 4
 #endif
 constexpr int TT_X = HMC_FWI_TILE_X, TT_Z = HMC_FWI_TILE_Z;
-constexpr uint64_t TMA_WAIT_NS = 2000000000ull;  // bounded wait: 2 s
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -229,19 +230,26 @@ __device__ __forceinline__ void tile_load_3d(void* dst, const CUtensorMap* map, 
 }
 
 // Thread 0 arms the barrier and issues the tile loads; every thread then
-// waits (at most 2 s).  Returns false when the wait expired.
-__device__ __forceinline__ bool tile_wait(uint64_t* bar) {
+// waits (at most g.wait_ns, 2 s in production).  Returns false when the wait
+// expired.
+__device__ __forceinline__ bool tile_wait(uint64_t* bar, uint64_t limit_ns) {
   if (tile_barrier_try(bar, 0)) return true;
   const uint64_t t0 = now_ns();
   while (!tile_barrier_try(bar, 0))
-    if (now_ns() - t0 > TMA_WAIT_NS) return false;
+    if (now_ns() - t0 > limit_ns) return false;
   return true;
 }
 
-__device__ __forceinline__ void tile_barrier_arm(uint64_t* bar, uint32_t bytes) {
+// Initialises the barrier and announces `bytes` of tile copies.  Returns
+// false, with the barrier initialised but never armed, in block (0, 0) when
+// the wait-limit test hook withholds its arrival: the caller then issues no
+// copies, so nothing is in flight when the block's wait runs out.
+__device__ __forceinline__ bool tile_barrier_arm(uint64_t* bar, uint32_t bytes, const Grid& g) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(1u) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (g.withhold && blockIdx.x == 0 && blockIdx.y == 0) return false;
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  return true;
 }
 
 struct TileOrigin {
@@ -278,10 +286,11 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
   step_dependents_go();
   const TileOrigin o = tile_of(g);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_sxx) + sizeof(t_sxz) + sizeof(t_szz)));
-    tile_load_3d(t_sxx, &m_sxx, &bar, o.c0, o.i0 - 1, o.j0);
-    tile_load_3d(t_sxz, &m_sxz, &bar, o.c0, o.i0 - 2, o.j0 - 2);
-    tile_load_3d(t_szz, &m_szz, &bar, o.c0, o.i0, o.j0 - 1);
+    if (tile_barrier_arm(&bar, (uint32_t)(sizeof(t_sxx) + sizeof(t_sxz) + sizeof(t_szz)), g)) {
+      tile_load_3d(t_sxx, &m_sxx, &bar, o.c0, o.i0 - 1, o.j0);
+      tile_load_3d(t_sxz, &m_sxz, &bar, o.c0, o.i0 - 2, o.j0 - 2);
+      tile_load_3d(t_szz, &m_szz, &bar, o.c0, o.i0, o.j0 - 1);
+    }
   }
   // the block's own cells do not depend on the tiles: their loads are in
   // flight while the tensor copies land
@@ -303,11 +312,11 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
     }
   }
   __syncthreads();
-  if (!tile_wait(&bar)) {
+  if (!tile_wait(&bar, g.wait_ns)) {
     // record the failure, give the copies in flight one more bounded wait
     // so that none lands in a retired block's shared memory, and leave
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
-    tile_wait(&bar);
+    tile_wait(&bar, g.wait_ns);
     return;
   }
   if (!active) return;
@@ -356,9 +365,10 @@ __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_cons
   step_dependents_go();
   const TileOrigin o = tile_of(g);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_vx) + sizeof(t_vz)));
-    tile_load_3d(t_vx, &m_vx, &bar, o.c0, o.i0 - 2, o.j0 - 1);
-    tile_load_3d(t_vz, &m_vz, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+    if (tile_barrier_arm(&bar, (uint32_t)(sizeof(t_vx) + sizeof(t_vz)), g)) {
+      tile_load_3d(t_vx, &m_vx, &bar, o.c0, o.i0 - 2, o.j0 - 1);
+      tile_load_3d(t_vz, &m_vz, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+    }
   }
   const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
   const bool active = c < g.C && i < g.nx;
@@ -378,11 +388,11 @@ __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_cons
     }
   }
   __syncthreads();
-  if (!tile_wait(&bar)) {
+  if (!tile_wait(&bar, g.wait_ns)) {
     // record the failure, give the copies in flight one more bounded wait
     // so that none lands in a retired block's shared memory, and leave
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
-    tile_wait(&bar);
+    tile_wait(&bar, g.wait_ns);
     return;
   }
   if (!active) return;
@@ -542,12 +552,14 @@ __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
   step_dependents_go();
   const TileOrigin o = tile_of(g, R);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t1) + sizeof(t_t3) + sizeof(t_t2) + sizeof(t_vx) + sizeof(t_vz)));
-    tile_load_3d(t_t1, &m_t1, &bar, o.c0, o.i0 - 1, o.j0);
-    tile_load_3d(t_t3, &m_t3, &bar, o.c0, o.i0 - 2, o.j0 - 2);
-    tile_load_3d(t_t2, &m_t2, &bar, o.c0, o.i0, o.j0 - 1);
-    tile_load_3d(t_vx, &m_store, &bar, o.c0, o.i0 - 2, row_vx + o.j0 - 1);
-    tile_load_3d(t_vz, &m_store, &bar, o.c0, o.i0 - 1, row_vz + o.j0 - 2);
+    if (tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t1) + sizeof(t_t3) + sizeof(t_t2) + sizeof(t_vx) + sizeof(t_vz)),
+                         g)) {
+      tile_load_3d(t_t1, &m_t1, &bar, o.c0, o.i0 - 1, o.j0);
+      tile_load_3d(t_t3, &m_t3, &bar, o.c0, o.i0 - 2, o.j0 - 2);
+      tile_load_3d(t_t2, &m_t2, &bar, o.c0, o.i0, o.j0 - 1);
+      tile_load_3d(t_vx, &m_store, &bar, o.c0, o.i0 - 2, row_vx + o.j0 - 1);
+      tile_load_3d(t_vz, &m_store, &bar, o.c0, o.i0 - 1, row_vz + o.j0 - 2);
+    }
   }
   const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
   const bool active = c < g.C && i >= 2 && i < g.nx - 2;
@@ -579,9 +591,9 @@ __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
     }
   }
   __syncthreads();
-  if (!tile_wait(&bar)) {
+  if (!tile_wait(&bar, g.wait_ns)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
-    tile_wait(&bar);
+    tile_wait(&bar, g.wait_ns);
     return;
   }
   if (!active) return;
@@ -640,9 +652,10 @@ __global__ void __launch_bounds__(32 * TT_X) adj_stress_tma_kernel(const __grid_
   step_dependents_go();
   const TileOrigin o = tile_of(g, R);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t4) + sizeof(t_t5)));
-    tile_load_3d(t_t4, &m_t4, &bar, o.c0, o.i0 - 2, o.j0 - 1);
-    tile_load_3d(t_t5, &m_t5, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+    if (tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t4) + sizeof(t_t5)), g)) {
+      tile_load_3d(t_t4, &m_t4, &bar, o.c0, o.i0 - 2, o.j0 - 1);
+      tile_load_3d(t_t5, &m_t5, &bar, o.c0, o.i0 - 1, o.j0 - 2);
+    }
   }
   const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
   const bool active = c < g.C && i >= 2 && i < g.nx - 2;
@@ -662,9 +675,9 @@ __global__ void __launch_bounds__(32 * TT_X) adj_stress_tma_kernel(const __grid_
     }
   }
   __syncthreads();
-  if (!tile_wait(&bar)) {
+  if (!tile_wait(&bar, g.wait_ns)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(status, 1);
-    tile_wait(&bar);
+    tile_wait(&bar, g.wait_ns);
     return;
   }
   if (!active) return;
@@ -828,6 +841,9 @@ static Grid grid_of(const hmc_fwi* s) {
   g.C = (int)s->chains;
   g.inv_h = 1.f / s->h;
   g.dt = s->dt;
+  const WaitLimits wl = wait_limits();
+  g.wait_ns = wl.ns;
+  g.withhold = wl.withhold;
   return g;
 }
 

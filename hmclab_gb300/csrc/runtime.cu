@@ -26,6 +26,11 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static std::atomic<uint64_t> g_wait_ns{2000000000ull};
+static std::atomic<int> g_withhold{0};
+
+WaitLimits wait_limits() { return WaitLimits{g_wait_ns.load(), g_withhold.load()}; }
+
 __global__ void philox_normal_kernel_f32(int64_t rows, int64_t chains, uint64_t seed, uint64_t proposal,
                                          uint32_t purpose, float* out) {
   const int64_t quads = (rows + 3) / 4;
@@ -82,6 +87,14 @@ const char* hmc_last_error(void) { return g_last_error; }
 
 int64_t hmc_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+int hmc_set_wait_limits(uint64_t wait_ns, int withhold) {
+  HMC_REQUIRE(wait_ns >= 1000ull && wait_ns <= 2000000000ull, "hmc_set_wait_limits: limit must be 1 us .. 2 s");
+  HMC_REQUIRE(withhold == 0 || withhold == 1, "hmc_set_wait_limits: withhold must be 0 or 1");
+  g_wait_ns.store(wait_ns);
+  g_withhold.store(withhold);
+  return HMC_OK;
+}
+
 int hmc_philox_normal(int dtype, int64_t rows, int64_t chains, uint64_t seed, uint64_t proposal,
                       uint32_t purpose, void* out, void* stream) {
   HMC_REQUIRE(rows >= 0 && chains >= 0, "hmc_philox_normal: negative size");
@@ -109,6 +122,15 @@ int hmc_philox_raw(int64_t n, uint32_t ctr0, uint32_t ctr1, uint32_t ctr2, uint3
   philox_raw_kernel<<<blocks_for(n, 128) > 4096 ? 4096 : blocks_for(n, 128), 128, 0, as_stream(stream)>>>(
       n, make_uint4(ctr0, ctr1, ctr2, ctr3), make_uint2(key0, key1), out);
   return check_launch("hmc_philox_raw");
+}
+
+int hmc_stream_capturing(void* stream, int* capturing) {
+  HMC_REQUIRE(capturing != nullptr, "hmc_stream_capturing: null output");
+  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(as_stream(stream), &status);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+  *capturing = status != cudaStreamCaptureStatusNone;
+  return HMC_OK;
 }
 
 int hmc_graph_begin(void* stream) {

@@ -9,8 +9,8 @@ batch of chains, and the per-rank results are combined at the end:
 
   rank_environment()       RANK / WORLD_SIZE / LOCAL_RANK from the launcher
   rank_seed(seed, rank)    a distinct Philox key per rank
-  combine_ess(ess, sec)    multi-chain ESS of the union of the ranks' chains
-                           (sum of per-rank ESS) and the slowest rank's time
+  combine_ess(ess, sec)    sum of the per-rank multi-chain ESS and the
+                           slowest rank's time (independent, stationary ranks)
   combine_moments(...)     pooled mean and standard deviation of all samples
 """
 import os
@@ -44,9 +44,15 @@ def _gather(vec):
 
 
 def combine_ess(ess, seconds):
-    """ESS per parameter of all ranks' chains together and the time of the
-    slowest rank.  Chains on different ranks are independent draws of the
-    same target, so their effective sample sizes add."""
+    """ESS per parameter over all ranks and the time of the slowest rank.
+
+    The per-rank multi-chain ESS values are added.  That equals the ESS of
+    the pooled chains only when every rank's chains are independent and
+    already stationary on the same target: the sum never sees the variance
+    between ranks, so ranks that have not mixed (different modes, unfinished
+    burn-in) make it overstate the pooled ESS, which a split-R-hat over the
+    pooled chains would expose.  The sampler's ranks start from burned-in
+    states with disjoint Philox keys, which is the case this estimate is for."""
     parts = _gather(_np.concatenate([_np.asarray(ess, _np.float64).reshape(-1), [float(seconds)]]))
     total = sum(p[:-1] for p in parts)
     return total, max(float(p[-1]) for p in parts)

@@ -57,6 +57,19 @@ HMC_API int hmc_version(void);
 HMC_API const char* hmc_last_error(void);
 /* Number of kernels this library has launched since load (host-side counter). */
 HMC_API int64_t hmc_launch_count(void);
+/* Limits of the bounded waits of the kernels that stage operands through
+ * tensor-copy barriers (tensor-core contractions, elastic stencils).  The
+ * default is 2 s with nothing withheld.  A test hook: with withhold = 1,
+ * block 0 of every such launch skips its first barrier arrival, so its wait
+ * runs out after wait_ns (1 us .. 2 s); the kernel then sets its status word
+ * (HMC_ERR_TIMEOUT, or 1 for the stencils), frees what it holds and returns.
+ * Launches captured in a CUDA graph keep the limits of their capture.
+ * Reference counterpart: none (the reference has no device code); it stands
+ * for the fault-injection tests of the sampler loop (tests/test_break.py). */
+HMC_API int hmc_set_wait_limits(uint64_t wait_ns, int withhold);
+/* *capturing = 1 while `stream` is being captured into a CUDA graph (the
+ * launch-shape autotuner times nothing then).  No reference counterpart. */
+HMC_API int hmc_stream_capturing(void* stream, int* capturing);
 
 /* ---- counter-based RNG (Philox4x32-10, Salmon et al. 2011) ---------------
  * Replaces the numpy Generator draws of MassMatrices.py:142,227,314 and
@@ -243,9 +256,11 @@ HMC_API int hmc_dense_resid_gradient(int dtype, int64_t n, int64_t d, int64_t C,
  * residual lives in a library-owned device array of
  * HMC_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library until
  * exit.  Larger n*C is rejected with HMC_ERR_INVALID_ARG.  No allocation is
- * made; the array's address is looked up on each device's first call (make
- * that call before any stream capture).  Calls share the array: calls that
- * overlap on the GPU race and must be serialised.                           */
+ * made; the array's address is looked up on the first call in each device
+ * context (make that call before any stream capture), and again on the first
+ * call after the context was destroyed and re-created (cudaDeviceReset).
+ * Calls share the array: calls that overlap on the GPU race and must be
+ * serialised.                                                                */
 #define HMC_NOALLOC_SCRATCH_BYTES (16u << 20)
 HMC_API int hmc_dense_resid_misfit_noalloc(int dtype, int64_t n, int64_t d,
                                            int64_t C, const void* M,
@@ -267,6 +282,39 @@ HMC_API int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C,
                      const void* t_val, const void* data,
                      const void* inv_var, void* resid, void* out_g,
                      int accumulate, void* stream);
+
+/* LinearMatrix.py:389-426 (sparse G, simple covariance) in FP32 for a CSR
+ * whose column indices are sorted within each row (canonical CSR, scipy's
+ * sort_indices).  The chain block is staged through shared memory in
+ * double-buffered slabs of `slab` columns (32 .. 448); slab_ptr[r * (n_slabs
+ * + 1) + s] is the first
+ * nonzero of row r whose column is >= s * slab, with n_slabs =
+ * ceil(cols / slab), so slab_ptr[r * (n_slabs + 1)] = row_ptr[r] and the last
+ * entry of a row is row_ptr[r + 1].  rows_per_warp (4, 8 or 16) sets the rows
+ * a block accumulates per slab pass (16 warps per block).  With center NULL
+ * the results equal hmc_csr_misfit / hmc_csr_gradient bit for bit; slab and
+ * rows_per_warp only change the speed (picked by the host autotuner).
+ * center ([cols], may be NULL) makes the first product G (M - center) -
+ * data: the caller passes data - G center (formed in FP64) so that the
+ * residual is unchanged but the FP32 sums no longer cancel terms of the size
+ * of G M (travel times ~1e3 x their residuals in the tomography workload).  */
+typedef struct hmc_csr_slabs {
+  const int32_t* col;      /* [nnz] column indices, sorted within rows */
+  const float* val;        /* [nnz] values                              */
+  const int32_t* slab_ptr; /* [rows][n_slabs + 1] slab starts per row   */
+  int64_t rows, cols;
+  int32_t slab;            /* columns per shared-memory slab            */
+  int32_t rows_per_warp;   /* 4, 8 or 16                                */
+} hmc_csr_slabs;
+HMC_API int hmc_csr_slab_misfit(const hmc_csr_slabs* G, int64_t C, const float* M,
+                                const float* center, const float* data,
+                                const float* inv_var, float* resid,
+                                double* out_x, int accumulate, void* stream);
+HMC_API int hmc_csr_slab_gradient(const hmc_csr_slabs* G, const hmc_csr_slabs* Gt,
+                                  int64_t C, const float* M, const float* center,
+                                  const float* data, const float* inv_var,
+                                  float* resid, float* out_g, int accumulate,
+                                  void* stream);
 
 /* SourceLocation.py:482-540 (SourceLocation3D, homogeneous velocity).
  * Parameters are interleaved [x,y,z,T] per event followed by v when

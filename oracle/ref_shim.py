@@ -16,7 +16,19 @@ import sys
 import types
 from unittest import mock
 
-REFERENCE_ROOT = os.environ.get("HMCLAB_REFERENCE_ROOT", "/root/reference")
+
+def _reference_root():
+    """The reference checkout: $HMCLAB_REFERENCE_ROOT when set, else a
+    directory named `reference` beside this repository (absent on machines
+    that only run the device tests, where load() returns None)."""
+    env = os.environ.get("HMCLAB_REFERENCE_ROOT")
+    if env:
+        return env
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    return os.path.join(os.path.dirname(repo), "reference")
+
+
+REFERENCE_ROOT = _reference_root()
 
 _STUBBED = [
     "h5py",

@@ -3,8 +3,9 @@
 oracle (GPU).
 
 Tolerances: oracle gradient vs central differences 1e-6 relative (FP64);
-FP32 device misfits vs the FP64 oracle 2e-5 relative; FP32 device gradients
-vs the FP64 oracle 2e-5 of the gradient scale (measured ~2e-6)."""
+FP32 device misfits vs the FP64 oracle 1e-5 relative; FP32 device gradients
+vs the FP64 oracle 1e-5 of the gradient scale (measured ~2e-6 here and at
+the full 240 x 140-cell, 1500-step grid, tests/test_gpu_fullsize.py)."""
 import numpy as np
 import pytest
 
@@ -97,12 +98,12 @@ def test_device_fwi_matches_oracle():
             for f in range(3):
                 gv[f] += gk[f]
         # device records of chain c agree with the oracle's
-        np.testing.assert_allclose(x[c], chi, rtol=2e-5)
+        np.testing.assert_allclose(x[c], chi, rtol=1e-5)
         g_ref = np.concatenate([Bs.T @ gv[1].reshape(-1), Bs.T @ gv[2].reshape(-1), Bs.T @ gv[0].reshape(-1)])
         scale = np.abs(g_ref).max()
         err = np.abs(g[:, c] - g_ref).max() / scale
         print(f"chain {c}: misfit {x[c]:.6e} vs oracle {chi:.6e}; gradient max rel err {err:.2e}")
-        assert err < 2e-5
+        assert err < 1e-5
 
 
 @pytest.mark.gpu
@@ -146,4 +147,4 @@ def test_device_fwi_staged_tiles_match_direct_loads():
     m32 = Md[:, 0].double().cpu().numpy()
     vp, vs, rho = (cfg.extend(f) for f in dists[0].fine_model(m32))
     chi = sum(s.gradient(rho, vp, vs, obs[k][0], obs[k][1], dists[0].weight)[0] for k, s in enumerate(shots))
-    np.testing.assert_allclose(x[0][0], chi, rtol=2e-5)
+    np.testing.assert_allclose(x[0][0], chi, rtol=1e-5)

@@ -51,6 +51,11 @@ def test_noalloc_matches_allocating_entry_point_twice(dtype, code_name, rtol):
         assert rc == 0, _lib.last_error()
         torch.cuda.synchronize()
         np.testing.assert_allclose(out.cpu().numpy(), ref.cpu().numpy(), rtol=rtol, err_msg=f"call {call}")
+        # and against the misfit in FP64 on the host, from the same (rounded) inputs
+        Gh, Mh = G.double().cpu().numpy(), M.double().cpu().numpy()
+        r = Gh @ Mh - data.double().cpu().numpy()[:, None]
+        x64 = 0.5 * np.sum(r * r * iv.double().cpu().numpy()[:, None], axis=0)
+        np.testing.assert_allclose(out.cpu().numpy(), x64, rtol=rtol, err_msg=f"call {call} vs FP64 host misfit")
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
