@@ -348,11 +348,17 @@ class SrclocWorkload:
 # ---------------------------------------------------------------------------
 # Workload: 2-D elastic FWI, surrogate-driven vs plain batched HMC, 64 chains
 # ---------------------------------------------------------------------------
-# Plain-HMC min-ESS per chain-proposal on the FWI workload, measured by this
-# bench's GPU arm (the `plain.ess_per_chain_proposal` field of its line); the
-# reference arm, which can only afford to time the CPU cost of a proposal,
-# converts that cost into min-ESS/s with it.
-FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL = 0.203
+# The FWI workload's reference run: one long plain-HMC run on the GPU
+# (tests/golden/make_fwi_reference.py) gives the posterior moments the
+# surrogate-driven run is judged against, plain HMC's ESS per chain-proposal
+# with lag windows that truncate, and posterior draws the chains start from.
+FWI_REFERENCE = os.path.join(ROOT, "tests", "golden", "fwi_reference.npz")
+# Validity of the headline: at least this fraction of the parameters' ESS lag
+# windows must truncate (Geyer), and the surrogate run's posterior means and
+# standard deviations must agree with the reference run's within their joint
+# Monte Carlo error (|z| at most this, over all 600 parameters)
+FWI_MIN_TRUNCATED = 0.95
+FWI_MAX_Z = 4.5
 # DRAM bytes (read + write) of one forward time step at C = 64 from one ncu
 # capture of velocity_tma_kernel (60.5 + 0.4 MB) and stress_tma_kernel
 # (69.0 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
@@ -369,10 +375,12 @@ class FwiWorkload:
     stepsize = 0.12  # prior-whitened units: the mass matrix is the prior precision
     noise_fraction = 10.0  # data noise std / RMS of the true records
     hidden = (512, 512)
-    # 300 surrogate proposals: the slowest parameters of the surrogate run
-    # decorrelate over tens of proposals, and the ESS lag window (K/2) must
-    # reach past them
-    default_steps, default_warmup = 300, 12
+    # a step is one block of `block` surrogate-driven proposals of every
+    # chain; 20 steps = 320 proposals, so that the ESS lag windows of the
+    # surrogate run can reach past its slowest parameters' autocorrelation
+    default_steps, default_warmup = 20, 3
+    block = 16
+    burn_in = 12  # exact proposals recording (position, gradient) training pairs
 
     def __init__(self, seed=0, chains=None):
         from hmclab_gb300 import fwi as F
@@ -685,15 +693,70 @@ def run_gpu_arm(args, wl):
 
 
 # ---------------------------------------------------------------------------
-def fwi_cpu_costs(wl, cores):
-    """Seconds of one forward and one forward+adjoint shot of the FP64 C
-    restatement (oracle/fwi_oracle.c) on the full grid, `cores` shots at once
-    on a spawn process pool (one task per core); returns the medians and the
-    wall time."""
+def load_fwi_reference(wl, path=None):
+    """The FWI reference run's fixture as a dict, or None (with the reason)
+    when it is missing or was made for other workload settings."""
+    path = path or FWI_REFERENCE
+    if not os.path.exists(path):
+        return None, f"no reference fixture ({os.path.relpath(path, ROOT)})"
+    ref = dict(np.load(path))
+    want = {"chains": wl.chains, "leapfrog_steps": wl.L, "stepsize": wl.stepsize,
+            "noise_fraction": wl.noise_fraction, "seed": wl.seed}
+    for k, v in want.items():
+        if not np.isclose(float(ref[k]), float(v)):
+            return None, f"reference fixture made for {k} = {float(ref[k])}, workload has {v}"
+    return ref, None
+
+
+def moment_check(mean, std, ess, ref):
+    """Posterior moments of a run against the reference run's: the largest
+    differences in units of the reference std, and z-scores against the
+    joint Monte Carlo error (std^2 / ESS of each run for means; std^2 / (2 ESS)
+    for standard deviations).  For unbiased chains |z| ~ N(0, 1)."""
+    rm, rs, re = ref["mean"], ref["std"], np.maximum(np.abs(ref["ess"]), 1.0)
+    e = np.maximum(np.abs(ess), 1.0)
+    z_mean = (mean - rm) / np.sqrt(std**2 / e + rs**2 / re)
+    z_std = (std - rs) / np.sqrt(std**2 / (2 * e) + rs**2 / (2 * re))
+    return {"mean": float(np.max(np.abs(mean - rm) / rs)), "std": float(np.max(np.abs(std - rs) / rs)),
+            "mc_floor": float(1.0 / np.sqrt(e.min())), "mean_z_max": float(np.abs(z_mean).max()),
+            "std_z_max": float(np.abs(z_std).max()), "mean_z_frac_above_3": float(np.mean(np.abs(z_mean) > 3)),
+            "within_2pct_of_reference_std": bool(np.max(np.abs(mean - rm) / rs) <= 0.02
+                                                 and np.max(np.abs(std - rs) / rs) <= 0.02)}
+
+
+def fwi_validity(ess_raw, mc):
+    """Reasons the surrogate run's min-ESS/s is not a valid headline (empty
+    when it is): lag windows that did not truncate, or moments inconsistent
+    with the reference run."""
+    reasons = []
+    truncated = float(np.mean(np.asarray(ess_raw) >= 0))
+    if truncated < FWI_MIN_TRUNCATED:
+        reasons.append(f"only {truncated:.2f} of the parameters' ESS lag windows truncated (need "
+                       f"{FWI_MIN_TRUNCATED}): the run is too short for its autocorrelation")
+    if mc is None:
+        reasons.append("no reference moments to check the run against")
+    elif max(mc["mean_z_max"], mc["std_z_max"]) > FWI_MAX_Z:
+        reasons.append(f"moments disagree with the reference run beyond Monte Carlo error (max |z| "
+                       f"{max(mc['mean_z_max'], mc['std_z_max']):.1f} > {FWI_MAX_Z})")
+    return reasons
+
+
+def _fwi_shot_task(task):
+    """One full-size shot of the FP64 C restatement: (forward seconds,
+    forward + adjoint seconds); a process-pool task."""
+    from oracle import fwi as OF
+
+    return OF.timed_shot(task)
+
+
+def fwi_cpu_shots(wl, cores, shots_per_core=1):
+    """Run `shots_per_core` forward + adjoint shots of the FP64 C restatement
+    (oracle/fwi_oracle.c) on every host core at once (spawn pool, one shot
+    per task, each on its own chain's model); returns per-shot forward and
+    forward + adjoint seconds (medians) and the wall time."""
     import multiprocessing as mp
 
     from oracle import build_oracle
-    from oracle import fwi as OF
     from hmclab_gb300 import fwi as F
 
     build_oracle.build()
@@ -701,54 +764,59 @@ def fwi_cpu_costs(wl, cores):
     bg = F.layered_model(cfg, anomalies=True)
     vp, vs, rho = (cfg.extend(f) for f in bg)
     tasks = [(cfg.nxc, cfg.nzc, cfg.nt, cfg.h, cfg.dt, cfg.taper(), cfg.ricker(), cfg.src[k % cfg.n_shots],
-              cfg.rec_x, cfg.rec_z, rho, vp, vs) for k in range(cores)]
+              cfg.rec_x, cfg.rec_z, rho, vp, vs) for k in range(cores * shots_per_core)]
     t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(OF.timed_shot, tasks)
+        res = pool.map(_fwi_shot_task, tasks, chunksize=1)
     wall = time.perf_counter() - t0
     return float(np.median([r[0] for r in res])), float(np.median([r[1] for r in res])), wall
 
 
-def fwi_cpu_rate(wl, cores):
-    """CPU chain-proposals/s of plain HMC on the FWI workload: L exact
-    gradients (4 shots forward + adjoint) plus one misfit (4 forward shots)
-    per chain-proposal, one chain per core."""
-    t_fwd, t_grad, wall = fwi_cpu_costs(wl, cores)
-    per_chain_proposal = wl.cfg.n_shots * (wl.L * t_grad + t_fwd)
-    return cores / per_chain_proposal, t_fwd, t_grad, wall
+def fwi_cpu_rate(wl, t_fwd, t_grad, cores):
+    """Plain-HMC chain-proposals/s of the CPU path, one chain per core: a
+    proposal is L exact gradients (4 shots forward + adjoint) and one misfit
+    (4 forward shots)."""
+    return cores / (wl.cfg.n_shots * (wl.L * t_grad + t_fwd))
 
 
 def run_fwi_reference_arm(args, wl):
+    """Plain HMC's hot path on the host cores: the FP64 C restatement of the
+    elastic stencils, one chain per core.  A step is one forward + adjoint
+    shot of every core's chain (a bounded sample of a proposal, which is
+    4 shots x (10 gradients + 1 misfit)); min-ESS/s converts the measured
+    chain-proposals/s with plain HMC's ESS per chain-proposal from the
+    reference run (the same algorithm on the GPU; a CPU run long enough to
+    estimate it takes hours)."""
     cores = os.cpu_count()
-    rate, t_fwd, t_grad, wall = fwi_cpu_rate(wl, cores)
-    e = FWI_PLAIN_ESS_PER_CHAIN_PROPOSAL
+    ref, why = load_fwi_reference(wl)
+    t_fwd, _, _ = fwi_cpu_shots(wl, cores)  # warm-up step, also gives the forward cost
+    for _ in range(args.warmup - 1):
+        fwi_cpu_shots(wl, cores)
+    per_step, grads = [], []
+    for _ in range(args.steps):
+        _, tg, wall = fwi_cpu_shots(wl, cores)
+        per_step.append(wall)
+        grads.append(tg)
+    t_grad = float(np.median(grads))
+    rate = fwi_cpu_rate(wl, t_fwd, t_grad, cores)
+    e = float(ref["ess_per_chain_proposal"]) if ref is not None else None
     value = rate * e if e is not None else None
-    sample = (f"{cores} full-size shots (forward {t_fwd:.2f} s, forward+adjoint {t_grad:.2f} s each, FP64 C "
-              f"restatement, one per core, {wall:.1f} s wall); chain-proposals/s = cores / (4 shots x (L x "
-              f"gradient + misfit)) = {rate:.4g}, times the plain-HMC min-ESS per chain-proposal measured on "
-              f"the GPU ({e})")
+    sample = (f"{args.steps} steps of one full-size forward + adjoint shot per core ({cores} cores, FP64 C "
+              f"restatement; forward {t_fwd:.2f} s, forward + adjoint {t_grad:.2f} s per shot); chain-proposals/s "
+              f"= cores / (4 shots x (L x gradient + misfit)) = {rate:.4g}, times plain HMC's min-ESS per "
+              f"chain-proposal from the reference run ({e})")
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": 1, "warmup": 0,
-        "ms_per_step": 1e3 * wl.chains / rate, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "impl": "reference", "config": wl.config(),
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(per_step)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": wl.config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "chain_proposals_per_s": rate,
+        "chain_proposals_per_s": rate, "ess_per_chain_proposal": e,
     }
+    if why:
+        line["reason"] = why
     print(json.dumps(line))
-
-
-def timed_proposals(smp, K, flush, evs):
-    import torch
-
-    for k in range(K):
-        with torch.cuda.stream(smp.stream):
-            flush.fill_(float(k))
-            evs[k][0].record(smp.stream)
-        smp.run(1)
-        evs[k][1].record(smp.stream)
-    smp.stream.synchronize()
-    return sum(a.elapsed_time(b) for a, b in evs) / 1e3
 
 
 def forward_step_timing(lik, smp, n_iter=2):
@@ -799,20 +867,24 @@ def run_fwi_arm(args, wl):
     wl.build()
     post, lik = wl.posterior(), wl.pb["likelihood"]
     d, C, L = wl.d, wl.chains, wl.L
-    K, W, Kp = args.steps, args.warmup, args.plain_steps
+    K, W, B, Kp, Nb = args.steps, args.warmup, args.block, args.plain_steps, args.burn_in
+    ref, ref_why = load_fwi_reference(wl)
+    # chains start at the reference run's final states (posterior draws): a
+    # converged exact burn-in, which this bench cannot afford to repeat
+    q_init = ref["q_final"] if ref is not None else wl.q0
     kw = wl.sampler_kwargs()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t_setup = time.perf_counter() - t_setup
 
-    # ---- exact burn-in, recording (position, gradient) pairs -------------
-    data = S.TrainingSet(d, W * L * C)
+    # ---- exact proposals from the start states, recording training pairs --
+    data = S.TrainingSet(d, Nb * L * C)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=wl.q0, proposals=W,
+    burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=q_init, proposals=Nb,
                                                                      training_set=data, **kw)
     t_burn = time.perf_counter() - t0
     q_start = burn.current_model
-    acc_burn = float(np.mean(burn.accepted_proposals) / W)
+    acc_burn = float(np.mean(burn.accepted_proposals) / Nb)
 
     # ---- surrogate training on the device ---------------------------------
     kind = S.PotentialSurrogate if args.surrogate == "potential" else S.MLPSurrogate
@@ -825,10 +897,10 @@ def run_fwi_arm(args, wl):
     net.freeze()
 
     # ---- pilot (untimed): the surrogate run's trajectory ------------------
-    # A few proposals per (L, stepsize) from the burn-in end states; the
-    # setting with the largest acceptance x (trajectory length)^2 — the
-    # diffusive-regime gain per proposal, length capped at the plain run's —
-    # is used for the timed run.  --surrogate-L / --surrogate-stepsize fix it.
+    # A few proposals per (L, stepsize) from the start states; the setting
+    # with the largest acceptance x (trajectory length)^2 — the diffusive-
+    # regime gain per proposal, length capped at the plain run's — is used
+    # for the timed run.  --surrogate-L / --surrogate-stepsize fix it.
     pilot = []
     if args.surrogate_L is None or args.surrogate_stepsize is None:
         tau_max = wl.stepsize * wl.L
@@ -844,70 +916,76 @@ def run_fwi_arm(args, wl):
         L_best, eps_best = choose_trajectory(pilot)
     else:
         L_best, eps_best = args.surrogate_L, args.surrogate_stepsize
-
-    # ---- timed: surrogate-driven HMC --------------------------------------
     kw_s = dict(kw, amount_of_steps=L_best, stepsize=eps_best)
 
-    def timed_run(seed, n, surrogate):
-        smp = H.Samplers.HMC(seed=seed)
-        smp.prepare(None, post, initial_model=q_start, proposals=n, keep_samples=True, surrogate=surrogate,
-                    **(kw_s if surrogate is not None else kw))
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
-        torch.cuda.synchronize()
-        l0 = _lib.launch_count()
-        t = timed_proposals(smp, n, flush, evs)
-        launches = _lib.launch_count() - l0
-        return smp, t, launches, [a.elapsed_time(b) / 1e3 for a, b in evs]
-
+    # ---- surrogate-driven HMC: W untimed blocks, then K timed blocks -------
+    smp_s = H.Samplers.HMC(seed=sharding.rank_seed(200, rank))
+    smp_s.prepare(None, post, initial_model=q_start, proposals=(W + K) * B, keep_samples=True, surrogate=net,
+                  **kw_s)
+    smp_s.run(W * B)
+    smp_s.stream.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    smp_s, t_s, launches, _ = timed_run(sharding.rank_seed(200, rank), K, net)
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    for k in range(K):
+        with torch.cuda.stream(smp_s.stream):
+            flush.fill_(float(k))
+            evs[k][0].record(smp_s.stream)
+        smp_s.run(B)
+        evs[k][1].record(smp_s.stream)
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
+    t_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     t_step = forward_step_timing(lik, smp_s)
     smp_s.finish()
-    qs = smp_s.samples_device[0]  # [K][d][C]
-    ess_s_raw = diagnostics.ess(qs, lags=min(K // 2, 200))
-    ess_s = np.abs(ess_s_raw)
-    acc_s = float(np.mean(smp_s.accepted_proposals) / K)
-
-    # ---- timed: plain HMC (exact gradients), same start -------------------
-    smp_p, t_p, _, per_p = timed_run(sharding.rank_seed(300, rank), Kp, None)
-    smp_p.finish()
-    qp = smp_p.samples_device[0]
-    ess_p_raw = diagnostics.ess(qp, lags=max(2, Kp // 2))
-    ess_p = np.abs(ess_p_raw)
-    acc_p = float(np.mean(smp_p.accepted_proposals) / Kp)
-    # rank-normalised bulk-ESS of the same draws, reported beside the headline
-    bulk_s = np.abs(diagnostics.ess(qs, lags=min(K // 2, 200), rank_normalize=True))
-    bulk_p = np.abs(diagnostics.ess(qp, lags=max(2, Kp // 2), rank_normalize=True))
+    qs = smp_s.samples_device[0][W * B:]  # [K*B][d][C]
+    N = qs.shape[0]
+    ess_s_raw = diagnostics.ess(qs, lags=min(N // 2, 200))
+    acc_s = float(np.mean(smp_s.accepted_proposals) / ((W + K) * B))
+    bulk_s = np.abs(diagnostics.ess(qs, lags=min(N // 2, 200), rank_normalize=True))
+    ess_s, t_s = sharding.combine_ess(np.abs(ess_s_raw), t_s)
     bulk_s, _ = sharding.combine_ess(bulk_s, t_s)
-    bulk_p, _ = sharding.combine_ess(bulk_p, t_p)
-    ess_s, t_s = sharding.combine_ess(ess_s, t_s)
-    ess_p, t_p = sharding.combine_ess(ess_p, t_p)
-    value = float(ess_s.min() / t_s)
-    plain_value = float(ess_p.min() / t_p)
-    mean_s, std_s = sharding.combine_moments(*diagnostics.moments(qs), K * C)
-    mean_p, std_p = sharding.combine_moments(*diagnostics.moments(qp), Kp * C)
-    me, se = diagnostics.moment_error(mean_s, std_s, mean_p, std_p)
-    # the same posterior mean in both runs? z = difference / its Monte Carlo
-    # standard error (std / sqrt(ESS) per run); for exact chains |z| ~ N(0, 1)
-    se_mean = np.sqrt(std_s**2 / np.maximum(ess_s, 1.0) + std_p**2 / np.maximum(ess_p, 1.0))
-    z = np.abs(mean_s - mean_p) / np.maximum(se_mean, 1e-300)
-    e_plain = float(ess_p.min() / (C * world * Kp))
+    mean_s, std_s = sharding.combine_moments(*diagnostics.moments(qs), N * C)
+    mc = moment_check(mean_s, std_s, ess_s, ref) if ref is not None else None
+    reasons = fwi_validity(ess_s_raw, mc)
+    if ref_why:
+        reasons.insert(0, ref_why)
+    value_measured = float(ess_s.min() / t_s)
+    value = value_measured if not reasons else None
+
+    # ---- plain HMC (exact gradients): its cost per proposal, timed ---------
+    smp_p = H.Samplers.HMC(seed=sharding.rank_seed(300, rank))
+    smp_p.prepare(None, post, initial_model=q_start, proposals=Kp, keep_samples=False, **kw)
+    evp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kp)]
+    for k in range(Kp):
+        with torch.cuda.stream(smp_p.stream):
+            flush.fill_(float(k))
+            evp[k][0].record(smp_p.stream)
+        smp_p.run(1)
+        evp[k][1].record(smp_p.stream)
+    smp_p.stream.synchronize()
+    t_p = sum(a.elapsed_time(b) for a, b in evp) / 1e3
+    smp_p.finish()
+    acc_p = float(np.mean(smp_p.accepted_proposals) / Kp)
+    e_plain = float(ref["ess_per_chain_proposal"]) if ref is not None else None
+    plain_value = e_plain * C * world * Kp / t_p if e_plain is not None else None
 
     # ---- end to end through the public API with host buffers -------------
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     smp_e = H.Samplers.HMC(seed=sharding.rank_seed(400, rank)).sample(
-        None, post, initial_model=q_start, proposals=K, keep_samples=True, surrogate=net, **kw_s)
+        None, post, initial_model=q_start, proposals=K * B, keep_samples=True, surrogate=net, **kw_s)
     host_q, host_x = smp_e.samples_host()
     t_e2e = time.perf_counter() - t0
-    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K // 2, 200)))
-    e2e_value = float(ess_e.min() / t_e2e)
+    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K * B // 2, 200)))
+    e2e_measured = float(ess_e.min() / t_e2e)
 
     hbm, bf16, bf16s, src = peaks()
     achieved = wl.stencil_bytes_per_step() / t_step / 1e9
@@ -915,35 +993,33 @@ def run_fwi_arm(args, wl):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded; records from the device forward of the true model + noise)",
-        "config": wl.config(),
-        "speedup_vs_plain": float(value / plain_value),
+        "config": {**wl.config(), "step": f"{B} surrogate-driven proposals of every chain",
+                   "start": "posterior draws: final states of the reference plain-HMC run"
+                            if ref is not None else "m_true + 0.3 prior std (no reference run)"},
+        "valid": not reasons, "invalid_reasons": reasons, "value_measured": value_measured,
+        "speedup_vs_plain": float(value_measured / plain_value) if plain_value else None,
         "including_burn_in_and_training": {
             "value": float(ess_s.min() / (t_burn + t_train + t_s)),
-            "plain_value": float(ess_p.min() / (t_burn + t_p)),
-            "note": "min-ESS over (exact burn-in + surrogate training + sampling) seconds; plain over "
-                    "(the same burn-in + its sampling)"},
-        # parameters whose autocorrelation sum the lag window cut before
-        # Geyer's truncation point: their ESS is an upper estimate
-        "ess_window_not_truncated": {"surrogate": float(np.mean(ess_s_raw < 0)),
-                                     "plain": float(np.mean(ess_p_raw < 0))},
-        "rank_normalised_bulk": {"value": float(bulk_s.min() / t_s), "plain_value": float(bulk_p.min() / t_p),
-                                 "speedup_vs_plain": float((bulk_s.min() / t_s) / (bulk_p.min() / t_p))},
+            "note": "min-ESS over (exact training-pair proposals + surrogate training + sampling) seconds"},
+        "ess_window_truncated": float(np.mean(ess_s_raw >= 0)), "proposals_per_chain": N,
+        "rank_normalised_bulk": {"value": float(bulk_s.min() / t_s)},
         "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
                                                       "pilot": [[L_, e_, round(a_, 4)] for _, L_, e_, a_ in pilot]},
-        "plain": {"value": plain_value, "steps": Kp, "ms_per_step": 1e3 * t_p / Kp, "acceptance": acc_p,
-                  "ess_per_chain_proposal": e_plain},
-        "moment_error_vs_plain": {"mean": me, "std": se,
-                                  "mc_floor": float(1.0 / np.sqrt(max(1.0, ess_p.min()))),
-                                  "mean_z_max": float(z.max()), "mean_z_frac_above_3": float(np.mean(z > 3.0))},
-        "burn_in": {"proposals": W, "seconds": t_burn, "acceptance": acc_burn, "pairs": data.count},
-        "surrogate": {"kind": args.surrogate, "train_steps": args.train_steps, "train_seconds": t_train, "train_pairs": fit["train_pairs"],
-                      "heldout_pairs": fit["heldout_pairs"], "loss_first": fit["history"][0][1],
-                      "loss_last": fit["history"][-1][1], "heldout_rel_error_linear_start": fit["heldout"][0][1],
-                      "heldout_rel_error": fit["best_heldout"], "best_step": fit["best_step"],
-                      "heldout_curve": [[k, round(e, 5)] for k, e in fit["heldout"]]},
+        "plain": {"value": plain_value, "proposals_timed": Kp, "ms_per_proposal": 1e3 * t_p / Kp,
+                  "acceptance": acc_p, "ess_per_chain_proposal": e_plain,
+                  "ess_source": "reference plain-HMC run (tests/golden/fwi_reference.npz): "
+                                f"{int(ref['proposals']) if ref is not None else 0} proposals x {C} chains, "
+                                "lag windows truncated"},
+        "moment_error_vs_reference": mc,
+        "training_proposals": {"proposals": Nb, "seconds": t_burn, "acceptance": acc_burn, "pairs": data.count},
+        "surrogate": {"kind": args.surrogate, "train_steps": args.train_steps, "train_seconds": t_train,
+                      "train_pairs": fit["train_pairs"], "heldout_pairs": fit["heldout_pairs"],
+                      "heldout_rel_error_linear_start": fit["heldout"][0][1], "heldout_rel_error": fit["best_heldout"],
+                      "best_step": fit["best_step"]},
         "setup_seconds": t_setup,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(q_start.size * 8 / K),
-                "d2h_bytes_per_step": int(d * C * 4 + C * 8), "seconds": t_e2e},
+        "e2e": {"value": e2e_measured if not reasons else None, "value_measured": e2e_measured, "unit": UNIT,
+                "h2d_bytes_per_step": int(q_start.size * 8 / K), "d2h_bytes_per_step": int(B * (d * C * 4 + C * 8)),
+                "seconds": t_e2e},
         "gpu_launches": int(launches),
         "roofline": {"kernel": "fwi forward time step: velocity_tma_kernel + stress_tma_kernel (the exact misfit)",
                      "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -960,16 +1036,146 @@ def run_fwi_arm(args, wl):
                                        "FP32 accumulate")
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count()
-        rate, t_fwd, t_grad, wall = fwi_cpu_rate(wl, cores)
+        t_fwd, t_grad, wall = fwi_cpu_shots(wl, cores)
+        rate = fwi_cpu_rate(wl, t_fwd, t_grad, cores)
         line["cpu_baseline"] = {
-            "value": rate * e_plain, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"{cores} full-size shots of the FP64 C restatement, one per core ({wall:.1f} s wall; "
-                       f"forward {t_fwd:.2f} s, forward+adjoint {t_grad:.2f} s); chain-proposals/s = {rate:.4g} "
-                       f"times the plain-HMC min-ESS per chain-proposal of this run ({e_plain:.4g})")}
+            "value": rate * e_plain if e_plain is not None else None, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"one full-size forward + adjoint shot of the FP64 C restatement per core ({wall:.1f} s wall; "
+                       f"forward {t_fwd:.2f} s, forward + adjoint {t_grad:.2f} s per shot); chain-proposals/s = "
+                       f"{rate:.4g} times plain HMC's min-ESS per chain-proposal from the reference run ({e_plain})")}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# Profiling cases: small, self-contained runs of the hot-path kernels
+#
+#   python bench.py --profile-case fwi-gradient [--nt 100] [--chains 64] [--repeat 2]
+#   python bench.py --profile-case fwi-misfit   [--nt 100] [--chains 64] [--repeat 2]
+#   python bench.py --profile-case mlp          [--chains 64] [--repeat 3]
+#   python bench.py --profile-case potential    [--chains 64] [--repeat 3]
+#   python bench.py --profile-case persistent   [--chains 4096] [--repeat 2]
+#   python bench.py --profile-case tomo         [--chains 1024] [--repeat 2]
+#   python bench.py --profile-case srcloc       [--chains 8192] [--repeat 2]
+#
+# The FWI cases build the workload's full spatial grid (200x100 cells plus
+# the 20-cell sponge, 4 shots, 600 blob parameters) with a shortened record
+# (`--nt` time steps) so that a profiler capture of every launch of one
+# gradient stays small, run the evaluation `--repeat` times and synchronise.
+# `mlp` runs the surrogate's training step (batch 256) and its sampler-side
+# prediction for 600 parameters; `potential` the same for the scalar-potential
+# surrogate (gradient pass and double backpropagation).  `persistent` runs
+# blocks of 10 proposals of a d = 50 dense linear-Gaussian posterior (FP32,
+# 10 leapfrog steps) through the persistent kernel; `tomo` and `srcloc`
+# evaluate the gradient of the tomography (64 x 64 cells, 2000 rays) and
+# source-location (32 events, 200 stations) posteriors.
+# ---------------------------------------------------------------------------
+PROFILE_CASES = ("fwi-gradient", "fwi-misfit", "mlp", "potential", "persistent", "tomo", "srcloc")
+
+
+def _profile_fwi(nt, chains):
+    import numpy as np
+    import torch
+
+    from hmclab_gb300 import fwi as F
+    from hmclab_gb300 import problems
+
+    cfg = F.ElasticConfig(nt=nt)
+    pb = problems.elastic_fwi(cfg, 20, 10, prior_fraction=0.1, noise_fraction=10.0, seed=0)
+    rng = np.random.default_rng(1)
+    q = pb["m_true"][:, None] + 0.3 * pb["prior_std"][:, None] * rng.normal(size=(pb["m_true"].size, chains))
+    return pb["posterior"], torch.from_numpy(q).float().cuda().contiguous()
+
+
+def run_profile_case(a):
+    """--profile-case: a small, self-contained run of one hot-path kernel for
+    an ncu capture (see PROFILE_CASES); prints one status line, no JSON."""
+    import torch
+
+    torch.cuda.set_device(0)
+    a.chains = a.chains or (4096 if a.profile_case == "persistent" else 1024 if a.profile_case == "tomo"
+                            else 8192 if a.profile_case == "srcloc" else 64)
+    a.case = a.profile_case
+    if a.case.startswith("fwi"):
+        post, q = _profile_fwi(a.nt, a.chains)
+        out = torch.empty_like(q)
+        x = torch.empty(a.chains, dtype=torch.float64, device="cuda")
+        t0 = time.perf_counter()
+        for _ in range(a.repeat):
+            if a.case == "fwi-gradient":
+                post.gradient_batch(q, out=out)
+            else:
+                post.misfit_batch(q, out=x)
+        torch.cuda.synchronize()
+        print(f"{a.case}: nt={a.nt} chains={a.chains} repeat={a.repeat} {time.perf_counter() - t0:.3f} s")
+    elif a.case == "persistent":
+        import numpy as np
+
+        import hmclab_gb300 as H
+
+        d = 50
+        rng = np.random.default_rng(0)
+        G = rng.normal(size=(2 * d, d)) / np.sqrt(d)
+        dat = G @ rng.normal(size=(d, 1)) + 0.1 * rng.normal(size=(2 * d, 1))
+        post = H.Distributions.BayesRule([H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1))),
+                                          H.Distributions.LinearMatrix(G, dat, 0.01, dtype=np.float64)])
+        w = np.sqrt(np.linalg.eigvalsh(G.T @ G / 0.01).max())
+        smp = H.Samplers.HMC(seed=1).prepare(None, post, stepsize=0.5 / w, amount_of_steps=10,
+                                            proposals=10 * (a.repeat + 1), chains=a.chains, dtype="float32",
+                                            proposals_per_graph=10, persistent=True)
+        smp.run(10 * (a.repeat + 1))
+        smp.finish()
+        print(f"persistent: d={d} chains={a.chains} warps={smp._persistent.warps} ok")
+    elif a.case in ("tomo", "srcloc"):
+        import numpy as np
+
+        import hmclab_gb300 as H
+        from hmclab_gb300 import problems
+
+        rng = np.random.default_rng(0)
+        if a.case == "tomo":
+            t = problems.tomography(64, 64, 2000, 1.0, 0.01, 0)
+            post = H.Distributions.BayesRule([H.Distributions.Normal(t["background"], np.full((4096, 1), 0.0025)),
+                                              H.Distributions.LinearMatrix(t["G"], t["d"], 1e-4)])
+            q = t["m_true"] + 0.01 * rng.normal(size=(4096, a.chains))
+        else:
+            t = problems.source_location(32, 200, 40.0, 10.0, 5.0, 0.05, 0)
+            post = H.Distributions.SourceLocation3D(t["rx"], t["ry"], t["rz"], t["obs"], 0.05)
+            q = t["m_true"] + 0.01 * rng.normal(size=(t["m_true"].size, a.chains))
+        M = torch.from_numpy(q).float().cuda().contiguous()
+        out = torch.empty_like(M)
+        for _ in range(a.repeat):
+            post.gradient_batch(M, out=out)
+        torch.cuda.synchronize()
+        print(f"{a.case}: chains={a.chains} repeat={a.repeat} ok")
+    else:
+        import numpy as np
+
+        from hmclab_gb300 import surrogate as S
+
+        d = 600
+        kind = S.PotentialSurrogate if a.case == "potential" else S.MLPSurrogate
+        net = kind(d, hidden=(512, 512), seed=0)
+        data = S.TrainingSet(d, 4096)
+        rng = np.random.default_rng(0)
+        st = torch.cuda.current_stream().cuda_stream
+        for k in range(4):
+            qb = torch.from_numpy(rng.normal(size=(d, 1024))).float().cuda()
+            data.record(qb, 2.0 * qb + torch.tanh(qb), st)
+        net.fit_normalization(data)
+        for _ in range(a.repeat):
+            net.train_step(data, rng.integers(0, 4096, size=256), lr=1e-3)
+        torch.cuda.synchronize()
+        net.freeze()
+        q = torch.from_numpy(rng.normal(size=(d, a.chains))).float().cuda()
+        g = torch.empty_like(q)
+        for _ in range(a.repeat):
+            net.predict_into(q, g, st)
+        torch.cuda.synchronize()
+        net.check_status()
+        print(f"{a.case}: d={d} hidden=512x512 batch=256 chains={a.chains} repeat={a.repeat} ok")
 
 
 def main():
@@ -979,7 +1185,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
-    ap.add_argument("--plain-steps", type=int, default=16, help="fwi: timed proposals of plain HMC")
+    ap.add_argument("--plain-steps", type=int, default=3, help="fwi: timed proposals of plain HMC (its cost)")
+    ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
+    ap.add_argument("--burn-in", type=int, default=None,
+                    help="fwi: exact proposals recording the surrogate's training pairs (independent of --warmup)")
     ap.add_argument("--train-steps", type=int, default=10000, help="fwi: Adam steps of the surrogate")
     ap.add_argument("--surrogate", default="potential", choices=["potential", "gradient"],
                     help="fwi: scalar-potential network (conservative field) or a network that outputs the gradient")
@@ -990,10 +1199,21 @@ def main():
     ap.add_argument("--cpu-chains", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", default=None, choices=PROFILE_CASES,
+                    help="run one small profiling case instead of a benchmark (no JSON line)")
+    ap.add_argument("--nt", type=int, default=100, help="profiling: time steps of the FWI cases")
+    ap.add_argument("--chains", type=int, default=None, help="profiling: chains of the case")
+    ap.add_argument("--repeat", type=int, default=2, help="profiling: evaluations of the case")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     wl = WORKLOADS[args.workload]()
     args.steps = wl.default_steps if args.steps is None else args.steps
     args.warmup = wl.default_warmup if args.warmup is None else args.warmup
+    if args.workload == "fwi":
+        args.block = wl.block if args.block is None else args.block
+        args.burn_in = wl.burn_in if args.burn_in is None else args.burn_in
     assert args.warmup >= 3, "at least 3 warm-up steps"
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

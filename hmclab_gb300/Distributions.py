@@ -174,51 +174,43 @@ class _AbstractDistribution:
         raise NotImplementedError()
 
     def corrector(self, coordinates: _numpy.ndarray, momentum: _numpy.ndarray):
-        """Reflect at the bounds in place (reference `base.py:239-270`).  The
+        """Mirror every coordinate that crossed a bound back inside it and
+        reverse its momentum, in place (the reference's contract,
+        `base.py:239-270`: the lower bound first, then the upper one).  The
         sampler applies the same rule on the device after every drift."""
-        if self.lower_bounds is not None:
-            too_low = coordinates < self.lower_bounds
-            coordinates[too_low] += 2 * (self.lower_bounds[too_low] - coordinates[too_low])
-            momentum[too_low] *= -1.0
-        if self.upper_bounds is not None:
-            too_high = coordinates > self.upper_bounds
-            coordinates[too_high] += 2 * (self.upper_bounds[too_high] - coordinates[too_high])
-            momentum[too_high] *= -1.0
+        for bound, crossed in ((self.lower_bounds, _numpy.less), (self.upper_bounds, _numpy.greater)):
+            if bound is None:
+                continue
+            hit = crossed(coordinates, bound)
+            coordinates[hit] += 2 * (bound[hit] - coordinates[hit])
+            momentum[hit] *= -1.0
 
     def update_bounds(self, lower=None, upper=None):
-        """Set bounds with the reference's validation (`base.py:272-359`)."""
-        old = (self.lower_bounds, self.upper_bounds)
-        if type(upper) == list:
-            upper = _numpy.array(upper)[:, None]
-        if type(lower) == list:
-            lower = _numpy.array(lower)[:, None]
-        self.upper_bounds, self.lower_bounds = upper, lower
-        if lower is not None and type(lower) is not _numpy.ndarray:
-            self.lower_bounds, self.upper_bounds = old
-            raise ValueError("Lower bounds object not understood.")
-        if upper is not None and type(upper) is not _numpy.ndarray:
-            self.lower_bounds, self.upper_bounds = old
-            raise ValueError("Upper bounds object not understood.")
-        if (self.lower_bounds is not None and self.lower_bounds.shape != (self.dimensions, 1)) or (
-            self.upper_bounds is not None and self.upper_bounds.shape != (self.dimensions, 1)
-        ):
-            self.lower_bounds, self.upper_bounds = old
+        """Replace the bounds (either may be None: unbounded).  Lists become
+        column vectors; anything else must be a (dimensions, 1) array with
+        every upper bound above its lower bound.  A rejected pair raises
+        ValueError with the reference's messages (`base.py:272-359`) and
+        leaves the current bounds in place."""
+
+        def column(b):
+            return _numpy.array(b)[:, None] if type(b) == list else b
+
+        lower, upper = column(lower), column(upper)
+        for b, which in ((lower, "Lower"), (upper, "Upper")):
+            if b is not None and type(b) is not _numpy.ndarray:
+                raise ValueError(f"{which} bounds object not understood.")
+        if any(b is not None and b.shape != (self.dimensions, 1) for b in (lower, upper)):
             raise ValueError("Bounds vectors are of incorrect size.")
-        if (
-            self.lower_bounds is not None
-            and self.upper_bounds is not None
-            and _numpy.any(self.upper_bounds <= self.lower_bounds)
-        ):
-            self.lower_bounds, self.upper_bounds = old
+        if lower is not None and upper is not None and _numpy.any(upper <= lower):
             raise ValueError("Bounds vectors are incompatible.")
+        self.lower_bounds, self.upper_bounds = lower, upper
 
     def misfit_bounds(self, coordinates: _numpy.ndarray) -> float:
-        """0 inside the bounds, +inf outside (reference `base.py:361-374`)."""
-        if (self.lower_bounds is not None and _numpy.any(coordinates < self.lower_bounds)) or (
-            self.upper_bounds is not None and _numpy.any(coordinates > self.upper_bounds)
-        ):
-            return _numpy.inf
-        return 0.0
+        """+inf when any coordinate lies outside the bounds, else 0
+        (`base.py:361-374`)."""
+        outside = (self.lower_bounds is not None and bool(_numpy.any(coordinates < self.lower_bounds))) or (
+            self.upper_bounds is not None and bool(_numpy.any(coordinates > self.upper_bounds)))
+        return _numpy.inf if outside else 0.0
 
 
 # ---------------------------------------------------------------------------

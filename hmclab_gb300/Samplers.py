@@ -38,6 +38,15 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
                 and each pair swaps its models with the replica-exchange
                 acceptance of `Samplers.py:589-669` (on the device)
 
+diagnostic_mode (reference `Samplers.py:449-460, 499-527, 759-764`) times
+every phase of the proposals with CUDA events on the sampler's stream:
+momentum draw and trajectory start, gradients, kicks and drifts (with the
+bound reflection), end-point misfits, the accept test, sample output and
+replica exchanges.  Timing needs the launches uncaptured, so this mode runs
+without CUDA graphs and without the persistent kernel.  `get_diagnostics()`
+returns the timers (`function.__name__`, `calls`, `time_spent` in seconds);
+`finish()` prints the split like the reference does.
+
 Each proposal is issued as: begin (momentum, K0, first drift) -> for every
 kick: gradient of the target on the device, then kick+drift -> misfit at the
 end point -> accept/record.  All of it runs on one CUDA stream; blocks of
@@ -64,6 +73,74 @@ try:
     import torch as _torch
 except ImportError:  # pragma: no cover
     _torch = None
+
+class DeviceTimer:
+    """Accumulated device time of one phase of the proposals: the GPU
+    counterpart of the reference's AccumulatingTimer (Helpers/Timers.py:23-60),
+    with the same `function.__name__`, `calls` and `time_spent` (seconds)."""
+
+    class _Name:
+        def __init__(self, name):
+            self.__name__ = name
+
+    def __init__(self, name):
+        self.function = DeviceTimer._Name(name)
+        self.calls = 0
+        self.time_spent = 0.0
+        self._pending = []
+
+    def begin(self, stream):
+        ev = _torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        return ev
+
+    def end(self, ev0, stream):
+        ev1 = _torch.cuda.Event(enable_timing=True)
+        ev1.record(stream)
+        self._pending.append((ev0, ev1))
+        self.calls += 1
+
+    def add_host_seconds(self, seconds):
+        self.time_spent += float(seconds)
+        self.calls += 1
+
+    def collect(self):
+        """Fold the finished event pairs into time_spent (synchronises on them)."""
+        for ev0, ev1 in self._pending:
+            ev1.synchronize()
+            self.time_spent += ev0.elapsed_time(ev1) / 1e3
+        self._pending.clear()
+
+    def print_statistics(self):
+        print(f"Function: {self.function.__name__}")
+        print(f"Calls: {self.calls}")
+        print(f"Total time spent: {self.time_spent} seconds")
+
+    def __str__(self):
+        return f"Function: {self.function.__name__}, Calls: {self.calls}, Total time spent: {self.time_spent} seconds, "
+
+
+class _Phase:
+    """Context manager that times a phase when the sampler has timers."""
+
+    __slots__ = ("timer", "stream", "ev")
+
+    def __init__(self, timer, stream):
+        self.timer, self.stream = timer, stream
+
+    def __enter__(self):
+        if self.timer is not None:
+            self.ev = self.timer.begin(self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        if self.timer is not None:
+            self.timer.end(self.ev, self.stream)
+        return False
+
+
+_PHASES = ("generate_momentum", "gradient", "integrator", "misfit", "_evaluate_acceptance", "samples.append",
+           "exchange")
 
 # Integrator coefficients (Samplers.py:1588-1592, 1666-1669).
 _A1_3S, _B1_3S = 0.11888010966548, 0.29619504261126
@@ -126,6 +203,8 @@ class HMC:
     beta = None
     use_persistent = None
     _persistent = None
+    _timers = None
+    diagnostic_mode = False
 
     def __init__(self, seed: int = None):
         self.seed = seed
@@ -450,34 +529,46 @@ class HMC:
             self.surrogate._buffers(C, False)  # allocate before any capture
 
     # ------------------------------------------------------------------
+    def _phase(self, name):
+        timers = self._timers
+        return _Phase(timers[name] if timers is not None else None, self.stream)
+
     def _issue_proposal(self, h):
         """Enqueue one proposal for every chain on stream handle h."""
         st, dist, dt = self._state_ref, self.distribution, self.dtype
         first, steps = self._schedule
-        _lib.call("hmc_begin_trajectory", st, first, h)
+        with self._phase("generate_momentum"):
+            _lib.call("hmc_begin_trajectory", st, first, h)
         fused = self._fused
         if fused is not None:
             # gradient + prior + kick + drift in the tensor-core epilogue
-            fused.after_begin(h)
-            for needs_grad, kick, drift in steps:
-                if needs_grad:
-                    fused.kick_drift(kick, drift, h)
-                else:
-                    fused.drift_only(drift, h)
-            fused.misfit(h)
-            _lib.call("hmc_end_trajectory", st, h)
+            with self._phase("integrator"):
+                fused.after_begin(h)
+                for needs_grad, kick, drift in steps:
+                    if needs_grad:
+                        fused.kick_drift(kick, drift, h)
+                    else:
+                        fused.drift_only(drift, h)
+            with self._phase("misfit"):
+                fused.misfit(h)
+            with self._phase("_evaluate_acceptance"):
+                _lib.call("hmc_end_trajectory", st, h)
             return
         for needs_grad, kick, drift in steps:
             if needs_grad:
-                if self.surrogate is not None:
-                    self.surrogate.predict_into(self.q, self.g, h)
-                else:
-                    dist._device_gradient(self.q, self.g, False, dt, h)
-                    if self.training_set is not None:
-                        self.training_set.record(self.q, self.g, h)
-            _lib.call("hmc_kick_drift", st, kick, drift, h)
-        dist._device_misfit(self.q, self.x_prop, False, dt, h)
-        _lib.call("hmc_end_trajectory", st, h)
+                with self._phase("gradient"):
+                    if self.surrogate is not None:
+                        self.surrogate.predict_into(self.q, self.g, h)
+                    else:
+                        dist._device_gradient(self.q, self.g, False, dt, h)
+                        if self.training_set is not None:
+                            self.training_set.record(self.q, self.g, h)
+            with self._phase("integrator"):
+                _lib.call("hmc_kick_drift", st, kick, drift, h)
+        with self._phase("misfit"):
+            dist._device_misfit(self.q, self.x_prop, False, dt, h)
+        with self._phase("_evaluate_acceptance"):
+            _lib.call("hmc_end_trajectory", st, h)
 
     def _issue_block(self, n_props, h):
         for _ in range(n_props):
@@ -545,6 +636,12 @@ class HMC:
         self._parse_surrogate(a["surrogate"], a["training_set"])
         self._parse_tempering(a["temperatures"], a["exchange_interval"])
         self.use_persistent = a["persistent"]
+        self._timers = None
+        if self.diagnostic_mode:
+            # every phase is timed with events: no graph capture, no persistent kernel
+            self.use_graph = False
+            self.use_persistent = False
+            self._timers = {name: DeviceTimer(name) for name in _PHASES}
         self._setup_device()
         self._open_files()
         self._done = 0
@@ -622,11 +719,38 @@ class HMC:
             else:
                 self._issue_block(n, h)
             if self.exchange_interval is not None and (self._done + n) % self.exchange_interval == 0:
-                self._exchange(h)
-            self._drain(self._done, n)
+                with self._phase("exchange"):
+                    self._exchange(h)
+            if self._timers is not None:
+                t0 = _time.perf_counter()
+                self._drain(self._done, n)
+                self._timers["samples.append"].add_host_seconds(_time.perf_counter() - t0)
+                for timer in self._timers.values():
+                    timer.collect()
+            else:
+                self._drain(self._done, n)
             self._done += n
             issued += n
         return issued
+
+    def get_diagnostics(self):
+        """The phase timers of diagnostic_mode (reference `Samplers.py:759-764`)."""
+        from hmclab_gb300.Helpers.CustomExceptions import InvalidCaseError
+
+        if not self.diagnostic_mode:
+            raise InvalidCaseError("Can't return diagnostics if sampler is not in diagnostic mode")
+        return list(self._timers.values())
+
+    def _print_diagnostics(self):
+        total = self.runtime_seconds
+        print("Detailed statistics:")
+        print(f"Total runtime: {total:.2f} seconds")
+        print()
+        print("Device time per phase (CUDA events on the sampler stream):")
+        print("{:<30} {:<12} {:<30}".format("Phase", "calls", "percentage of time"))
+        for timer in self._timers.values():
+            pct = 100.0 * timer.time_spent / total if total > 0 else 0.0
+            print("{:<30} {:<12} {:<30.2f}".format(timer.function.__name__, timer.calls, pct))
 
     def finish(self):
         """Synchronise, release the graph, write attributes and close files."""
@@ -644,6 +768,10 @@ class HMC:
         if check is not None:
             check()
         self._finalise(self._done)
+        if self._timers is not None:
+            for timer in self._timers.values():
+                timer.collect()
+            self._print_diagnostics()
         return self
 
     def _run(self):

@@ -370,6 +370,52 @@ def case_integrators_autotune():
     save("integrators_autotune.npz", mean=mean, var=var, q0=q0, z=z, f=f, u=u, za=za, fa=fa, ua=ua, **out)
 
 
+class _GridModel:
+    """Stands in for the psvWave fdModel that the reference's
+    BlobParametrization (ElasticFullWaveform2D.py:229-341) reads: cell-centre
+    coordinates of the whole grid as [x][z] arrays, the boundary widths, the
+    free-parameter count and a background model vector (vp | vs | rho over
+    the physical cells, x fastest).  psvWave itself is not installed."""
+
+    def __init__(self, nx, nz, pad, h, background):
+        self.np_boundary, self.nx_inner_boundary, self.nz_inner_boundary = pad, 0, 0
+        self.free_parameters = 3 * nx * nz
+        self._bg = background
+        ix = (np.arange(nx + 2 * pad) - pad + 0.5) * h
+        iz = (np.arange(nz + 2 * pad) - pad + 0.5) * h
+        self._x, self._z = np.meshgrid(ix, iz, indexing="ij")
+
+    def get_coordinates(self, _all):
+        return self._x.copy(), self._z.copy()
+
+    def get_model_vector(self):
+        return self._bg.copy()
+
+
+def case_blob_projection():
+    """The reference's Gaussian-blob collocation matrix, its (C^T C)^-1 C^T
+    map applied to grid gradients, and the forward map of a blob vector, on a
+    12 x 8-cell grid with 4 x 3 blobs per field."""
+    import importlib
+    import types
+
+    stub = types.ModuleType("psvWave")
+    stub.fdModel = _GridModel  # only named in a class annotation at import
+    sys.modules.setdefault("psvWave", stub)
+
+    efwi = importlib.import_module("hmclab.Distributions.ElasticFullWaveform2D")
+    nx, nz, pad, h, nbx, nbz = 12, 8, 4, 5.0, 4, 3
+    rng = np.random.default_rng(17)
+    bg = np.concatenate([np.full(nx * nz, 2000.0), np.full(nx * nz, 1100.0), np.full(nx * nz, 2100.0)])
+    blob = efwi.BlobParametrization(_GridModel(nx, nz, pad, h, bg), nbx, nbz)
+    g = rng.normal(size=(3 * nx * nz, 3))
+    m = rng.normal(size=(3 * nbx * nbz, 1)) * 50.0
+    save("blob_projection.npz", nx=nx, nz=nz, pad=pad, h=h, nbx=nbx, nbz=nbz, background=bg,
+         collocation=blob.collocation_matrix, confusion=blob.confusion_matrix, grid_gradients=g,
+         projected=np.stack([blob.inverse_transform(g[:, k]) for k in range(3)], axis=1), blob_model=m,
+         fine_model=blob.forward_transform_background(m))
+
+
 if __name__ == "__main__":
     case_cfg1()
     case_public_linearmatrix()
@@ -379,3 +425,4 @@ if __name__ == "__main__":
     case_srcloc_small()
     case_full_mass_bounds()
     case_integrators_autotune()
+    case_blob_projection()

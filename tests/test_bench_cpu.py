@@ -53,3 +53,51 @@ def test_fwi_workload_algorithmic_bytes():
     assert wl.stencil_bytes_per_step() == 80.0 * 240 * 140 * 64
     cfg = wl.config()
     assert cfg["chains"] == 64 and cfg["nt"] == 1500 and cfg["params"] == 600
+
+
+def _fake_reference(wl, path, **over):
+    import numpy as np
+
+    d = 600
+    ref = dict(mean=np.zeros(d), std=np.ones(d), ess=np.full(d, 2000.0), ess_per_chain_proposal=0.15,
+               q_final=np.zeros((d, wl.chains)), chains=wl.chains, leapfrog_steps=wl.L, stepsize=wl.stepsize,
+               noise_fraction=wl.noise_fraction, seed=0, proposals=200)
+    ref.update(over)
+    np.savez(path, **ref)
+    return str(path)
+
+
+def test_fwi_reference_fixture_is_checked_against_the_workload(tmp_path):
+    wl = bench.FwiWorkload()
+    ref, why = bench.load_fwi_reference(wl, str(tmp_path / "missing.npz"))
+    assert ref is None and "no reference fixture" in why
+    ref, why = bench.load_fwi_reference(wl, _fake_reference(wl, tmp_path / "ok.npz"))
+    assert why is None and float(ref["ess_per_chain_proposal"]) == 0.15
+    ref, why = bench.load_fwi_reference(wl, _fake_reference(wl, tmp_path / "bad.npz", stepsize=0.2))
+    assert ref is None and "stepsize" in why
+
+
+def test_fwi_headline_validity_gates():
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    d = 600
+    ref = dict(mean=np.zeros(d), std=np.ones(d), ess=np.full(d, 4000.0))
+    ess = np.full(d, 400.0)
+    # unbiased run: z ~ N(0, 1)
+    mean = rng.normal(size=d) * np.sqrt(1 / 400 + 1 / 4000)
+    std = 1 + rng.normal(size=d) * np.sqrt(1 / 800 + 1 / 8000)
+    mc = bench.moment_check(mean, std, ess, ref)
+    assert mc["mean_z_max"] < 4.5 and mc["std_z_max"] < 4.5
+    assert bench.fwi_validity(ess, mc) == []
+    # windows that did not truncate are flagged negative by the estimator
+    raw = ess.copy()
+    raw[:100] *= -1
+    assert any("lag windows" in r for r in bench.fwi_validity(raw, mc))
+    # a biased run: one parameter's mean off by 10 Monte Carlo errors
+    mean_b = mean.copy()
+    mean_b[7] += 10 * np.sqrt(1 / 400 + 1 / 4000)
+    mc_b = bench.moment_check(mean_b, std, ess, ref)
+    assert any("moments disagree" in r for r in bench.fwi_validity(ess, mc_b))
+    assert bench.fwi_validity(ess, None) == ["no reference moments to check the run against"]
+    assert not mc["within_2pct_of_reference_std"]

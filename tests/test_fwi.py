@@ -148,3 +148,67 @@ def test_device_fwi_staged_tiles_match_direct_loads():
     vp, vs, rho = (cfg.extend(f) for f in dists[0].fine_model(m32))
     chi = sum(s.gradient(rho, vp, vs, obs[k][0], obs[k][1], dists[0].weight)[0] for k, s in enumerate(shots))
     np.testing.assert_allclose(x[0][0], chi, rtol=1e-5)
+
+
+def _blob_case(golden):
+    g = golden("blob_projection.npz")
+    cfg = FW.ElasticConfig(nx=int(g["nx"]), nz=int(g["nz"]), pad=int(g["pad"]), h=float(g["h"]), dt=5e-4, nt=10,
+                           src_x=(20.0,), src_z=10.0, rec_x=np.array([10.0, 50.0]), rec_z=10.0)
+    return g, cfg, FW.BlobBasis(cfg, int(g["nbx"]), int(g["nbz"]))
+
+
+def test_blob_basis_and_projection_match_the_reference(golden):
+    """BlobBasis against the reference's BlobParametrization
+    (ElasticFullWaveform2D.py:229-341, golden fixture from the reference
+    itself): the same collocation matrix, the same (C^T C)^-1 C^T map that
+    the reference applies to grid gradients (`gradient_projection=
+    "least_squares"`), and the same forward map of a blob vector."""
+    g, cfg, blob = _blob_case(golden)
+    n, nb = cfg.nx * cfg.nz, blob.n_blobs
+    Cref = g["collocation"]
+    for f in range(3):
+        np.testing.assert_allclose(Cref[f * n:(f + 1) * n, f * nb:(f + 1) * nb], blob.B, rtol=1e-12, atol=1e-15)
+        off = np.delete(Cref[f * n:(f + 1) * n], np.s_[f * nb:(f + 1) * nb], axis=1)
+        assert not off.any()
+    proj = np.linalg.inv(blob.B.T @ blob.B)
+    for k in range(3):
+        gg = g["grid_gradients"][:, k].reshape(3, n)
+        mine = np.concatenate([proj @ (blob.B.T @ gg[f]) for f in range(3)])
+        np.testing.assert_allclose(mine, g["projected"][:, k], rtol=1e-9, atol=1e-9 * np.abs(mine).max())
+    m = g["blob_model"][:, 0].reshape(3, nb)
+    bg = g["background"].reshape(3, n)
+    fine = np.concatenate([blob.B @ m[f] + bg[f] for f in range(3)])
+    np.testing.assert_allclose(fine, g["fine_model"], rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_device_least_squares_projection_is_the_reference_map():
+    """`gradient_projection="least_squares"` on the device returns the
+    reference's (C^T C)^-1 C^T map of the grid gradient: per field,
+    (B^T B)^-1 times the chain-rule blob gradient (which the oracle pins)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import hmclab_gb300 as H
+
+    cfg = small_config(nt=200)
+    shots = oracle_shots(cfg)
+    truth = FW.layered_model(cfg, anomalies=True)
+    obs = [s.forward(*(cfg.extend(f) for f in (truth[2], truth[0], truth[1]))) for s in shots]
+    ux, uz = np.stack([o[0] for o in obs]), np.stack([o[1] for o in obs])
+    std = float(np.sqrt(np.mean(ux**2 + uz**2))) * 0.1
+    bg = FW.layered_model(cfg, anomalies=False)
+    kw = dict(data_std=std, free_parameter_grid=[5, 3], background=bg)
+    chain = H.Distributions.ElasticFullWaveform2D(cfg, ux, uz, **kw)
+    ls = H.Distributions.ElasticFullWaveform2D(cfg, ux, uz, gradient_projection="least_squares", **kw)
+    rng = np.random.default_rng(6)
+    M = torch.from_numpy(rng.normal(size=(45, 32)) * np.repeat([40.0, 20.0, 15.0], 15)[:, None]).to("cuda",
+                                                                                                 torch.float32)
+    g_cr = chain.gradient_batch(M).double().cpu().numpy()
+    g_ls = ls.gradient_batch(M).double().cpu().numpy()
+    proj = np.linalg.inv(chain.blob.B.T @ chain.blob.B)
+    nb = chain.blob.n_blobs
+    want = np.concatenate([proj @ g_cr[f * nb:(f + 1) * nb] for f in range(3)])
+    err = np.abs(g_ls - want).max() / np.abs(want).max()
+    print(f"least-squares projection on the device vs (B^T B)^-1 chain-rule gradient: {err:.2e}")
+    assert err < 1e-5  # FP32 products; cond(B^T B) is 14 here

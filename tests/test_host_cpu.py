@@ -319,3 +319,85 @@ def test_batched_calls_reject_host_arrays_and_wrong_shapes():
         dist.misfit_batch(torch.zeros(4, 3))
     with pytest.raises(ValueError, match="CUDA tensor"):
         dist.gradient_batch(np.zeros((4, 3)))
+
+
+def test_get_diagnostics_needs_diagnostic_mode():
+    import hmclab_gb300 as H
+    from hmclab_gb300.Helpers.CustomExceptions import InvalidCaseError
+
+    with pytest.raises(InvalidCaseError):
+        H.Samplers.HMC(seed=0).get_diagnostics()
+    t = H.Samplers.DeviceTimer("gradient")
+    t.add_host_seconds(0.25)
+    assert t.function.__name__ == "gradient" and t.calls == 1 and t.time_spent == 0.25
+    assert "gradient" in str(t)
+
+
+def test_samples_file_opens_with_the_reference_reader(tmp_path):
+    """A file written by hmclab_gb300's Samples writer (the one the sampler
+    drains thinned samples into) is opened unchanged by the reference's own
+    `Samples` reader (hmclab/Samples.py:23-278): same (d+1, N) layout, same
+    attributes, burn-in slicing and misfit row."""
+    from oracle import ref_shim
+
+    ref = ref_shim.load()
+    if ref is None:
+        pytest.skip("reference sources not present on this machine")
+    from hmclab.Samples import Samples as RefSamples
+
+    fn = str(tmp_path / "chain.npy")
+    rng = np.random.default_rng(3)
+    d, N = 5, 40
+    cols = rng.normal(size=(d + 1, N))
+    w = H.Samples(fn, mode="w")
+    for k in range(0, N, 8):
+        w.append_columns(cols[:, k:k + 8])
+    for name, value in (("stepsize", 0.1), ("amount_of_steps", 10), ("mass_matrix", "Unit"),
+                        ("integrator", "leapfrog"), ("proposals", N), ("online_thinning", 1), ("sampler", "HMC")):
+        w.write_attribute(name, value)
+    w.close()
+    with RefSamples(fn, burn_in=10) as r:
+        assert r.numpy.shape == (d + 1, N - 10)
+        np.testing.assert_array_equal(r.samples, cols[:-1, 10:])
+        np.testing.assert_array_equal(r.misfits, cols[-1, 10:])
+        assert r.read_attribute("write_index") == N
+        assert r.read_attribute("proposals") == N and r.read_attribute("sampler") == "HMC"
+        # the reference's [] applies the burn-in on top of `numpy`, which already has it
+        np.testing.assert_array_equal(r[:, :3], cols[:, 20:23])
+
+
+def test_bound_handling_matches_the_reference_contract():
+    """corrector / update_bounds / misfit_bounds against the reference's own
+    methods (hmclab/Distributions/base.py:239-374) on the same inputs:
+    reflections, momentum flips, the lower-then-upper order, error messages
+    and that rejected bounds leave the old ones in place."""
+    from oracle import ref_shim
+
+    ref = ref_shim.load()
+    if ref is None:
+        pytest.skip("reference sources not present on this machine")
+    rng = np.random.default_rng(5)
+    d = 7
+    mine = H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1)))
+    theirs = ref.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1)))
+    lo, hi = -np.ones((d, 1)), np.ones((d, 1))
+    for dist in (mine, theirs):
+        dist.update_bounds(lower=list(lo[:, 0]), upper=hi)
+    for _ in range(20):
+        q = rng.normal(size=(d, 1)) * 2.5  # some beyond both reflections
+        p = rng.normal(size=(d, 1))
+        q1, p1, q2, p2 = q.copy(), p.copy(), q.copy(), p.copy()
+        mine.corrector(q1, p1)
+        theirs.corrector(q2, p2)
+        np.testing.assert_array_equal(q1, q2)
+        np.testing.assert_array_equal(p1, p2)
+        assert mine.misfit_bounds(q) == theirs.misfit_bounds(q)
+    for args in ({"lower": "x"}, {"upper": 3.0}, {"lower": np.zeros((d + 1, 1))}, {"lower": hi, "upper": lo}):
+        msgs = []
+        for dist in (mine, theirs):
+            with pytest.raises(ValueError) as e:
+                dist.update_bounds(**args)
+            msgs.append(str(e.value))
+            np.testing.assert_array_equal(dist.lower_bounds, lo)
+            np.testing.assert_array_equal(dist.upper_bounds, hi)
+        assert msgs[0] == msgs[1]

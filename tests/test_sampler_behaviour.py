@@ -160,3 +160,33 @@ def test_interrupt_ends_the_run_cleanly(tmp_path):
     assert 0 < smp.current_proposal < 9999
     n = H.Samples(f).numpy.shape[1]
     assert n == smp.current_proposal + 1
+
+
+def test_diagnostic_mode_times_every_phase(capsys):
+    """diagnostic_mode (reference Samplers.py:449-460, 499-527, 759-764):
+    CUDA-event timers per phase with the reference's timer attributes, call
+    counts that follow the proposal structure, and the printed split."""
+    import hmclab_gb300 as H
+
+    rng = np.random.default_rng(4)
+    d, C, P, L = 30, 16, 6, 5
+    G = rng.normal(size=(60, d)) / np.sqrt(d)
+    dat = G @ rng.normal(size=(d, 1))
+    post = H.Distributions.BayesRule([H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1))),
+                                      H.Distributions.LinearMatrix(G, dat, 0.01, dtype=np.float64)])
+    smp = H.Samplers.HMC(seed=2).sample(None, post, stepsize=0.01, amount_of_steps=L, proposals=P, chains=C,
+                                        dtype="float64", diagnostic_mode=True, initial_model=np.zeros((d, C)))
+    timers = {t.function.__name__: t for t in smp.get_diagnostics()}
+    assert timers["generate_momentum"].calls == P
+    assert timers["gradient"].calls == P * L  # position Verlet: L gradients per trajectory
+    assert timers["integrator"].calls == P * L  # one kick+drift per gradient
+    assert timers["misfit"].calls == P and timers["_evaluate_acceptance"].calls == P
+    for name in ("generate_momentum", "gradient", "integrator", "misfit", "_evaluate_acceptance"):
+        assert timers[name].time_spent > 0.0, name
+    assert sum(t.time_spent for t in timers.values()) <= smp.runtime_seconds
+    out = capsys.readouterr().out
+    assert "Detailed statistics:" in out and "gradient" in out
+    # the same launch-per-step run without the timers (graph-captured) gives the same chains
+    ref = H.Samplers.HMC(seed=2).sample(None, post, stepsize=0.01, amount_of_steps=L, proposals=P, chains=C,
+                                        dtype="float64", initial_model=np.zeros((d, C)), persistent=False)
+    assert np.array_equal(ref.current_model, smp.current_model)
