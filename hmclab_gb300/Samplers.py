@@ -34,9 +34,15 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
                 run whole blocks of proposals in one persistent launch, one
                 warp per chain; False forces one launch per leapfrog step
   exchange_interval
-                every this many proposals, the chains are paired at random
-                and each pair swaps its models with the replica-exchange
-                acceptance of `Samplers.py:589-669` (on the device)
+                after every proposal whose index is a multiple of this (the
+                first one included, as in the reference), the chains are
+                paired at random and each pair swaps its models with the
+                replica-exchange acceptance of `Samplers.py:589-669` (on the
+                device)
+  exchange_streams
+                parity mode for the exchanges: (schedule [E][2 (C // 2)],
+                uniforms [E][C // 2]) replacing the pairing and accept draws
+                of exchange row e = proposal index // exchange_interval
 
 diagnostic_mode (reference `Samplers.py:449-460, 499-527, 759-764`) times
 every phase of the proposals with CUDA events on the sampler's stream:
@@ -200,11 +206,13 @@ class HMC:
     training_set = None
     _temperatures = None
     exchange_interval = None
+    _exchange_streams = None
     beta = None
     use_persistent = None
     _persistent = None
     _timers = None
     diagnostic_mode = False
+    _proposal_base = 0  # proposals done before a resumed run (its Philox counter origin)
 
     def __init__(self, seed: int = None):
         self.seed = seed
@@ -249,8 +257,15 @@ class HMC:
         temperatures=None,
         exchange_interval: int = None,
         persistent: bool = None,
+        resume=None,
+        exchange_streams=None,
     ):
         """Run `proposals` HMC proposals for every chain; returns self.
+
+        `resume` (a path written by `checkpoint()`) continues earlier chains:
+        positions, per-chain step sizes, chain count, dtype, Philox key and
+        proposal count (and a passed surrogate's state) come from the
+        checkpoint.
 
         Raises AssertionError / ValueError / TypeError / FileExistsError for
         invalid arguments like the reference."""
@@ -263,7 +278,8 @@ class HMC:
             autotuning=autotuning, target_acceptance_rate=target_acceptance_rate, learning_rate=learning_rate,
             chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
             keep_samples=keep_samples, surrogate=surrogate, training_set=training_set, temperatures=temperatures,
-            exchange_interval=exchange_interval, persistent=persistent,
+            exchange_interval=exchange_interval, persistent=persistent, resume=resume,
+            exchange_streams=exchange_streams,
         )
         self._run()
         return self
@@ -440,6 +456,7 @@ class HMC:
             self._ex_total = _torch.zeros((1,), dtype=_torch.int64, device=dev)
         self.flags = _torch.zeros((C,), dtype=_torch.int32, device=dev)
         self.control = _torch.zeros((2,), dtype=_torch.int64, device=dev)
+        self.control[0] = self._proposal_base  # a resumed run continues the Philox counter
         lo, hi = self.distribution.lower_bounds, self.distribution.upper_bounds
         self.lower = _dev.upload(lo[:, 0], dt, dev) if lo is not None else None
         self.upper = _dev.upload(hi[:, 0], dt, dev) if hi is not None else None
@@ -451,8 +468,8 @@ class HMC:
         self.ring_q = E((slots, d, C))
         self.ring_x = E((slots, C), "float64")
         if self.autotuning:
-            self.rec_eps = Z((self.proposals, C), "float64")
-            self.rec_acc = Z((self.proposals, C), "float64")
+            self.rec_eps = Z((self._proposal_base + self.proposals, C), "float64")
+            self.rec_acc = Z((self._proposal_base + self.proposals, C), "float64")
         else:
             self.rec_eps = self.rec_acc = None
         # injected streams
@@ -498,7 +515,7 @@ class HMC:
         st.ring_q, st.ring_x = self.ring_q.data_ptr(), self.ring_x.data_ptr()
         st.ring_slots, st.thinning = slots, self.online_thinning
         st.rec_stepsize, st.rec_acceptance = _dev.ptr(self.rec_eps), _dev.ptr(self.rec_acc)
-        st.rec_len = self.proposals if self.autotuning else 0
+        st.rec_len = self._proposal_base + self.proposals if self.autotuning else 0
         st.beta = _dev.ptr(self.beta)
         self._state = st
         self._state_ref = _ct.byref(st)
@@ -601,12 +618,13 @@ class HMC:
         """Move the thinned samples of proposals [n0, n0+n) to the files."""
         if self._writers is None or self.keep_samples:
             return
-        m = n // self.online_thinning
+        first, m = self._recorded(n0, n)
         if m == 0:
             return
+        sel = self._ring_index(first, m)
         with _torch.cuda.stream(self.stream):
-            q = self.ring_q[:m].to(_torch.float64).cpu().numpy()  # m, d, C
-            x = self.ring_x[:m].cpu().numpy()  # m, C
+            q = self.ring_q[sel].to(_torch.float64).cpu().numpy()  # m, d, C
+            x = self.ring_x[sel].cpu().numpy()  # m, C
         for c, w in enumerate(self._writers):
             w.append_columns(_numpy.vstack([q[:, :, c].T, x[None, :, c]]))
 
@@ -620,12 +638,16 @@ class HMC:
             max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
             dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
             surrogate=None, training_set=None, temperatures=None, exchange_interval=None, persistent=None,
+            resume=None, exchange_streams=None,
         )
         unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
         if unknown:
             raise TypeError(f"Unidentified argument(s) not applicable to sampler: {unknown}")
         defaults.update({k: v for k, v in kwargs.items() if k in defaults})
         a = defaults
+        ck = None
+        if a["resume"] is not None:
+            ck = self._read_checkpoint(a["resume"], distribution, a)
         self._parse(
             samples_filename, distribution, a["stepsize"], a["randomize_stepsize"], a["amount_of_steps"],
             a["mass_matrix"], a["integrator"], a["initial_model"], a["proposals"], a["online_thinning"],
@@ -633,8 +655,16 @@ class HMC:
             a["target_acceptance_rate"], a["learning_rate"], a["chains"], a["dtype"], a["rng_streams"], a["graph"],
             a["proposals_per_graph"], a["keep_samples"],
         )
+        if ck is not None:
+            self.philox_seed = int(ck["philox_seed"])
+            self._proposal_base = int(ck["proposals_done"])
+            if a["surrogate"] is not None:
+                keys = [k for k in ck if k.startswith("surrogate.")]
+                if not keys:
+                    raise ValueError("the checkpoint holds no surrogate state to resume the surrogate from")
+                a["surrogate"].load_state_arrays({k[len("surrogate."):]: ck[k] for k in keys})
         self._parse_surrogate(a["surrogate"], a["training_set"])
-        self._parse_tempering(a["temperatures"], a["exchange_interval"])
+        self._parse_tempering(a["temperatures"], a["exchange_interval"], a["exchange_streams"])
         self.use_persistent = a["persistent"]
         self._timers = None
         if self.diagnostic_mode:
@@ -650,6 +680,85 @@ class HMC:
         self._launches0 = _lib.launch_count()
         return self
 
+    # ---- checkpoint / resume ------------------------------------------------
+    CHECKPOINT_FORMAT = "hmclab_gb300.checkpoint.v1"
+
+    def checkpoint(self, path):
+        """Write what continuing these chains needs to `path` (.npz): current
+        positions, per-chain base step sizes (as adapted by autotuning), the
+        Philox key, the number of proposals done, and the surrogate's weights,
+        Adam moments and normalisation when a surrogate drives the sampler.
+        `sample(..., resume=path)` continues from it: with the same target,
+        mass matrix and settings the continued chains equal an uninterrupted
+        run bit for bit (the reference saves no chain or random state,
+        Samples.py:280-335, so it has no counterpart)."""
+        from hmclab_gb300.Helpers.CustomExceptions import InvalidCaseError
+
+        if getattr(self, "current_model", None) is None:
+            raise InvalidCaseError("checkpoint() needs a finished run (sample() or finish())")
+        arrays = {
+            "format": _numpy.array(self.CHECKPOINT_FORMAT),
+            "q": _numpy.asarray(self.current_model, _numpy.float64),
+            "eps": self.eps.to(_torch.float64).cpu().numpy(),
+            "proposals_done": _numpy.array(self._proposal_base + self.proposals_done, _numpy.int64),
+            "philox_seed": _numpy.array(self.philox_seed, _numpy.uint64),
+            "dimensions": _numpy.array(self.dimensions, _numpy.int64),
+            "chains": _numpy.array(self.chains, _numpy.int64),
+            "dtype": _numpy.array(self.dtype),
+            "online_thinning": _numpy.array(self.online_thinning, _numpy.int64),
+        }
+        if self.surrogate is not None:
+            for k, v in self.surrogate.state_arrays().items():
+                arrays["surrogate." + k] = v
+        with open(path, "wb") as f:
+            _numpy.savez(f, **arrays)
+        return path
+
+    def _read_checkpoint(self, path, distribution, a):
+        """Load a checkpoint and fill the sampler arguments it determines."""
+        with _numpy.load(path, allow_pickle=False) as f:
+            ck = {k: f[k] for k in f.files}
+        if str(ck.get("format", "")) != self.CHECKPOINT_FORMAT:
+            raise ValueError(f"{path} is not an hmclab_gb300 sampler checkpoint")
+        if int(ck["dimensions"]) != distribution.dimensions:
+            raise ValueError(f"checkpoint has {int(ck['dimensions'])} dimensions, the target {distribution.dimensions}")
+        C = int(ck["chains"])
+        if a["chains"] is not None and int(a["chains"]) != C:
+            raise ValueError(f"checkpoint has {C} chains, {a['chains']} were requested")
+        if a["dtype"] is not None and _dev.normalise_dtype(a["dtype"]) != str(ck["dtype"]):
+            raise ValueError(f"checkpoint chains are {ck['dtype']}, {a['dtype']} was requested")
+        if a["initial_model"] is not None:
+            raise ValueError("`initial_model` and `resume` exclude each other: the checkpoint holds the positions")
+        if a["rng_streams"] is not None:
+            raise ValueError("resuming continues the Philox streams; injected `rng_streams` cannot be resumed")
+        done = int(ck["proposals_done"])
+        thin = int(a["online_thinning"])
+        if done % thin:
+            raise ValueError(f"the checkpoint's {done} proposals are not a multiple of online_thinning = {thin}")
+        a["initial_model"] = ck["q"]
+        a["stepsize"] = ck["eps"] if C > 1 else float(ck["eps"][0])
+        a["chains"] = C
+        a["dtype"] = str(ck["dtype"])
+        return ck
+
+    def _recorded(self, n0, n):
+        """(first thinned-sample number, count) of the samples recorded by
+        this run's proposals [n0, n0 + n): proposal g (counted from the first
+        proposal of the chains, a resumed run included) is recorded when
+        g % online_thinning == 0, as sample g // online_thinning."""
+        t = self.online_thinning
+        g0 = self._proposal_base + n0
+        first = -(-g0 // t)
+        return first, -(-(g0 + n) // t) - first
+
+    def _ring_index(self, first, m):
+        """Ring slots of thinned samples first .. first + m - 1 (the device
+        indexes the ring by the sample number, modulo its slots)."""
+        idx = (first + _numpy.arange(m)) % self.ring_slots
+        if m == 0 or (idx[0] == 0 and m <= self.ring_slots and _numpy.all(_numpy.diff(idx) == 1)):
+            return slice(0, m)
+        return _torch.from_numpy(idx).to(self.device)
+
     def _parse_surrogate(self, surrogate, training_set):
         self.surrogate = surrogate
         self.training_set = training_set
@@ -663,7 +772,7 @@ class HMC:
         if training_set is not None or not self.distribution.graph_safe:
             self.use_graph = False
 
-    def _parse_tempering(self, temperatures, exchange_interval):
+    def _parse_tempering(self, temperatures, exchange_interval, exchange_streams=None):
         self._temperatures = None
         if temperatures is not None:
             t = _numpy.asarray(temperatures, dtype=_numpy.float64).reshape(-1)
@@ -679,13 +788,37 @@ class HMC:
             self.exchange_interval = exchange_interval
             # exchanges happen between graph blocks: one block per interval
             self.proposals_per_graph = exchange_interval
+        self._exchange_streams = None
+        if exchange_streams is not None:
+            assert exchange_interval is not None, "`exchange_streams` needs an exchange_interval"
+            sched, uu = exchange_streams
+            sched = _numpy.asarray(sched, _numpy.int64)
+            uu = _numpy.asarray(uu, _numpy.float64)
+            npairs = self.chains // 2
+            assert sched.ndim == 2 and sched.shape[1] == 2 * npairs, "exchange schedule rows hold 2 * (C // 2) chains"
+            assert uu.shape == (sched.shape[0], npairs), "one exchange uniform per pair and schedule row"
+            assert all(len(set(r)) == len(r) and r.min() >= 0 and r.max() < self.chains for r in sched), (
+                "every schedule row must list distinct chains")
+            self._exchange_streams = (sched, uu)
 
-    def _exchange(self, h):
-        """Pair the chains at random and let each pair swap models."""
+    def _exchange(self, h, n_last):
+        """Pair the chains at random and let each pair swap models, after
+        proposal n_last (a multiple of exchange_interval).  The pairing is the
+        reference's schedule row (Samplers.py:1872-1885): 2 floor(C / 2)
+        distinct chains drawn without replacement, consecutive entries
+        paired; injected `exchange_streams` replace the draws."""
         C = self.chains
         npairs = C // 2
-        perm = self.rng.permutation(C)[: 2 * npairs].astype(_numpy.int32)
-        u = self.rng.uniform(0, 1, size=npairs)
+        if self._exchange_streams is not None:
+            sched, uu = self._exchange_streams
+            row = n_last // self.exchange_interval
+            if row >= len(sched):
+                return
+            perm = _numpy.asarray(sched[row], _numpy.int32)
+            u = _numpy.asarray(uu[row], _numpy.float64)
+        else:
+            perm = self.rng.choice(C, 2 * npairs, replace=False).astype(_numpy.int32)
+            u = self.rng.uniform(0, 1, size=npairs)
         with _torch.cuda.stream(self.stream):
             self._ex_pairs[: 2 * npairs].copy_(_torch.from_numpy(perm))
             self._ex_u[:npairs].copy_(_torch.from_numpy(u))
@@ -702,6 +835,12 @@ class HMC:
         issued = 0
         while self._done < target:
             n = min(k, target - self._done)
+            if self.exchange_interval is not None:
+                # blocks end right after the proposals that exchange (indices
+                # that are multiples of the interval, the first one included)
+                g = self._proposal_base + self._done
+                nxt = -(-g // self.exchange_interval) * self.exchange_interval
+                n = min(n, nxt - g + 1)
             self._load_streams(self._done, n)
             if self._persistent is not None:
                 self._persistent.run(n, h)
@@ -718,9 +857,10 @@ class HMC:
                 _lib.call("hmc_graph_launch", self._graph, h)
             else:
                 self._issue_block(n, h)
-            if self.exchange_interval is not None and (self._done + n) % self.exchange_interval == 0:
+            n_last = self._proposal_base + self._done + n - 1
+            if self.exchange_interval is not None and n_last % self.exchange_interval == 0:
                 with self._phase("exchange"):
-                    self._exchange(h)
+                    self._exchange(h, n_last)
             if self._timers is not None:
                 t0 = _time.perf_counter()
                 self._drain(self._done, n)
@@ -803,8 +943,9 @@ class HMC:
         if self.autotuning:
             self.stepsize = float(eps[0]) if C == 1 else eps
             n = self.current_proposal  # the reference keeps [:current_proposal]
-            se = self.rec_eps[:n].cpu().numpy()
-            ra = self.rec_acc[:n].cpu().numpy()
+            b = self._proposal_base  # records are indexed by the global proposal count
+            se = self.rec_eps[b:b + n].cpu().numpy()
+            ra = self.rec_acc[b:b + n].cpu().numpy()
             self.stepsizes = se if C > 1 else se[:, :1]
             self.acceptance_rates = ra if C > 1 else ra[:, :1]
         rate = acc / max(done, 1)
@@ -821,8 +962,9 @@ class HMC:
                 w.close()
             self._writers = None
         if self.keep_samples:
-            m = done // self.online_thinning
-            self.samples_device = (self.ring_q[:m], self.ring_x[:m])
+            first, m = self._recorded(0, done)
+            sel = self._ring_index(first, m)
+            self.samples_device = (self.ring_q[sel], self.ring_x[sel])
 
     # ------------------------------------------------------------------
     def samples_numpy(self, chain=None):

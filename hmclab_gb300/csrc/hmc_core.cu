@@ -551,10 +551,20 @@ __global__ void exchange_decide_kernel(int64_t npairs, int64_t C, const int32_t*
   if (ok && total) atomicAdd((unsigned long long*)total, 1ull);
 }
 
-// Swap the columns of accepted pairs: thread (pair k, dimension i).
+// Swap the columns of accepted pairs: thread (pair k, dimension i).  The
+// exchange follows the last proposal's accept step; when that proposal was
+// recorded in the thinned ring, its entry is swapped too, so the recorded
+// sample is the post-exchange state, as in the reference (the sample is
+// appended after the exchange, Samplers.py:589-678).  Its misfit entry is
+// the tempered misfit of the swapped-in model.
 template <typename T>
 __global__ void exchange_swap_kernel(int64_t npairs, int64_t d, int64_t C, const int32_t* __restrict__ pairs,
-                                     const int32_t* __restrict__ swapped, T* q_cur, double* x_cur) {
+                                     const int32_t* __restrict__ swapped, T* q_cur, double* x_cur,
+                                     const int64_t* __restrict__ control, T* ring_q, double* ring_x,
+                                     int64_t ring_slots, int64_t thin, const double* __restrict__ beta) {
+  const int64_t n_last = control ? control[0] - 1 : -1;
+  const bool rec = ring_q != nullptr && n_last >= 0 && n_last % thin == 0;
+  const int64_t slot = rec ? (n_last / thin) % ring_slots : 0;
   const int64_t total = npairs * d;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = e / d, i = e - k * d;
@@ -563,10 +573,19 @@ __global__ void exchange_swap_kernel(int64_t npairs, int64_t d, int64_t C, const
     const T t = q_cur[i * C + a];
     q_cur[i * C + a] = q_cur[i * C + b];
     q_cur[i * C + b] = t;
+    if (rec) {
+      T* r = ring_q + (slot * d + i) * C;
+      r[a] = q_cur[i * C + a];
+      r[b] = q_cur[i * C + b];
+    }
     if (i == 0) {
       const double tx = x_cur[a];
       x_cur[a] = x_cur[b];
       x_cur[b] = tx;
+      if (rec && ring_x) {
+        ring_x[slot * C + a] = (beta ? beta[a] : 1.0) * x_cur[a];
+        ring_x[slot * C + b] = (beta ? beta[b] : 1.0) * x_cur[b];
+      }
     }
   }
 }
@@ -582,8 +601,10 @@ int exchange_impl(const hmc_chains* s, int64_t npairs, const int32_t* pairs, con
   exchange_decide_kernel<<<blocks_for(npairs, 256), 256, 0, st>>>(npairs, s->chains, pairs, u, s->beta, s->x_cur,
                                                                    swapped, total);
   HMC_TRY(check_launch("exchange_decide_kernel"));
-  exchange_swap_kernel<T><<<ew_grid(npairs * s->dims), 256, 0, st>>>(npairs, s->dims, s->chains, pairs, swapped,
-                                                                      (T*)s->q_cur, s->x_cur);
+  if (s->ring_q) HMC_REQUIRE(s->ring_slots > 0 && s->thinning > 0, "hmc_exchange: bad sample ring");
+  exchange_swap_kernel<T><<<ew_grid(npairs * s->dims), 256, 0, st>>>(
+      npairs, s->dims, s->chains, pairs, swapped, (T*)s->q_cur, s->x_cur, s->proposal, (T*)s->ring_q, s->ring_x,
+      s->ring_slots, s->thinning, s->beta);
   return check_launch("exchange_swap_kernel");
 }
 

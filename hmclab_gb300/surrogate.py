@@ -148,6 +148,40 @@ class _Surrogate:
         self.frozen = True
         return self
 
+    # ---- checkpoints -----------------------------------------------------------
+    def _state_tensors(self):
+        """name -> FP32 device tensor of everything training and prediction
+        read (master weights, Adam moments, normalisation); the BF16 copies
+        are derived from these."""
+        raise NotImplementedError
+
+    def state_arrays(self):
+        """Host copies of the surrogate's state: continuing training or
+        sampling from `load_state_arrays` of these is bit for bit the same as
+        continuing this object."""
+        out = {k: v.detach().cpu().numpy().copy() for k, v in self._state_tensors().items()}
+        out["steps"] = _np.array(self.steps, _np.int64)
+        out["frozen"] = _np.array(bool(self.frozen))
+        out["kind"] = _np.array(type(self).__name__)
+        return out
+
+    def load_state_arrays(self, arrays):
+        import torch
+
+        kind = str(arrays["kind"])
+        if kind != type(self).__name__:
+            raise ValueError(f"checkpoint holds a {kind}, not a {type(self).__name__}")
+        for k, t in self._state_tensors().items():
+            a = _np.asarray(arrays[k])
+            if a.shape != tuple(t.shape):
+                raise ValueError(f"checkpoint entry {k} has shape {a.shape}, the surrogate {tuple(t.shape)}")
+            t.copy_(torch.from_numpy(a).to(t.device, t.dtype))
+        self.steps = int(arrays["steps"])
+        self.frozen = bool(arrays["frozen"])
+        self._recast(_dev.stream_handle())
+        torch.cuda.synchronize(self.device)
+        return self
+
     def relative_error(self, data: TrainingSet, rows, stop=None, stream=None):
         """|f(q) - g| / |g| (Frobenius norms) over stored pairs of data: the
         rows [rows, stop) when `stop` is given, else the index tensor `rows`.
@@ -366,6 +400,19 @@ class MLPSurrogate(_Surrogate):
         _lib.call("hmc_mlp_input", self.d, C, q.data_ptr(), self.mu_q.data_ptr(), self.inv_q.data_ptr(),
                   b["X"].data_ptr(), b["A2"].shape[1], stream)
         self._forward(b, C, stream, g_state=g)
+
+    def _state_tensors(self):
+        t = {}
+        for l in range(3):
+            for name, lst in (("W", self.W), ("b", self.b), ("mW", self.mW), ("vW", self.vW), ("mb", self.mb),
+                              ("vb", self.vb)):
+                t[f"{name}{l}"] = lst[l]
+        for name in ("mu_q", "inv_q", "mu_g", "sig_g", "inv_g"):
+            t[name] = getattr(self, name)
+        return t
+
+    def _recast(self, stream):
+        self._cast(stream)
 
     def _snapshot(self):
         return [w.clone() for w in self.W] + [b.clone() for b in self.b]
@@ -636,6 +683,20 @@ class PotentialSurrogate(_Surrogate):
         o = self._out(g=g, accumulate=int(accumulate))
         _lib.call("hmc_tc_mlp", _lib.HMC_MLP_WGRAD, n_in, n_out, B, act_t.data_ptr(), act_t.shape[1],
                   delta_t.data_ptr(), delta_t.shape[1], None, ctypes.byref(o), self.status.data_ptr(), stream)
+
+    def _state_tensors(self):
+        t = {}
+        for k in self.params:
+            t[k] = self.params[k]
+            t["m1_" + k] = self.m1[k]
+            t["m2_" + k] = self.m2[k]
+        for name in ("A", "beta", "mu_q", "inv_q", "mu_g", "sig_g", "inv_g", "scale", "bias_out"):
+            t[name] = getattr(self, name)
+        return t
+
+    def _recast(self, stream):
+        self._cast(stream)
+        self._cast_quadratic(stream)
 
     def _snapshot(self):
         return {k: v.clone() for k, v in self.params.items()}

@@ -176,7 +176,11 @@ HMC_API int hmc_end_trajectory(const hmc_chains* s, void* stream);
  * iff exp((beta[a] - beta[b]) * (x_cur[a] - x_cur[b])) > u[k] (the sum of
  * both chains' misfit improvements; FP64, NaN rejects).  Positions and
  * misfits move; step sizes stay with their chain.  swapped[k] receives the
- * decision; accepted_total (nullable) counts the swaps.                    */
+ * decision; accepted_total (nullable) counts the swaps.  When the last
+ * completed proposal (proposal counter - 1) was recorded in the thinned
+ * ring, its ring entry is swapped too (the reference appends the sample
+ * after the exchange, Samplers.py:675-678), with the tempered misfit of the
+ * swapped-in model.                                                        */
 HMC_API int hmc_exchange(const hmc_chains* s, int64_t npairs,
                          const int32_t* pairs, const double* u,
                          int32_t* swapped, int64_t* accepted_total,

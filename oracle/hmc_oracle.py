@@ -262,6 +262,50 @@ class SourceLocation3D:
         return out
 
 
+class Tempered:
+    """Per-chain tempered target: chain c has misfit beta[c] * U and gradient
+    beta[c] * grad U (the reference tempers by giving each parallel chain its
+    own distribution with the misfit divided by the temperature)."""
+
+    def __init__(self, dist, beta):
+        self.dist = dist
+        self.beta = np.asarray(beta, float).reshape(-1)
+
+    def misfit(self, M):
+        return self.beta * self.dist.misfit(M)
+
+    def gradient(self, M):
+        return self.beta[None, :] * self.dist.gradient(M)
+
+
+def run_tempered_exchange(dist, beta, mass, q0, eps0, streams, proposals, interval, schedule, exchange_u,
+                          amount_of_steps=10):
+    """Parallel tempering as the reference's ParallelSampleSMP runs it
+    (Samplers.py:529-704 with the exchange section 589-669 and the schedule
+    of 1872-1885): every chain makes one proposal on its tempered target;
+    after proposals n with n % interval == 0 the pairs of schedule row
+    n // interval (entries 2j, 2j+1) swap models iff
+    exp(improvement_a + improvement_b) > u; then the sample is recorded.
+    The recorded misfit is the chain's current misfit, which the reference's
+    exchange leaves unchanged, so a swapped chain records its pre-swap value.
+    Returns samples [N][d+1][C] and the swap decisions [E][pairs]."""
+    z, f, u = streams
+    beta = np.asarray(beta, float)
+    tdist = Tempered(dist, beta)
+    q = np.array(q0, float, copy=True)
+    out, decisions = [], []
+    for n in range(proposals):
+        res = run_chains(tdist, mass, q, eps0, (z[n:n + 1], f[n:n + 1], u[n:n + 1]), 1,
+                         amount_of_steps=amount_of_steps)
+        q, x = res["q"], res["x"]
+        if n % interval == 0 and n // interval < len(schedule):
+            pairs = np.asarray(schedule[n // interval]).reshape(-1, 2)
+            q, _, sw = exchange(q, x / beta, beta, pairs, exchange_u[n // interval])
+            decisions.append(sw)
+        out.append(np.vstack([q, x[None, :]]))
+    return np.array(out), np.array(decisions)
+
+
 class Sum:
     """BayesRule / AdditiveDistribution (base.py:1036-1054): sum in list order."""
 

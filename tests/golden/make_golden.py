@@ -416,6 +416,49 @@ def case_blob_projection():
          fine_model=blob.forward_transform_background(m))
 
 
+def case_replica_exchange():
+    """Parallel tempering through the reference's own ParallelSampleSMP
+    (Samplers.py:1807-1977, forked chains exchanging over pipes,
+    Samplers.py:589-669): four chains on Normal posteriors tempered by
+    T = 1, 2, 4, 8, exchanges after proposals 0, 2, 4, ...  Stored: the
+    exchange schedule, every chain's samples file, and the random streams
+    each chain's generator produced in the reference's draw order, with the
+    exchange uniform the pair's second ("master") chain draws after its
+    accept draw."""
+    d, C, P, interval = 3, 4, 20, 2
+    temps = np.array([1.0, 2.0, 4.0, 8.0])
+    mean = np.arange(d, dtype=float).reshape(d, 1)
+    var = np.array([1.0, 2.0, 0.5]).reshape(d, 1)
+    seeds = [100 + i for i in range(C)]
+    with tempfile.TemporaryDirectory() as tmp:
+        fns = [os.path.join(tmp, f"chain{i}.npy") for i in range(C)]
+        psmp = hmclab.Samplers.ParallelSampleSMP(seed=7)
+        psmp.sample([hmclab.Samplers.HMC(seed=s) for s in seeds], fns, [D.Normal(mean.copy(), var * T) for T in temps],
+                    overwrite_existing_files=True, proposals=P, exchange=True, exchange_interval=interval,
+                    initial_model=[mean.copy() for _ in range(C)],
+                    kwargs={"stepsize": 0.5, "amount_of_steps": 3, "disable_progressbar": True})
+        samples = np.stack([np.load(fn).T for fn in fns], axis=-1)  # (d+1, N, C)
+    sched = np.asarray(psmp.exchange_schedule)
+    npairs = C // 2
+    z = np.empty((P, d, C))
+    f = np.empty((P, C))
+    u = np.empty((P, C))
+    uex = np.full((sched.shape[0], npairs), np.nan)
+    for c, seed in enumerate(seeds):
+        rng = np.random.default_rng(seed)
+        for n in range(P):
+            z[n, :, c] = rng.normal(size=(d, 1))[:, 0]
+            f[n, c] = rng.uniform(0.5, 1.5)
+            u[n, c] = rng.uniform(0, 1)
+            if n % interval == 0:
+                row = sched[n // interval]
+                pos = int(np.where(row == c)[0][0]) if c in row else -1
+                if pos >= 0 and pos % 2 == 1:  # odd position: the pair's master draws the uniform
+                    uex[n // interval, pos // 2] = rng.uniform(0, 1)
+    save("replica_exchange.npz", mean=mean, var=var, temps=temps, interval=interval, stepsize=0.5, amount_of_steps=3,
+         schedule=sched, samples=samples, z=z, f=f, u=u, exchange_u=uex)
+
+
 if __name__ == "__main__":
     case_cfg1()
     case_public_linearmatrix()
@@ -426,3 +469,4 @@ if __name__ == "__main__":
     case_full_mass_bounds()
     case_integrators_autotune()
     case_blob_projection()
+    case_replica_exchange()

@@ -135,3 +135,24 @@ def test_integrators_and_autotune(golden):
     np.testing.assert_allclose(res["stepsizes"][:n, 0], g["auto_stepsizes"], rtol=1e-13)
     np.testing.assert_allclose(res["acceptance_rates"][:n, 0], g["auto_rates"], rtol=1e-12)
     np.testing.assert_allclose(res["stepsize"][0], g["auto_final_stepsize"], rtol=1e-13)
+
+
+def test_oracle_replica_exchange_matches_reference_parallel_sampler(golden):
+    """The oracle's parallel-tempering restatement replays the reference's
+    own ParallelSampleSMP run (fixture from the reference: schedule, samples
+    files, per-chain streams) to 1e-12: same pairing convention, exchange
+    after proposals 0, interval, ..., same acceptance, samples recorded after
+    the exchange (with the pre-swap misfit the reference keeps)."""
+    g = golden("replica_exchange.npz")
+    d = g["mean"].shape[0]
+    beta = 1.0 / g["temps"]
+    C = beta.size
+    P = g["z"].shape[0]
+    q0 = np.repeat(g["mean"], C, axis=1)
+    samples, decisions = O.run_tempered_exchange(
+        O.NormalDiag(g["mean"][:, 0], g["var"][:, 0]), beta, O.Mass("unit"), q0, float(g["stepsize"]),
+        (g["z"], g["f"], g["u"]), P, int(g["interval"]), g["schedule"], g["exchange_u"],
+        amount_of_steps=int(g["amount_of_steps"]))
+    ref = np.transpose(g["samples"], (1, 0, 2))  # N, d+1, C
+    np.testing.assert_allclose(samples, ref, rtol=1e-12, atol=1e-12)
+    assert decisions.any() and not decisions.all()  # the fixture exercises both outcomes
