@@ -100,31 +100,22 @@ class PersistentDense:
 
     def autotune(self, h, proposals=4):
         """Time every chains-per-block choice on dry runs (which write no
-        state) of the live chains and keep the fastest."""
-        import torch
+        state) of the live chains and keep the fastest (cached per problem
+        shape by hmclab_gb300.autotune, in memory and on disk)."""
+        from hmclab_gb300 import autotune as _autotune
 
         if self.warps is not None:
             return self.warps
-        st = self.smp.stream
         slen = self.smp._state.stream_len
         if slen > 0:
             proposals = min(proposals, slen)
-        best = None
         full = self.smp.mass_matrix.kind == _lib.HMC_MASS_FULL
         esize = 8 if self.smp.dtype == "float64" else 4
-        for w in _WARPS:
-            if _smem(self.smp.dimensions, full, w, esize) > _SMEM:
-                continue
-            self._call(1, w, True, h)  # warm
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            self._call(proposals, w, True, h)
-            e1.record(st)
-            st.synchronize()
-            t = e0.elapsed_time(e1)
-            if best is None or t < best[0]:
-                best = (t, w)
-        self.warps = best[1]
+        cands = [(w,) for w in _WARPS if _smem(self.smp.dimensions, full, w, esize) <= _SMEM]
+        shape = {"d": self.key[0], "C": self.key[1], "dtype": self.key[2], "mass": int(self.key[3]),
+                 "prior": self.key[4], "steps": self.key[5]}
+        (self.warps,) = _autotune.choose("persistent_dense", shape, cands,
+                                         lambda c: self._call(proposals, c[0], True, h), self.smp.device, h, reps=1)
         _tuned[self.key] = self.warps
         return self.warps
 

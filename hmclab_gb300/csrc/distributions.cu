@@ -505,6 +505,128 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
   }
 }
 
+// FP32 source location with the per-pair work cut to the arithmetic that
+// matters (the kernel above is issue-bound, so instructions are the lever):
+//   - stations staged as float4 (x, y, z, -) and the pair data of 16 events x
+//     a chunk of stations as float2 (w, o) = (1 / std^2, observed time), both
+//     in shared memory; a NaN observation or weight is staged as (0, 0), which
+//     makes every term of that pair zero — the nansum of the reference
+//     (SourceLocation.py:495-540) without a NaN test per pair;
+//   - one reciprocal square root per pair of the distance clamped below by
+//     1e-30 (an event on a station then contributes zero partials, nansum's
+//     treatment of 0 / 0);
+//   - 1 / v is factored out of the x, y, z partials and 1 / v^2 out of the
+//     velocity partial: per pair k = (t_calc - o) w / dist, and the thread
+//     accumulates k dx, k dy, k dz, (t_calc - o) w and (t_calc - o) w dist;
+//   - misfit terms are summed in FP32 over at most SL_CHUNK stations, then in
+//     FP64.
+constexpr int SL_CHUNK = 512;
+
+template <bool GRAD>
+__global__ void srcloc_f32_kernel(int64_t E, int64_t S, int64_t C, const float* __restrict__ M,
+                                  const float* __restrict__ rx, const float* __restrict__ ry,
+                                  const float* __restrict__ rz, const float* __restrict__ obs,
+                                  const float* __restrict__ iv, int infer_v, float v_fixed, double* out_x,
+                                  float* out_g, int accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* st = (float4*)smem_raw;                 // [SL_CHUNK]
+  float2* pw = (float2*)(st + SL_CHUNK);          // [SL_EY][SL_CHUNK]
+  __shared__ double red[SL_EY][RED_X + 1];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
+  const bool live = c < C;
+  const float v = live ? (infer_v ? M[(4 * E) * C + c] : v_fixed) : 1.f;
+  const float inv_v = 1.f / v;
+  double mis = 0.0, gvd_total = 0.0;
+  for (int64_t e0 = 0; e0 < E; e0 += SL_EY) {
+    const int64_t e = e0 + threadIdx.y;
+    const bool ev = live && e < E;
+    float x = 0.f, y = 0.f, z = 0.f, t0 = 0.f;
+    if (ev) {
+      x = M[(4 * e + 0) * C + c];
+      y = M[(4 * e + 1) * C + c];
+      z = M[(4 * e + 2) * C + c];
+      t0 = M[(4 * e + 3) * C + c];
+    }
+    float gx = 0.f, gy = 0.f, gz = 0.f, gT = 0.f, gvd = 0.f;
+    for (int64_t s0 = 0; s0 < S; s0 += SL_CHUNK) {
+      const int sn = (int)(S - s0 < SL_CHUNK ? S - s0 : SL_CHUNK);
+      __syncthreads();  // the previous chunk is consumed
+      for (int k = tid; k < sn; k += nthr) st[k] = make_float4(rx[s0 + k], ry[s0 + k], rz[s0 + k], 0.f);
+      for (int k = tid; k < SL_EY * sn; k += nthr) {
+        const int ye = k / sn, ks = k - ye * sn;
+        const int64_t ee = e0 + ye;
+        float w = 0.f, o = 0.f;
+        if (ee < E) {
+          w = iv[ee * S + s0 + ks];
+          o = obs[ee * S + s0 + ks];
+          if (isnan(w) || isnan(o)) w = o = 0.f;
+        }
+        pw[ye * SL_CHUNK + ks] = make_float2(w, o);
+      }
+      __syncthreads();
+      if (!ev) continue;
+      const float2* my = pw + threadIdx.y * SL_CHUNK;
+      float ms = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < sn; ++k) {
+        const float4 q = st[k];
+        const float2 p = my[k];
+        const float dx = x - q.x, dy = y - q.y, dz = z - q.z;
+        const float r2 = fmaxf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)), 1e-30f);
+        const float inv = rsqrtf(r2);
+        const float dist = r2 * inv;
+        const float res = fmaf(dist, inv_v, t0) - p.y;  // t_calc - obs
+        if (GRAD) {
+          const float mg = res * p.x;
+          const float k2 = mg * inv;
+          gx = fmaf(k2, dx, gx);
+          gy = fmaf(k2, dy, gy);
+          gz = fmaf(k2, dz, gz);
+          gT += mg;
+          gvd = fmaf(mg, dist, gvd);
+        } else {
+          ms = fmaf(res * res, p.x, ms);
+        }
+      }
+      if (!GRAD) mis += (double)ms;
+    }
+    if (GRAD && ev) {
+      const int64_t o0 = (4 * e) * C + c;
+      const float ax = gx * inv_v, ay = gy * inv_v, az = gz * inv_v;
+      if (accumulate) {
+        out_g[o0] += ax;
+        out_g[o0 + C] += ay;
+        out_g[o0 + 2 * C] += az;
+        out_g[o0 + 3 * C] += gT;
+      } else {
+        out_g[o0] = ax;
+        out_g[o0 + C] = ay;
+        out_g[o0 + 2 * C] = az;
+        out_g[o0 + 3 * C] = gT;
+      }
+      gvd_total += (double)gvd;
+    }
+  }
+  // Reduce the velocity partial (or the misfit) over the event lanes.
+  red[threadIdx.y][threadIdx.x] = GRAD ? gvd_total : mis;
+  __syncthreads();
+  if (threadIdx.y == 0 && live) {
+    double sum = 0.0;
+    for (int yy = 0; yy < SL_EY; ++yy) sum += red[yy][threadIdx.x];
+    if (GRAD) {
+      if (infer_v) {
+        const int64_t o = (4 * E) * C + c;
+        const float gv = (float)(-sum) * inv_v * inv_v;
+        out_g[o] = accumulate ? out_g[o] + gv : gv;
+      }
+    } else {
+      const double val = 0.5 * sum;
+      out_x[c] = accumulate ? out_x[c] + val : val;
+    }
+  }
+}
+
 template <typename T>
 int srcloc(bool grad, int64_t E, int64_t S, int64_t C, const void* M, const void* rx, const void* ry, const void* rz,
            const void* obs, const void* iv, int infer_v, double v_fixed, double* out_x, void* out_g, int accumulate,
@@ -514,6 +636,24 @@ int srcloc(bool grad, int64_t E, int64_t S, int64_t C, const void* M, const void
   if (C == 0) return HMC_OK;
   HMC_REQUIRE(M && rx && ry && rz && obs && iv, "%s: null argument", who);
   HMC_REQUIRE(grad ? out_g != nullptr : out_x != nullptr, "%s: null output", who);
+  if (sizeof(T) == 4) {
+    const size_t smem = SL_CHUNK * sizeof(float4) + (size_t)SL_EY * SL_CHUNK * sizeof(float2);
+    auto k32 = grad ? srcloc_f32_kernel<true> : srcloc_f32_kernel<false>;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaError_t e1 = cudaFuncSetAttribute(srcloc_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem);
+      cudaError_t e2 = cudaFuncSetAttribute(srcloc_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem);
+      if (e1 != cudaSuccess || e2 != cudaSuccess)
+        return cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaFuncSetAttribute(srcloc_f32)");
+      attr_set = true;
+    }
+    k32<<<red_grid(C), dim3(RED_X, SL_EY), smem, st>>>(E, S, C, (const float*)M, (const float*)rx, (const float*)ry,
+                                                        (const float*)rz, (const float*)obs, (const float*)iv, infer_v,
+                                                        (float)v_fixed, out_x, (float*)out_g, accumulate);
+    return check_launch(who);
+  }
   const size_t smem = 3 * (size_t)S * sizeof(T);
   HMC_REQUIRE(smem <= 160 * 1024, "%s: too many stations (%lld)", who, (long long)S);
   auto kern = grad ? srcloc_kernel<T, true> : srcloc_kernel<T, false>;
