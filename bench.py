@@ -898,7 +898,7 @@ def run_fwi_arm(args, wl):
     t_setup = time.perf_counter() - t_setup
 
     # ---- exact proposals from the start states, recording training pairs --
-    data = S.TrainingSet(d, Nb * L * C)
+    data = S.TrainingSet(d, Nb * L * C, values=args.value_weight > 0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=q_init, proposals=Nb,
@@ -910,6 +910,8 @@ def run_fwi_arm(args, wl):
     # ---- surrogate training on the device ---------------------------------
     kind = S.PotentialSurrogate if args.surrogate == "potential" else S.MLPSurrogate
     net = kind(d, hidden=wl.hidden, seed=rank)
+    if args.surrogate == "potential":
+        net.value_weight = args.value_weight
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     fit = net.fit(data, steps=args.train_steps, batch=256, lr=1e-3, holdout_fraction=0.1)
@@ -924,8 +926,8 @@ def run_fwi_arm(args, wl):
     # for the timed run.  --surrogate-L / --surrogate-stepsize fix it.
     pilot = []
     if args.surrogate_L is None or args.surrogate_stepsize is None:
-        tau_max = wl.stepsize * wl.L
-        for L_s in (2, 4, 8, 16):
+        tau_max = args.pilot_max_length * wl.stepsize * wl.L
+        for L_s in (2, 4, 8, 16, 32):
             for eps_s in (0.03, 0.06, 0.12):
                 if L_s * eps_s > tau_max + 1e-9:
                     continue
@@ -1037,6 +1039,9 @@ def run_fwi_arm(args, wl):
         "surrogate": {"kind": args.surrogate, "train_steps": args.train_steps, "train_seconds": t_train,
                       "train_pairs": fit["train_pairs"], "heldout_pairs": fit["heldout_pairs"],
                       "heldout_rel_error_linear_start": fit["heldout"][0][1], "heldout_rel_error": fit["best_heldout"],
+                      "value_weight": args.value_weight if args.surrogate == "potential" else None,
+                      "heldout_value_error": fit.get("best_heldout_value"),
+                      "heldout_value_error_start": (fit.get("heldout_value") or [(0, None)])[0][1],
                       "best_step": fit["best_step"]},
         "setup_seconds": t_setup,
         "e2e": {"value": e2e_measured if not reasons else None, "value_measured": e2e_measured, "unit": UNIT,
@@ -1212,6 +1217,10 @@ def main():
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
     ap.add_argument("--plain-steps", type=int, default=3, help="fwi: timed proposals of plain HMC (its cost)")
     ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
+    ap.add_argument("--value-weight", type=float, default=1.0,
+                    help="fwi: weight of the misfit-value matching loss of the potential surrogate (0: gradients only)")
+    ap.add_argument("--pilot-max-length", type=float, default=2.0,
+                    help="fwi: longest surrogate trajectory the pilot tries, in units of plain HMC's")
     ap.add_argument("--burn-in", type=int, default=None,
                     help="fwi: exact proposals recording the surrogate's training pairs (independent of --warmup)")
     ap.add_argument("--train-steps", type=int, default=10000, help="fwi: Adam steps of the surrogate")

@@ -137,6 +137,11 @@ class _AbstractDistribution:
     def _device_gradient(self, M, out, accumulate, dtype, stream):
         raise _AbstractMethodError()
 
+    def _device_misfit_after_gradient(self, M, out, accumulate, dtype, stream):
+        """The misfit at M, called right after _device_gradient at the same
+        M (targets whose gradient runs a forward simulation reuse it)."""
+        self._device_misfit(M, out, accumulate, dtype, stream)
+
     # ---- device parameter / scratch caches ---------------------------------
     def _params(self, dtype):
         cache = self.__dict__.setdefault("_param_cache", {})
@@ -160,6 +165,7 @@ class _AbstractDistribution:
         state = self.__dict__.copy()
         state.pop("_param_cache", None)
         state.pop("_scratch_cache", None)
+        state.pop("_last_gradient_descriptor", None)
         return state
 
     # ---- reference API kept as is -----------------------------------------
@@ -390,6 +396,10 @@ class AdditiveDistribution(_AbstractDistribution):
     def _device_gradient(self, M, out, accumulate, dtype, stream):
         for k, dist in enumerate(self.separate_distributions):
             dist._device_gradient(M, out, accumulate or k > 0, dtype, stream)
+
+    def _device_misfit_after_gradient(self, M, out, accumulate, dtype, stream):
+        for k, dist in enumerate(self.separate_distributions):
+            dist._device_misfit_after_gradient(M, out, accumulate or k > 0, dtype, stream)
 
     def check_device_status(self):
         for dist in self.separate_distributions:
@@ -898,6 +908,17 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         d = self._forward_all(M, ws, stream, False)
         _lib.call("hmc_fwi_misfit", ctypes.byref(d), self.config.n_shots, out.data_ptr(), int(accumulate), stream)
 
+    def _device_misfit_after_gradient(self, M, out, accumulate, dtype, stream):
+        """The misfit of the records the gradient's forward simulation left
+        in the workspace (the reduction only: no second forward)."""
+        import ctypes
+
+        self._check_dtype(dtype)
+        d = getattr(self, "_last_gradient_descriptor", None)
+        if d is None or d.chains != M.shape[1]:
+            return self._device_misfit(M, out, accumulate, dtype, stream)
+        _lib.call("hmc_fwi_misfit", ctypes.byref(d), self.config.n_shots, out.data_ptr(), int(accumulate), stream)
+
     def _device_gradient(self, M, out, accumulate, dtype, stream):
         import ctypes
 
@@ -905,6 +926,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         C = M.shape[1]
         ws = self._workspace(C, M.device, True)
         d = self._forward_all(M, ws, stream, True)
+        self._last_gradient_descriptor = d
         _lib.call("hmc_fwi_param_gradient", ctypes.byref(d), ws["g_rho"].data_ptr(), ws["g_vp"].data_ptr(),
                   ws["g_vs"].data_ptr(), 0, stream)
         p = self._params("float32")

@@ -544,6 +544,7 @@ class HMC:
         )
         if self.surrogate is not None:
             self.surrogate._buffers(C, False)  # allocate before any capture
+        self._training_x = Z((C,), "float64") if self.training_set is not None else None
 
     # ------------------------------------------------------------------
     def _phase(self, name):
@@ -579,7 +580,11 @@ class HMC:
                     else:
                         dist._device_gradient(self.q, self.g, False, dt, h)
                         if self.training_set is not None:
-                            self.training_set.record(self.q, self.g, h)
+                            tx = None
+                            if self.training_set.with_values:
+                                tx = self._training_x
+                                dist._device_misfit_after_gradient(self.q, tx, False, dt, h)
+                            self.training_set.record(self.q, self.g, h, tx)
             with self._phase("integrator"):
                 _lib.call("hmc_kick_drift", st, kick, drift, h)
         with self._phase("misfit"):

@@ -232,6 +232,9 @@ SIGNATURES = {
     "hmc_pot_w3_grad": [I64, I64, P, I64, P, I64, P, S],
     "hmc_pot_loss": [I64, I64, P, I64, P, I64, P, P, I64, P, I64, P, S],
     "hmc_pot_scaled_cast": [I64, I64, P, I64, I, P, P, I64, I64, S],
+    "hmc_pot_value_residual": [I64, I64, P, I64, P, P, P, _ct.c_float, P, P, S],
+    "hmc_pot_weighted_colsum": [I64, I64, P, I64, P, P, S],
+    "hmc_pot_scale_columns": [I64, I64, P, I64, P, P, I64, S],
     "hmc_fwi_prepare": [P, S],
     "hmc_fwi_forward_shot": [P, I, I, I, I, S],
     "hmc_fwi_misfit": [P, I, P, I, S],

@@ -136,6 +136,76 @@ __global__ void sum_kernel(int n, const double* __restrict__ p, double scale, do
   if (threadIdx.x == 0) *out = s * scale;
 }
 
+// Value matching.  The exact misfit U is known wherever an exact gradient
+// was taken (the forward simulation that precedes an adjoint gives it), and
+// the acceptance of a surrogate trajectory depends on how well f tracks U
+// between its end points, so the loss can also match values:
+//   L_v = 0.5 w mean_b (r_b - rbar)^2,  r_b = v_b - t_b,  v_b = w3 . a2_b,
+// with t_b = U_b minus the (fixed) quadratic part at x_b; centring on the
+// batch mean removes the potential's free constant.  dL_v / dv_b =
+// w (r_b - rbar) / B = dv_b, and the weight gradients are those of v scaled
+// per row: dw3 += sum_b dv_b a2_b, dz2_b = dv_b delta2_b, dz1_b = dv_b delta1_b
+// (delta2 = w3 GELU'(z2) and delta1 = (W2^T delta2) GELU'(z1) are the
+// gradient pass's own intermediates).
+// One block of B <= 1024 threads; a2 is the forward pass's BF16 activation.
+__global__ void value_residual_kernel(int B, int h, const __nv_bfloat16* __restrict__ a2, int64_t lda,
+                                      const float* __restrict__ w3, const double* __restrict__ targets,
+                                      const int32_t* __restrict__ idx, float weight, float* dv, double* loss) {
+  __shared__ double sh[1024];
+  const int b = threadIdx.x;
+  double r = 0.0;
+  if (b < B) {
+    float v = 0.f;
+    for (int j = 0; j < h; ++j) v = fmaf(w3[j], __bfloat162float(a2[(int64_t)b * lda + j]), v);
+    r = (double)v - targets[idx[b]];
+  }
+  sh[b] = r;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {  // fixed-order tree: deterministic
+    if (b < w && b + w < (int)blockDim.x) sh[b] += sh[b + w];
+    __syncthreads();
+  }
+  const double rbar = sh[0] / B;
+  __syncthreads();
+  const double c = b < B ? r - rbar : 0.0;
+  if (b < B) dv[b] = (float)(weight * c / B);
+  sh[b] = c * c;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (b < w && b + w < (int)blockDim.x) sh[b] += sh[b + w];
+    __syncthreads();
+  }
+  if (b == 0) *loss = 0.5 * weight * sh[0] / B;
+}
+
+// out[j] += sum_b dv[b] in[b][j] (in BF16 [B][ld]); block: 32 columns x 16
+// batch rows, partial sums added in a fixed order.
+__global__ void weighted_colsum_kernel(int64_t B, int64_t n, const __nv_bfloat16* __restrict__ in, int64_t ld,
+                                       const float* __restrict__ dv, float* out) {
+  __shared__ float part[16][33];
+  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  float s = 0.f;
+  if (j < n)
+    for (int64_t b = threadIdx.y; b < B; b += 16) s = fmaf(dv[b], __bfloat162float(in[b * ld + j]), s);
+  part[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && j < n) {
+    float t = 0.f;
+    for (int y = 0; y < 16; ++y) t += part[y][threadIdx.x];
+    out[j] += t;
+  }
+}
+
+// out_t[r][b] = in_t[r][b] dv[b] (BF16, rows x B of [rows][ld] arrays).
+__global__ void scale_columns_kernel(int64_t rows, int64_t B, const __nv_bfloat16* __restrict__ in_t, int64_t ldi,
+                                     const float* __restrict__ dv, __nv_bfloat16* out_t, int64_t ldo) {
+  const int64_t total = rows * B;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = k / B, b = k - r * B;
+    out_t[r * ldo + b] = __float2bfloat16_rn(__bfloat162float(in_t[r * ldi + b]) * dv[b]);
+  }
+}
+
 // dst[r][k0 + k] = bf16(scale[r] * src(r, k)) for r < rows, k < cols, with
 // src(r, k) = src[k][r] (transposed) or src[r][k].
 __global__ void scaled_cast_kernel(int64_t rows, int64_t cols, const float* __restrict__ src, int64_t lds,
@@ -221,6 +291,33 @@ HMC_API int hmc_pot_loss(int64_t B, int64_t n, const float* y, int64_t ldy, cons
   HMC_TRY(check_launch("pot loss_kernel"));
   sum_kernel<<<1, 32, 0, as_stream(stream)>>>((int)grid, loss + 1, 1.0 / (double)B, loss);
   return check_launch("pot sum_kernel");
+}
+
+HMC_API int hmc_pot_value_residual(int64_t B, int64_t h, const void* a2, int64_t lda, const float* w3,
+                                   const double* targets, const int32_t* idx, float weight, float* dv, double* loss,
+                                   void* stream) {
+  HMC_REQUIRE(B > 0 && B <= 1024 && h > 0 && lda >= h, "hmc_pot_value_residual: bad sizes");
+  HMC_REQUIRE(a2 && w3 && targets && idx && dv && loss, "hmc_pot_value_residual: null argument");
+  value_residual_kernel<<<1, 1024, 0, as_stream(stream)>>>((int)B, (int)h, (const __nv_bfloat16*)a2, lda, w3,
+                                                           targets, idx, weight, dv, loss);
+  return check_launch("pot value_residual_kernel");
+}
+
+HMC_API int hmc_pot_weighted_colsum(int64_t B, int64_t n, const void* in, int64_t ld, const float* dv, float* out,
+                                    void* stream) {
+  HMC_REQUIRE(B > 0 && n > 0 && ld >= n && in && dv && out, "hmc_pot_weighted_colsum: bad arguments");
+  weighted_colsum_kernel<<<(unsigned)((n + 31) / 32), dim3(32, 16), 0, as_stream(stream)>>>(
+      B, n, (const __nv_bfloat16*)in, ld, dv, out);
+  return check_launch("pot weighted_colsum_kernel");
+}
+
+HMC_API int hmc_pot_scale_columns(int64_t rows, int64_t B, const void* in_t, int64_t ldi, const float* dv,
+                                  void* out_t, int64_t ldo, void* stream) {
+  HMC_REQUIRE(rows > 0 && B > 0 && ldi >= B && ldo >= B && in_t && dv && out_t, "hmc_pot_scale_columns: bad arguments");
+  const unsigned g = blocks_for(rows * B, 256);
+  scale_columns_kernel<<<g > 4096u ? 4096u : g, 256, 0, as_stream(stream)>>>(
+      rows, B, (const __nv_bfloat16*)in_t, ldi, dv, (__nv_bfloat16*)out_t, ldo);
+  return check_launch("pot scale_columns_kernel");
 }
 
 HMC_API int hmc_pot_scaled_cast(int64_t rows, int64_t cols, const float* src, int64_t lds, int transposed,

@@ -41,24 +41,38 @@ def _pad(n):
 
 
 class TrainingSet:
-    """Device stores of (position, exact gradient) pairs, [capacity][d] FP32."""
+    """Device stores of (position, exact gradient) pairs, [capacity][d] FP32,
+    and with `values=True` the exact misfit at each position ([capacity]
+    FP64; the sampler fills it from the forward simulation that precedes
+    each exact gradient, where the target offers that)."""
 
-    def __init__(self, dimensions, capacity, device=None):
+    def __init__(self, dimensions, capacity, device=None, values=False):
         import torch
 
         device = device or _dev.require_cuda()
         self.d, self.capacity = int(dimensions), int(capacity)
         self.q = torch.zeros((self.capacity, self.d), dtype=torch.float32, device=device)
         self.g = torch.zeros_like(self.q)
+        self.x = torch.full((self.capacity,), float("nan"), dtype=torch.float64, device=device) if values else None
         self.count = 0
 
-    def record(self, q, g, stream):
-        """Append the columns of q, g ([d][C] device tensors) as C new rows."""
+    @property
+    def with_values(self):
+        return self.x is not None
+
+    def record(self, q, g, stream, x=None):
+        """Append the columns of q, g ([d][C] device tensors) as C new rows
+        (and x [C], the misfits at q, when the set keeps values)."""
+        import torch
+
         C = q.shape[1]
         if self.count + C > self.capacity:
             return False
         _lib.call("hmc_mlp_record", self.d, C, q.data_ptr(), self.q.data_ptr(), self.count, stream)
         _lib.call("hmc_mlp_record", self.d, C, g.data_ptr(), self.g.data_ptr(), self.count, stream)
+        if self.x is not None and x is not None:
+            with torch.cuda.stream(torch.cuda.ExternalStream(stream, device=self.q.device)):
+                self.x[self.count:self.count + C].copy_(x)
         self.count += C
         return True
 
@@ -74,11 +88,14 @@ class _Surrogate:
     @staticmethod
     def _finite_rows(data: TrainingSet, n):
         """Indices (host) of the first n stored pairs whose position and
-        gradient are finite: trajectories that diverged record non-finite
-        gradients, which must not reach the normalisation or the loss."""
+        gradient (and misfit, when kept) are finite: trajectories that
+        diverged record non-finite values, which must not reach the
+        normalisation or the loss."""
         import torch
 
         ok = torch.isfinite(data.q[:n]).all(dim=1) & torch.isfinite(data.g[:n]).all(dim=1)
+        if data.with_values:
+            ok &= torch.isfinite(data.x[:n])
         return _np.flatnonzero(ok.cpu().numpy())
 
     def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
@@ -118,9 +135,18 @@ class _Surrogate:
         train_rows = _np.sort(perm[n_hold:])
         assert len(train_rows) >= batch, "not enough training pairs"
         self.fit_normalization(data, rows=train_rows)
-        err0 = self.relative_error(data, held, stream=stream)
-        best = (err0, 0, self._snapshot())
-        errors = [(0, err0)]
+        value_err = getattr(self, "value_error", None)
+
+        def score():
+            # model selection: the held-out value error when values are
+            # matched (what the acceptance sees), else the gradient error
+            e = self.relative_error(data, held, stream=stream)
+            ve = value_err(data, held, stream=stream) if value_err is not None else None
+            return e, ve, (ve if ve is not None else e)
+
+        err0, verr0, s0 = score()
+        best = (s0, 0, self._snapshot())
+        errors, verrors = [(0, err0)], [(0, verr0)]
         history = []
         done = 0
         while done < steps:
@@ -133,15 +159,18 @@ class _Surrogate:
                 if k % 50 == 0:
                     history.append((k, float(loss[0].item())))
             done += chunk
-            e = self.relative_error(data, held, stream=stream)
+            e, ve, sc = score()
             errors.append((done, e))
-            if e < best[0]:
-                best = (e, done, self._snapshot())
+            verrors.append((done, ve))
+            if sc < best[0]:
+                best = (sc, done, self._snapshot())
         self.check_status()
         self._restore(best[2])
         self._cast(_dev.stream_handle(stream))
         torch.cuda.synchronize(self.device)
-        return {"history": history, "heldout": errors, "best_step": best[1], "best_heldout": best[0],
+        at_best = dict(errors)[best[1]]
+        return {"history": history, "heldout": errors, "heldout_value": verrors, "best_step": best[1],
+                "best_heldout": at_best, "best_heldout_value": dict(verrors)[best[1]],
                 "train_pairs": len(train_rows), "heldout_pairs": n_hold, "skipped_pairs": data.count - n}
 
     def freeze(self):
@@ -499,6 +528,11 @@ class PotentialSurrogate(_Surrogate):
         self.Wg = torch.zeros((d, _pad(self.kg)), **bf)  # [scale W1^T | scale A]
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.loss_buf = torch.zeros(1025, dtype=torch.float64, device=self.device)
+        self.value_loss = torch.zeros(1, dtype=torch.float64, device=self.device)
+        # value matching (off unless value_weight > 0 and the training set keeps misfits)
+        self.value_weight = 0.0
+        self._vt = None  # per stored pair: U minus the quadratic part (FP64, device)
+        self._vt_w = 0.0
         self.steps = 0
         self._bufs = {}
         h = _dev.stream_handle()
@@ -533,6 +567,7 @@ class PotentialSurrogate(_Surrogate):
                 "ZB1p": z((B, h1), f32), "DB2": z((B, h2), f32),
                 "ZB2": z((B, _pad(h2)), bf), "ZB2t": z((h2, pB), bf),
                 "AB1": z((B, h1), f32), "ZB1": z((B, _pad(h1)), bf), "ZB1t": z((h1, pB), bf),
+                "dv": z((B,), f32), "S2t": z((h2, pB), bf), "S1t": z((h1, pB), bf),
             })
         self._bufs[key] = b
         return b
@@ -627,7 +662,52 @@ class PotentialSurrogate(_Surrogate):
         h = _dev.stream_handle()
         self._cast(h)
         self._cast_quadratic(h)
+        self._value_targets(data, rows, A, beta)
         torch.cuda.synchronize(self.device)
+
+    def _value_targets(self, data: TrainingSet, rows, A, beta):
+        """Value-matching targets of every stored pair: the exact misfit
+        minus the quadratic part x^T A x / 2 + beta . x (the part the network
+        does not learn), and the loss weight value_weight / var(targets)."""
+        import torch
+
+        self._vt = None
+        if not (self.value_weight > 0 and data.with_values):
+            return
+        n = data.count
+        q = data.q[:n].double().cpu().numpy()
+        x = (q - self.mu_q.double().cpu().numpy()) * self.inv_q.double().cpu().numpy()
+        U = data.x[:n].cpu().numpy()
+        quad = 0.5 * _np.einsum("bi,ij,bj->b", x, A, x) + x @ beta
+        t = U - quad
+        sel = _np.arange(n) if rows is None else _np.asarray(rows)
+        sel = sel[_np.isfinite(t[sel])]
+        var = float(_np.var(t[sel])) if sel.size > 1 else 1.0
+        self._vt_w = float(self.value_weight / max(var, 1e-300))
+        self._vt = torch.from_numpy(_np.where(_np.isfinite(t), t, 0.0)).to(self.device)
+
+    def value_error(self, data: TrainingSet, rows, stream=None):
+        """Standard deviation over the given stored pairs (at most 1024) of
+        f(q) - U(q) about its mean, in misfit units: the potential's error
+        that enters the acceptance of a surrogate trajectory through the
+        difference of its end points.  None when values are not matched."""
+        import torch
+
+        if self._vt is None:
+            return None
+        rows = _np.asarray(rows.cpu().numpy() if hasattr(rows, "cpu") else rows)[:1024]
+        B = len(rows)
+        q = data.q[torch.as_tensor(rows, device=self.device)].t().contiguous()
+        g = torch.empty_like(q)
+        h = _dev.stream_handle(stream)
+        self.predict_into(q, g, h)
+        b = self._bufs[(B, False)]
+        idx = torch.as_tensor(rows.astype(_np.int32), device=self.device)
+        dv = torch.empty(B, dtype=torch.float32, device=self.device)
+        _lib.call("hmc_pot_value_residual", B, self.sizes[2], b["A2"].data_ptr(), b["A2"].shape[1],
+                  self.params["w3"].data_ptr(), self._vt.data_ptr(), idx.data_ptr(), 1.0, dv.data_ptr(),
+                  self.value_loss.data_ptr(), h)
+        return float(_np.sqrt(2.0 * self.value_loss.item()))
 
     # ---- training --------------------------------------------------------------
     def train_step(self, data: TrainingSet, idx_host, lr=1e-3, stream=None, beta1=0.9, beta2=0.999, eps=1e-8):
@@ -669,6 +749,8 @@ class PotentialSurrogate(_Surrogate):
         _lib.call("hmc_mlp_bias_grad", h2, B, b["ZB2t"].data_ptr(), pB, G["b2"].data_ptr(), h)
         self._wgrad(d, h1, B, b["Xt"], b["ZB1t"], G["W1"], 1, h)
         _lib.call("hmc_mlp_bias_grad", h1, B, b["ZB1t"].data_ptr(), pB, G["b1"].data_ptr(), h)
+        if self._vt is not None and self._vt_w > 0:
+            self._value_step(b, B, h)
         self.steps += 1
         for k in P:
             _lib.call("hmc_mlp_adam", P[k].numel(), P[k].data_ptr(), G[k].data_ptr(), self.m1[k].data_ptr(),
@@ -683,6 +765,32 @@ class PotentialSurrogate(_Surrogate):
         o = self._out(g=g, accumulate=int(accumulate))
         _lib.call("hmc_tc_mlp", _lib.HMC_MLP_WGRAD, n_in, n_out, B, act_t.data_ptr(), act_t.shape[1],
                   delta_t.data_ptr(), delta_t.shape[1], None, ctypes.byref(o), self.status.data_ptr(), stream)
+
+    def _value_step(self, b, B, h):
+        """Add the value-matching loss's weight gradients to self.grads (the
+        forward and gradient passes of this step left a2, delta2, delta1,
+        a1 and x in the buffers; see csrc/potential.cu)."""
+        d, h1, h2 = self.sizes
+        P, G = self.params, self.grads
+        pB = _pad(B)
+        _lib.call("hmc_pot_value_residual", B, h2, b["A2"].data_ptr(), b["A2"].shape[1], P["w3"].data_ptr(),
+                  self._vt.data_ptr(), b["idx"].data_ptr(), float(self._vt_w), b["dv"].data_ptr(),
+                  self.value_loss.data_ptr(), h)
+        # z2 = W2 a1 + b2: dz2 = dv delta2
+        _lib.call("hmc_pot_scale_columns", h2, B, b["D2t"].data_ptr(), pB, b["dv"].data_ptr(), b["S2t"].data_ptr(),
+                  pB, h)
+        self._wgrad(h1, h2, B, b["A1t"], b["S2t"], G["W2"], 1, h)
+        _lib.call("hmc_pot_weighted_colsum", B, h2, b["D2"].data_ptr(), b["D2"].shape[1], b["dv"].data_ptr(),
+                  G["b2"].data_ptr(), h)
+        # z1 = W1 x + b1: dz1 = dv delta1 (delta1 sits in the first h1 columns of Ag)
+        _lib.call("hmc_pot_scale_columns", h1, B, b["D1t"].data_ptr(), pB, b["dv"].data_ptr(), b["S1t"].data_ptr(),
+                  pB, h)
+        self._wgrad(d, h1, B, b["Xt"], b["S1t"], G["W1"], 1, h)
+        _lib.call("hmc_pot_weighted_colsum", B, h1, b["Ag"].data_ptr(), b["Ag"].shape[1], b["dv"].data_ptr(),
+                  G["b1"].data_ptr(), h)
+        # v = w3 . a2
+        _lib.call("hmc_pot_weighted_colsum", B, h2, b["A2"].data_ptr(), b["A2"].shape[1], b["dv"].data_ptr(),
+                  G["w3"].data_ptr(), h)
 
     def _state_tensors(self):
         t = {}

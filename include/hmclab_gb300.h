@@ -496,6 +496,20 @@ HMC_API int hmc_pot_loss(int64_t B, int64_t n, const float* y, int64_t ldy,
 HMC_API int hmc_pot_scaled_cast(int64_t rows, int64_t cols, const float* src,
                                 int64_t lds, int transposed, const float* scale,
                                 void* dst, int64_t ldd, int64_t k0, void* stream);
+/* Value matching of the potential surrogate (no reference counterpart):
+ * dv[b] = weight (r_b - rbar) / B and *loss = 0.5 weight mean (r_b - rbar)^2
+ * with r_b = w3 . a2[b] - targets[idx[b]] (a2 BF16 [B][lda], B <= 1024);
+ * out[j] += sum_b dv[b] in[b][j] (in BF16 [B][ld]); out_t[r][b] =
+ * in_t[r][b] dv[b] (BF16 [rows][ld]).                                        */
+HMC_API int hmc_pot_value_residual(int64_t B, int64_t h, const void* a2, int64_t lda,
+                                   const float* w3, const double* targets,
+                                   const int32_t* idx, float weight, float* dv,
+                                   double* loss, void* stream);
+HMC_API int hmc_pot_weighted_colsum(int64_t B, int64_t n, const void* in, int64_t ld,
+                                    const float* dv, float* out, void* stream);
+HMC_API int hmc_pot_scale_columns(int64_t rows, int64_t B, const void* in_t,
+                                  int64_t ldi, const float* dv, void* out_t,
+                                  int64_t ldo, void* stream);
 
 /* ---- 2-D elastic P-SV full-waveform misfit and gradient ------------------
  * Replaces psvWave's forward_simulate / calculate_l2_misfit / adjoint_simulate

@@ -108,6 +108,27 @@ def potential_loss_grads(x, t, scale, shift, W1, b1, W2, b2, w3, A, beta):
     return loss, {"W1": gW1, "b1": zbar1.sum(0), "W2": gW2, "b2": zbar2.sum(0), "w3": gw3}
 
 
+def potential_value_loss_grads(x, t, weight, W1, b1, W2, b2, w3):
+    """Value-matching loss 0.5 weight mean_b (r_b - rbar)^2 with
+    r_b = w3 . GELU(W2 GELU(W1 x_b + b1) + b2) - t_b (t_b: the exact misfit
+    minus the fixed quadratic part) and its gradients with respect to
+    W1, b1, W2, b2, w3 (FP64, no rounding; plain backpropagation)."""
+    B = x.shape[0]
+    z1 = x @ W1.T + b1
+    a1 = gelu(z1)
+    z2 = a1 @ W2.T + b2
+    a2 = gelu(z2)
+    r = a2 @ w3 - t
+    c = r - r.mean()
+    loss = 0.5 * weight * np.sum(c * c) / B
+    dv = weight * c / B
+    delta2 = w3 * gelu_grad(z2)
+    delta1 = (delta2 @ W2) * gelu_grad(z1)
+    dz2 = dv[:, None] * delta2
+    dz1 = dv[:, None] * delta1
+    return loss, {"W1": dz1.T @ x, "b1": dz1.sum(0), "W2": dz2.T @ a1, "b2": dz2.sum(0), "w3": dv @ a2}
+
+
 def potential_predict(q, mu_q, s_q, mu_g, sig_g, W1, b1, W2, b2, w3, A, beta):
     """Surrogate gradient grad_q f at positions q [d][C] with the device's
     rounding points: x, W1, W2 and the scaled output matrix [W1^T | A] / (s

@@ -255,3 +255,80 @@ def test_quadratic_fit_recovers_a_quadratic_potential():
     M = rng.normal(size=(d, d))
     A2, _ = quadratic_fit(x, x @ M.T, ridge=1e-9)
     np.testing.assert_allclose(A2, 0.5 * (M + M.T), atol=1e-6)
+
+
+def test_oracle_value_loss_gradients_match_finite_differences():
+    rng = np.random.default_rng(8)
+    P, _, _ = small_params(rng)
+    x = rng.normal(size=(6, 7))
+    t = rng.normal(size=6) * 3
+    loss, G = MO.potential_value_loss_grads(x, t, 0.7, **P)
+    eps = 1e-6
+    for k in P:
+        for idx in list(np.ndindex(P[k].shape))[:5]:
+            Pp = {kk: v.copy() for kk, v in P.items()}
+            Pm = {kk: v.copy() for kk, v in P.items()}
+            Pp[k][idx] += eps
+            Pm[k][idx] -= eps
+            fd = (MO.potential_value_loss_grads(x, t, 0.7, **Pp)[0] - MO.potential_value_loss_grads(x, t, 0.7, **Pm)[0])
+            fd /= 2 * eps
+            assert abs(fd - G[k][idx]) <= 1e-6 * max(1.0, abs(fd)), (k, idx, fd, G[k][idx])
+
+
+@pytest.mark.gpu
+def test_device_value_matching_gradients_match_oracle():
+    """With values matched, a training step adds the value loss's weight
+    gradients (csrc/potential.cu value kernels + tensor-core WGRAD) to the
+    gradient-matching ones: the difference of the two steps' gradients
+    against the oracle's FP64 backpropagation on the same minibatch (BF16
+    activations and deltas on the device: 3 % Frobenius)."""
+    torch = _torch()
+    from hmclab_gb300 import surrogate as S
+
+    d, B, n = 48, 128, 512
+    rng = np.random.default_rng(12)
+    data = S.TrainingSet(d, n, values=True)
+    Q = rng.normal(size=(d, n))
+
+    def U(q):
+        return 0.75 * np.sum(q * q, axis=0) + np.sum(np.log(np.cosh(2 * q[:5])), axis=0)
+
+    def grad(q):
+        g = 1.5 * q
+        g[:5] += 2 * np.tanh(2 * q[:5])
+        return g
+
+    st = torch.cuda.current_stream().cuda_stream
+    for k in range(n // 256):
+        qc = Q[:, k * 256:(k + 1) * 256]
+        data.record(torch.from_numpy(qc.copy()).float().cuda(), torch.from_numpy(grad(qc)).float().cuda(), st,
+                    torch.from_numpy(U(qc)).cuda())
+    torch.cuda.synchronize()
+    assert torch.isfinite(data.x[:n]).all()
+    net = S.PotentialSurrogate(d, hidden=(64, 64), seed=1)
+    net.value_weight = 0.5
+    net.fit_normalization(data)
+    net.train(data, steps=10, batch=B, lr=1e-3)
+    idx = rng.integers(0, n, size=B)
+    w = net._vt_w
+    net._vt_w = 0.0
+    net.train_step(data, idx, lr=0.0)
+    g_grad = {k: h(v) for k, v in net.grads.items()}
+    net._vt_w = w
+    net.train_step(data, idx, lr=0.0)
+    torch.cuda.synchronize()
+    net.check_status()
+    q = h(data.q[torch.from_numpy(idx).cuda()])
+    x = (q - h(net.mu_q)) * h(net.inv_q)
+    t = h(net._vt)[idx]
+    P = _oracle_params(net)
+    loss, G = MO.potential_value_loss_grads(x, t, w, P["W1"], P["b1"], P["W2"], P["b2"], P["w3"])
+    assert abs(float(net.value_loss[0]) - loss) <= 0.02 * loss
+    for k, ref in G.items():
+        got = h(net.grads[k]) - g_grad[k]
+        rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        print(f"value loss {k}: relative error {rel:.2e}")
+        assert rel < 0.03, (k, rel)
+    # the held-out value error is measured and finite
+    ve = net.value_error(data, np.arange(256))
+    assert ve is not None and np.isfinite(ve)
