@@ -270,12 +270,19 @@ class TomoWorkload:
     def roofline_spec(self, smp):
         C = self.chains
         work = 2 * (8.0 * self.nnz + 4.0 * C * (self.n_data + self.n_model)) + 4.0 * (self.n_data + 1) * 2
-        # every nonzero also gathers a row of the dense operand (C values)
-        # from L2: the traffic the kernel actually moves
+        # every nonzero also multiplies a row of the dense operand (C values),
+        # gathered from L2 or staged in shared memory: the bytes the kernels
+        # actually move through the memory hierarchy
         gather = 2 * 4.0 * self.nnz * C
-        return {"kernel": "csr_spmm_kernel x2 (G @ Q - d, G^T @ R)", "bound": "hbm", "unit": "GB/s", "work": work,
+        names = {0: "csr_gather_kernel<1>", 1: "csr_gather_kernel<4>", 2: "csr_slab_kernel"}
+        lik = smp.distribution.separate_distributions[1]
+        plan = lik.__dict__.get("_scratch_cache", {}).get(("csr_slab", C))
+        shapes = (plan.shape_g, plan.shape_gt) if plan is not None else None
+        kern = (f"{names[shapes[0][0]]} (G @ (Q - c) - d_c) + {names[shapes[1][0]]} (G^T @ R), shapes picked by "
+                f"the autotuner {list(shapes[0])} / {list(shapes[1])}" if shapes else "CSR products G @ Q, G^T @ R")
+        return {"kernel": kern, "bound": "hbm", "unit": "GB/s", "work": work,
                 "work_name": "algorithmic_bytes_per_launch",
-                "extra": {"nnz": int(self.nnz), "l2_gather_bytes_per_launch": gather}}
+                "extra": {"nnz": int(self.nnz), "gather_bytes_per_launch": gather}}
 
     def config(self):
         return {"workload": self.name, "cells": self.n_model, "rays": self.n_data, "nnz": int(self.nnz),

@@ -1,10 +1,12 @@
-"""Host side of the shared-memory column-slab CSR products (FP32).
+"""Host side of the FP32 CSR products of the sparse LinearMatrix.
 
 `CsrSlabPlan` holds, for one sparse LinearMatrix and a chain count C, the
-slab pointers of G and of G^T for the launch shapes the autotuner picked
-(slab width, rows per warp), and issues hmc_csr_slab_misfit /
-hmc_csr_slab_gradient (csrc/distributions.cu).  Every launch shape gives the
-same sums bit for bit; the shape only changes the speed.
+launch shape the autotuner picked for G and for G^T — a gather kernel (one
+or four chains per thread) or the shared-memory column-slab kernel with its
+slab width and rows per warp, with the slab pointers it needs — and issues
+hmc_csr_slab_misfit / hmc_csr_slab_gradient (csrc/distributions.cu).  Every
+shape adds a row's nonzeros in CSR order, so all give the same sums bit for
+bit; the shape only changes the speed.
 
 Centring: the residual G m - d of a travel-time problem is about a thousandth
 of G m, so forming it from FP32 sums of G m would lose three digits.  The
@@ -21,6 +23,17 @@ from hmclab_gb300 import autotune as _autotune
 
 SLABS = (128, 192, 256, 320, 384, 448)
 ROWS_PER_WARP = (4, 8, 16)
+
+
+def candidates(C):
+    """Launch shapes (kernel, slab, rows per warp) the autotuner times: the
+    per-nonzero gather kernels (one or four chains per thread) and the
+    shared-memory slab kernel's shapes."""
+    out = [(_lib.HMC_CSR_GATHER, 0, 0)]
+    if C % 4 == 0:
+        out.append((_lib.HMC_CSR_GATHER4, 0, 0))
+    out += [(_lib.HMC_CSR_SLAB, s, r) for s in SLABS for r in ROWS_PER_WARP]
+    return out
 
 
 def slab_pointers(indptr, indices, cols, slab):
@@ -54,26 +67,28 @@ def columns_sorted(indptr, indices):
 class _Matrix:
     """One CSR operand (G or G^T) on the device with its slab pointers."""
 
-    def __init__(self, indptr, indices, col_dev, val_dev, rows, cols, device):
+    def __init__(self, indptr, indices, rp_dev, col_dev, val_dev, rows, cols, device):
         if not columns_sorted(indptr, indices):
             raise ValueError("the slab CSR products need column indices sorted within rows")
         self.indptr, self.indices = indptr, indices
-        self.col, self.val = col_dev, val_dev
+        self.rp, self.col, self.val = rp_dev, col_dev, val_dev
         self.rows, self.cols, self.device = int(rows), int(cols), device
         self._sp = {}
 
-    def descriptor(self, slab, rpw):
-        sp = self._sp.get(slab)
-        if sp is None:
-            sp = _dev.upload_int32(slab_pointers(self.indptr, self.indices, self.cols, slab), self.device)
-            self._sp[slab] = sp
+    def descriptor(self, kernel, slab=0, rpw=0):
         d = _lib.HmcCsrSlabs()
-        d.col, d.val, d.slab_ptr = self.col.data_ptr(), self.val.data_ptr(), sp.data_ptr()
-        d.rows, d.cols, d.slab, d.rows_per_warp = self.rows, self.cols, int(slab), int(rpw)
+        d.col, d.val, d.row_ptr = self.col.data_ptr(), self.val.data_ptr(), self.rp.data_ptr()
+        d.rows, d.cols, d.kernel = self.rows, self.cols, int(kernel)
+        if kernel == _lib.HMC_CSR_SLAB:
+            sp = self._sp.get(slab)
+            if sp is None:
+                sp = _dev.upload_int32(slab_pointers(self.indptr, self.indices, self.cols, slab), self.device)
+                self._sp[slab] = sp
+            d.slab_ptr, d.slab, d.rows_per_warp = sp.data_ptr(), int(slab), int(rpw)
         return d
 
-    def keep_only(self, slab):
-        self._sp = {slab: self._sp[slab]}
+    def keep_only(self, shape):
+        self._sp = {shape[1]: self._sp[shape[1]]} if shape[0] == _lib.HMC_CSR_SLAB else {}
 
 
 class CsrSlabPlan:
@@ -89,15 +104,15 @@ class CsrSlabPlan:
         n, d = lik.n_data, lik.dimensions
         self.C = int(C)
         self.p = p
-        self.g = _Matrix(G.indptr, G.indices, p["col"], p["val"], n, d, device)
-        self.gt = _Matrix(Gt.indptr, Gt.indices, p["tcol"], p["tval"], d, n, device)
+        self.g = _Matrix(G.indptr, G.indices, p["rp"], p["col"], p["val"], n, d, device)
+        self.gt = _Matrix(Gt.indptr, Gt.indices, p["trp"], p["tcol"], p["tval"], d, n, device)
         # autotune each product on zero operands (the timing does not depend on values)
         X = torch.zeros((d, self.C), dtype=torch.float32, device=device)
         R = torch.zeros((n, self.C), dtype=torch.float32, device=device)
         out_n = torch.empty((n, self.C), dtype=torch.float32, device=device)
         out_d = torch.empty((d, self.C), dtype=torch.float32, device=device)
         x = torch.empty((self.C,), dtype=torch.float64, device=device)
-        shapes = [(s, r) for s in SLABS for r in ROWS_PER_WARP]
+        shapes = candidates(self.C)
         nnz = int(G.nnz)
 
         zeros_d = torch.zeros((d,), dtype=torch.float32, device=device)
@@ -127,8 +142,8 @@ class CsrSlabPlan:
                                          device, stream)
         self.desc_g = self.g.descriptor(*self.shape_g)
         self.desc_gt = self.gt.descriptor(*self.shape_gt)
-        self.g.keep_only(self.shape_g[0])
-        self.gt.keep_only(self.shape_gt[0])
+        self.g.keep_only(self.shape_g)
+        self.gt.keep_only(self.shape_gt)
         self._ref_g = _lib._ct.byref(self.desc_g)
         self._ref_gt = _lib._ct.byref(self.desc_gt)
         torch.cuda.current_stream(device).synchronize()

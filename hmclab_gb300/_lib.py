@@ -29,6 +29,8 @@ HMC_MASS_FULL = 2
 
 HMC_FLAG_OUT_OF_BOUNDS = 1
 
+HMC_CSR_GATHER, HMC_CSR_GATHER4, HMC_CSR_SLAB = 0, 1, 2
+
 c_void_p = _ct.c_void_p
 c_int = _ct.c_int
 c_int32 = _ct.c_int32
@@ -132,6 +134,9 @@ class HmcCsrSlabs(_ct.Structure):
         ("cols", c_int64),
         ("slab", c_int32),
         ("rows_per_warp", c_int32),
+        ("row_ptr", c_void_p),
+        ("kernel", c_int32),
+        ("reserved", c_int32),
     ]
 
 

@@ -9,6 +9,8 @@
 //   SourceLocation3D       Distributions/SourceLocation.py:482-540,697-713
 #include <math.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace hmc {
@@ -344,11 +346,102 @@ __global__ void __launch_bounds__(CSR_THREADS, 2)
   }
 }
 
+// ---- gather variants of the FP32 CSR product ---------------------------------
+// One block row per CSR row; VEC chains per thread (1, or 4 with 16-byte
+// loads of X and stores of out).  The nonzeros of the row are added in CSR
+// order with fused multiply-adds (four rows of X in flight), optionally on
+// the centred operand X - center[col].
+template <int VEC>
+__global__ void csr_gather_kernel(int rows, int C, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                  const float* __restrict__ val, const float* __restrict__ X,
+                                  const float* __restrict__ center, const float* __restrict__ bias,
+                                  const float* __restrict__ rs, float* out, int accumulate) {
+  using V = typename std::conditional<VEC == 4, float4, float>::type;
+  const int r = blockIdx.y;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * VEC;
+  if (r >= rows || c >= C) return;
+  float a[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; ++v) a[v] = 0.f;
+  const int b = rp[r], e = rp[r + 1];
+  auto load = [&](int k, float* x) {
+    const int j = col[k];
+    const float cj = center ? center[j] : 0.f;
+    const V xv = *(const V*)(X + (int64_t)j * C + c);
+    const float* xs = (const float*)&xv;
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) x[v] = xs[v] - cj;
+  };
+  int k = b;
+  for (; k + 4 <= e; k += 4) {
+    float x0[VEC], x1[VEC], x2[VEC], x3[VEC];
+    load(k, x0);
+    load(k + 1, x1);
+    load(k + 2, x2);
+    load(k + 3, x3);
+    const float v0 = val[k], v1 = val[k + 1], v2 = val[k + 2], v3 = val[k + 3];
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) {
+      a[v] = fmaf(v0, x0[v], a[v]);
+      a[v] = fmaf(v1, x1[v], a[v]);
+      a[v] = fmaf(v2, x2[v], a[v]);
+      a[v] = fmaf(v3, x3[v], a[v]);
+    }
+  }
+  for (; k < e; ++k) {
+    float x0[VEC];
+    load(k, x0);
+    const float v0 = val[k];
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) a[v] = fmaf(v0, x0[v], a[v]);
+  }
+  const float bb = bias ? bias[r] : 0.f, ss = rs ? rs[r] : 1.f;
+  float* o = out + (int64_t)r * C + c;
+  V ov;
+  float* os = (float*)&ov;
+  if (accumulate) ov = *(const V*)o;
+#pragma unroll
+  for (int v = 0; v < VEC; ++v) {
+    float y = a[v];
+    if (bias) y -= bb;
+    if (rs) y *= ss;
+    os[v] = accumulate ? os[v] + y : y;
+  }
+  *(V*)o = ov;
+}
+
+int csr_gather(const hmc_csr_slabs* A, int64_t C, const float* X, const float* center, const float* bias,
+               const float* rs, float* out, int accumulate, cudaStream_t st) {
+  HMC_REQUIRE(A->rows <= 65535, "csr gather product: at most 65535 rows per launch");
+  if (A->kernel == HMC_CSR_GATHER4) {
+    HMC_REQUIRE(C % 4 == 0 && ((uintptr_t)X & 15) == 0 && ((uintptr_t)out & 15) == 0,
+                "csr gather product: four chains per thread need C % 4 == 0 and 16-byte aligned operands");
+    const int64_t q = C / 4;
+    const int threads = q >= 256 ? 256 : (q >= 128 ? 128 : (q >= 64 ? 64 : 32));
+    const dim3 grid((unsigned)((q + threads - 1) / threads), (unsigned)A->rows);
+    csr_gather_kernel<4><<<grid, threads, 0, st>>>((int)A->rows, (int)C, A->row_ptr, A->col, A->val, X, center, bias,
+                                                   rs, out, accumulate);
+  } else {
+    const int threads = C >= 256 ? 256 : (C >= 128 ? 128 : (C >= 64 ? 64 : 32));
+    const dim3 grid((unsigned)((C + threads - 1) / threads), (unsigned)A->rows);
+    csr_gather_kernel<1><<<grid, threads, 0, st>>>((int)A->rows, (int)C, A->row_ptr, A->col, A->val, X, center, bias,
+                                                   rs, out, accumulate);
+  }
+  return check_launch("csr_gather_kernel");
+}
+
 int csr_slab_check(const hmc_csr_slabs* A, const char* who) {
   HMC_REQUIRE(A != nullptr, "%s: null CSR descriptor", who);
-  HMC_REQUIRE(A->col && A->val && A->slab_ptr, "%s: CSR descriptor has a null array", who);
+  HMC_REQUIRE(A->kernel >= HMC_CSR_GATHER && A->kernel <= HMC_CSR_SLAB, "%s: unknown CSR kernel %d", who,
+              (int)A->kernel);
+  HMC_REQUIRE(A->col && A->val, "%s: CSR descriptor has a null array", who);
   HMC_REQUIRE(A->rows > 0 && A->cols > 0 && A->rows < (1ll << 31) && A->cols < (1ll << 31), "%s: bad CSR shape",
               who);
+  if (A->kernel != HMC_CSR_SLAB) {
+    HMC_REQUIRE(A->row_ptr != nullptr, "%s: the gather kernels need row_ptr", who);
+    return HMC_OK;
+  }
+  HMC_REQUIRE(A->slab_ptr != nullptr, "%s: the slab kernel needs slab_ptr", who);
   HMC_REQUIRE(A->slab >= 32 && A->slab <= 448,
               "%s: slab of %d columns outside 32 .. 448 (two double-buffered blocks per SM)", who, (int)A->slab);
   HMC_REQUIRE(A->rows_per_warp == 4 || A->rows_per_warp == 8 || A->rows_per_warp == 16,
@@ -388,6 +481,7 @@ int csr_slab_launch(const hmc_csr_slabs* A, int64_t C, const float* X, const flo
 int csr_slab(const hmc_csr_slabs* A, int64_t C, const float* X, const float* center, const float* bias,
              const float* rs, float* out, int accumulate, cudaStream_t st) {
   HMC_REQUIRE(C < (1ll << 31) && (C + 31) / 32 <= 0x7fffffff, "csr slab product: too many chains");
+  if (A->kernel != HMC_CSR_SLAB) return csr_gather(A, C, X, center, bias, rs, out, accumulate, st);
   switch (A->rows_per_warp) {
     case 4:
       return csr_slab_launch<4>(A, C, X, center, bias, rs, out, accumulate, st);

@@ -297,18 +297,27 @@ HMC_API int hmc_csr_gradient(int dtype, int64_t n, int64_t d, int64_t C,
  * entry of a row is row_ptr[r + 1].  rows_per_warp (4, 8 or 16) sets the rows
  * a block accumulates per slab pass (16 warps per block).  With center NULL
  * the results equal hmc_csr_misfit / hmc_csr_gradient bit for bit; slab and
- * rows_per_warp only change the speed (picked by the host autotuner).
+ * rows_per_warp only change the speed (picked by the host autotuner, which
+ * also times the gather kernels: `kernel` selects the variant, and every
+ * variant adds the nonzeros of a row in CSR order with fused multiply-adds,
+ * so all give the same sums).
  * center ([cols], may be NULL) makes the first product G (M - center) -
  * data: the caller passes data - G center (formed in FP64) so that the
  * residual is unchanged but the FP32 sums no longer cancel terms of the size
  * of G M (travel times ~1e3 x their residuals in the tomography workload).  */
+#define HMC_CSR_GATHER 0  /* one thread per chain, X rows gathered per nonzero   */
+#define HMC_CSR_GATHER4 1 /* four chains per thread (16-byte loads; C % 4 == 0)  */
+#define HMC_CSR_SLAB 2    /* column slabs of X staged in shared memory          */
 typedef struct hmc_csr_slabs {
   const int32_t* col;      /* [nnz] column indices, sorted within rows */
   const float* val;        /* [nnz] values                              */
-  const int32_t* slab_ptr; /* [rows][n_slabs + 1] slab starts per row   */
+  const int32_t* slab_ptr; /* [rows][n_slabs + 1] slab starts per row (SLAB) */
   int64_t rows, cols;
-  int32_t slab;            /* columns per shared-memory slab            */
-  int32_t rows_per_warp;   /* 4, 8 or 16                                */
+  int32_t slab;            /* columns per shared-memory slab (SLAB)     */
+  int32_t rows_per_warp;   /* 4, 8 or 16 (SLAB)                         */
+  const int32_t* row_ptr;  /* [rows + 1] (GATHER, GATHER4)              */
+  int32_t kernel;          /* HMC_CSR_GATHER / GATHER4 / SLAB           */
+  int32_t reserved;
 } hmc_csr_slabs;
 HMC_API int hmc_csr_slab_misfit(const hmc_csr_slabs* G, int64_t C, const float* M,
                                 const float* center, const float* data,

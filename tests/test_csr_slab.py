@@ -2,10 +2,11 @@
 hmclab_gb300/_csr.py) and the launch-shape autotuner (autotune.py).
 
 CPU: slab pointers partition every row by column slab; the sortedness check;
-the autotuner's cache file.  GPU: every launch shape gives the same FP32
-misfits and gradients as the per-nonzero gather kernels (hmc_csr_misfit /
-hmc_csr_gradient) bit for bit, and matches the FP64 host product within the
-FP32 parity tolerance (1e-5 of the largest |gradient| entry)."""
+the autotuner's cache file.  GPU: every launch shape (the gather kernels with
+one or four chains per thread, the slab kernel's shapes) gives the same FP32
+misfits and gradients as hmc_csr_misfit / hmc_csr_gradient bit for bit, and
+the centred public path matches the FP64 host product within the FP32
+parity tolerance (1e-5 of the largest |gradient| entry)."""
 import json
 
 import numpy as np
@@ -90,18 +91,19 @@ def test_slab_products_equal_gather_kernels(rows, cols, C):
     _lib.call("hmc_csr_misfit", _lib.HMC_F32, rows, cols, C, M.data_ptr(), p["rp"].data_ptr(), p["col"].data_ptr(),
               p["val"].data_ptr(), p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), x_old.data_ptr(), 0, h)
     plan = lik._csr_plan(C, M.device, h)
-    for slab in _csr.SLABS[::2] + (32,):
-        for rpw in _csr.ROWS_PER_WARP:
-            dg, dgt = plan.g.descriptor(slab, rpw), plan.gt.descriptor(slab, rpw)
-            g = torch.full((cols, C), float("nan"), dtype=torch.float32, device="cuda")
-            x = torch.empty((C,), dtype=torch.float64, device="cuda")
-            _lib.call("hmc_csr_slab_gradient", _lib._ct.byref(dg), _lib._ct.byref(dgt), C, M.data_ptr(), None,
-                      p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), g.data_ptr(), 0, h)
-            _lib.call("hmc_csr_slab_misfit", _lib._ct.byref(dg), C, M.data_ptr(), None, p["data"].data_ptr(),
-                      p["iv"].data_ptr(), resid.data_ptr(), x.data_ptr(), 0, h)
-            torch.cuda.synchronize()
-            assert torch.equal(g, g_old), (slab, rpw)
-            assert torch.equal(x, x_old), (slab, rpw)
+    shapes = [c for c in _csr.candidates(C) if c[0] != _lib.HMC_CSR_SLAB or c[1] in _csr.SLABS[::2]]
+    shapes += [(_lib.HMC_CSR_SLAB, 32, r) for r in _csr.ROWS_PER_WARP]
+    for shape in shapes:
+        dg, dgt = plan.g.descriptor(*shape), plan.gt.descriptor(*shape)
+        g = torch.full((cols, C), float("nan"), dtype=torch.float32, device="cuda")
+        x = torch.empty((C,), dtype=torch.float64, device="cuda")
+        _lib.call("hmc_csr_slab_gradient", _lib._ct.byref(dg), _lib._ct.byref(dgt), C, M.data_ptr(), None,
+                  p["data"].data_ptr(), p["iv"].data_ptr(), resid.data_ptr(), g.data_ptr(), 0, h)
+        _lib.call("hmc_csr_slab_misfit", _lib._ct.byref(dg), C, M.data_ptr(), None, p["data"].data_ptr(),
+                  p["iv"].data_ptr(), resid.data_ptr(), x.data_ptr(), 0, h)
+        torch.cuda.synchronize()
+        assert torch.equal(g, g_old), shape
+        assert torch.equal(x, x_old), shape
     # the public path (autotuned shape, centred products) and the FP64 host product
     g = lik.gradient_batch(M).double().cpu().numpy()
     x = lik.misfit_batch(M).cpu().numpy()

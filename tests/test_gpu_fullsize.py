@@ -10,7 +10,8 @@ misfits and blob gradients.
 Tolerances: positions within 1e-5 of the largest |coordinate| of the chain
 (FP32 relative); the misfits the device recorded within 1e-5 relative of
 the FP64 misfits of the positions it recorded; accept decisions identical
-except where |dH - log u| < 1e-9 in the oracle.  The chains the oracle replays are
+except where |dH - log u| < 1e-3 in the oracle (the FP32 states' dH error
+scale; chains with such a decision are not compared further).  The chains the oracle replays are
 spread over the whole batch (first, last and evenly spaced ones), so every
 block of the device launch is covered."""
 import numpy as np
@@ -26,7 +27,11 @@ from oracle import hmc_oracle as O  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 FP32_RTOL = 1e-5
-TIE = 1e-9
+# Accept-decision tie band of the FP32 chains: the decision compares dH with
+# log u, and an FP32 state carries dH to about 1e-6 of the Hamiltonian
+# (misfits of 1e3 here), so decisions within 1e-3 of the threshold may part
+# legitimately; the FP64 path's band is 1e-9 (tests/test_gpu_parity.py).
+TIE = 1e-3
 
 
 @pytest.fixture(scope="module", autouse=True)
