@@ -362,7 +362,8 @@ class SrclocWorkload:
 
     def roofline_spec(self, smp):
         work = float(self.FLOP_PER_PAIR) * self.chains * self.E * self.S
-        return {"kernel": "srcloc_kernel<float, true> (one thread per chain and event lane)", "bound": "fp32",
+        return {"kernel": "srcloc_f32_kernel<true> (one thread per chain and event lane, pair data in shared memory)",
+                "bound": "fp32",
                 "unit": "TFLOP/s", "work": work, "work_name": "algorithmic_flop_per_launch",
                 "extra": {"pairs_per_launch": self.chains * self.E * self.S}}
 
@@ -905,7 +906,9 @@ def run_fwi_arm(args, wl):
     t_setup = time.perf_counter() - t_setup
 
     # ---- exact proposals from the start states, recording training pairs --
-    data = S.TrainingSet(d, Nb * L * C, values=args.value_weight > 0)
+    R = args.refresh_interval if args.refresh_interval > 0 else None
+    extra = 2 * (W + K) * B // R * C if R else 0  # rows the refreshes of the timed and e2e runs append
+    data = S.TrainingSet(d, Nb * L * C + extra, values=args.value_weight > 0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=q_init, proposals=Nb,
@@ -925,6 +928,7 @@ def run_fwi_arm(args, wl):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     net.freeze()
+    fitted, n_fit = net.state_arrays(), data.count
 
     # ---- pilot (untimed): the surrogate run's trajectory ------------------
     # A few proposals per (L, stepsize) from the start states; the setting
@@ -949,9 +953,10 @@ def run_fwi_arm(args, wl):
     kw_s = dict(kw, amount_of_steps=L_best, stepsize=eps_best)
 
     # ---- surrogate-driven HMC: W untimed blocks, then K timed blocks -------
+    refresh_kw = dict(training_set=data, refresh_interval=R, refresh_steps=args.refresh_steps) if R else {}
     smp_s = H.Samplers.HMC(seed=sharding.rank_seed(200, rank))
     smp_s.prepare(None, post, initial_model=q_start, proposals=(W + K) * B, keep_samples=True, surrogate=net,
-                  **kw_s)
+                  **refresh_kw, **kw_s)
     smp_s.run(W * B)
     smp_s.stream.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
@@ -1008,10 +1013,16 @@ def run_fwi_arm(args, wl):
     plain_value = e_plain * C * world * Kp / t_p if e_plain is not None else None
 
     # ---- end to end through the public API with host buffers -------------
+    # the same method from the fitted network: the timed run's refreshes are undone
+    refreshes_timed = getattr(smp_s, "refreshes", 0)
+    net.load_state_arrays(fitted)
+    data.count = n_fit
+    if getattr(net, "_vt", None) is not None:
+        net._vt = net._vt[:n_fit]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     smp_e = H.Samplers.HMC(seed=sharding.rank_seed(400, rank)).sample(
-        None, post, initial_model=q_start, proposals=K * B, keep_samples=True, surrogate=net, **kw_s)
+        None, post, initial_model=q_start, proposals=K * B, keep_samples=True, surrogate=net, **refresh_kw, **kw_s)
     host_q, host_x = smp_e.samples_host()
     t_e2e = time.perf_counter() - t0
     ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K * B // 2, 200)))
@@ -1034,6 +1045,9 @@ def run_fwi_arm(args, wl):
             "note": "min-ESS over (exact training-pair proposals + surrogate training + sampling) seconds"},
         "ess_window_truncated": float(np.mean(ess_s_raw >= 0)), "proposals_per_chain": N,
         "rank_normalised_bulk": {"value": float(bulk_s.min() / t_s)},
+        "refresh": {"interval": R, "adam_steps": args.refresh_steps if R else 0, "refreshes": refreshes_timed,
+                    "note": "after every block: exact gradient and misfit at the chains' current positions appended "
+                            "to the training set, then more training; inside the timed region"},
         "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
                                                       "pilot": [[L_, e_, round(a_, 4)] for _, L_, e_, a_ in pilot]},
         "plain": {"value": plain_value, "proposals_timed": Kp, "ms_per_proposal": 1e3 * t_p / Kp,
@@ -1226,6 +1240,10 @@ def main():
     ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
     ap.add_argument("--value-weight", type=float, default=1.0,
                     help="fwi: weight of the misfit-value matching loss of the potential surrogate (0: gradients only)")
+    ap.add_argument("--refresh-interval", type=int, default=16,
+                    help="fwi: surrogate proposals between refreshes of the network on exact gradients at the chains' "
+                         "positions (0: never)")
+    ap.add_argument("--refresh-steps", type=int, default=300, help="fwi: Adam steps per refresh")
     ap.add_argument("--pilot-max-length", type=float, default=2.0,
                     help="fwi: longest surrogate trajectory the pilot tries, in units of plain HMC's")
     ap.add_argument("--burn-in", type=int, default=None,

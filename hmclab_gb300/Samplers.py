@@ -43,6 +43,14 @@ optional Robbins-Monro step adaptation (`:1494-1522`), thinned samples
                 parity mode for the exchanges: (schedule [E][2 (C // 2)],
                 uniforms [E][C // 2]) replacing the pairing and accept draws
                 of exchange row e = proposal index // exchange_interval
+  refresh_interval
+                with a surrogate and a training_set: after every this many
+                proposals the exact gradient (and misfit) at every chain's
+                current position is appended to the training set and the
+                surrogate trains `refresh_steps` more Adam steps at
+                `refresh_lr` (half of each minibatch from the newest pairs),
+                then freezes again; each block between refreshes runs with a
+                fixed network, so its kernel keeps the exact posterior
 
 diagnostic_mode (reference `Samplers.py:449-460, 499-527, 759-764`) times
 every phase of the proposals with CUDA events on the sampler's stream:
@@ -207,6 +215,7 @@ class HMC:
     _temperatures = None
     exchange_interval = None
     _exchange_streams = None
+    refresh_interval = None
     beta = None
     use_persistent = None
     _persistent = None
@@ -259,6 +268,9 @@ class HMC:
         persistent: bool = None,
         resume=None,
         exchange_streams=None,
+        refresh_interval: int = None,
+        refresh_steps: int = 300,
+        refresh_lr: float = 2e-4,
     ):
         """Run `proposals` HMC proposals for every chain; returns self.
 
@@ -279,7 +291,8 @@ class HMC:
             chains=chains, dtype=dtype, rng_streams=rng_streams, graph=graph, proposals_per_graph=proposals_per_graph,
             keep_samples=keep_samples, surrogate=surrogate, training_set=training_set, temperatures=temperatures,
             exchange_interval=exchange_interval, persistent=persistent, resume=resume,
-            exchange_streams=exchange_streams,
+            exchange_streams=exchange_streams, refresh_interval=refresh_interval, refresh_steps=refresh_steps,
+            refresh_lr=refresh_lr,
         )
         self._run()
         return self
@@ -614,10 +627,19 @@ class HMC:
         else:
             zz, ff, uu = self._explicit_streams
             z, f, u = zz[n0 : n0 + n], ff[n0 : n0 + n], uu[n0 : n0 + n]
+        # the device reads proposal g's draws from slot g % slots (g counts
+        # from the chains' first proposal), so a block that does not start on
+        # a multiple of the slot count wraps around
+        slots = self.stream_z.shape[0]
+        s0 = (self._proposal_base + n0) % slots
+        parts = [(0, s0, min(n, slots - s0))]
+        if parts[0][2] < n:
+            parts.append((parts[0][2], 0, n - parts[0][2]))
         with _torch.cuda.stream(self.stream):
-            self.stream_z[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(z)).to(self.stream_z.dtype), non_blocking=False)
-            self.stream_f[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(f)).to(self.stream_f.dtype), non_blocking=False)
-            self.stream_u[:n].copy_(_torch.from_numpy(_numpy.ascontiguousarray(u)), non_blocking=False)
+            for j0, t0, m in parts:
+                for dst, src in ((self.stream_z, z), (self.stream_f, f), (self.stream_u, u)):
+                    dst[t0:t0 + m].copy_(_torch.from_numpy(_numpy.ascontiguousarray(src[j0:j0 + m])).to(dst.dtype),
+                                         non_blocking=False)
 
     def _drain(self, n0, n):
         """Move the thinned samples of proposals [n0, n0+n) to the files."""
@@ -643,7 +665,7 @@ class HMC:
             max_time=None, autotuning=False, target_acceptance_rate=0.65, learning_rate=0.75, chains=None,
             dtype=None, rng_streams=None, graph=True, proposals_per_graph=None, keep_samples=False,
             surrogate=None, training_set=None, temperatures=None, exchange_interval=None, persistent=None,
-            resume=None, exchange_streams=None,
+            resume=None, exchange_streams=None, refresh_interval=None, refresh_steps=300, refresh_lr=2e-4,
         )
         unknown = set(kwargs) - set(defaults) - {"queue", "disable_progressbar"}
         if unknown:
@@ -668,7 +690,8 @@ class HMC:
                 if not keys:
                     raise ValueError("the checkpoint holds no surrogate state to resume the surrogate from")
                 a["surrogate"].load_state_arrays({k[len("surrogate."):]: ck[k] for k in keys})
-        self._parse_surrogate(a["surrogate"], a["training_set"])
+        self._parse_surrogate(a["surrogate"], a["training_set"], a["refresh_interval"], a["refresh_steps"],
+                              a["refresh_lr"])
         self._parse_tempering(a["temperatures"], a["exchange_interval"], a["exchange_streams"])
         self.use_persistent = a["persistent"]
         self._timers = None
@@ -764,9 +787,17 @@ class HMC:
             return slice(0, m)
         return _torch.from_numpy(idx).to(self.device)
 
-    def _parse_surrogate(self, surrogate, training_set):
+    def _parse_surrogate(self, surrogate, training_set, refresh_interval=None, refresh_steps=300, refresh_lr=2e-4):
         self.surrogate = surrogate
         self.training_set = training_set
+        self.refresh_interval = None
+        if refresh_interval is not None:
+            assert surrogate is not None and training_set is not None, (
+                "`refresh_interval` needs a surrogate and a training_set to append to")
+            assert type(refresh_interval) == int and refresh_interval > 0, "refresh_interval must be a positive int"
+            self.refresh_interval = refresh_interval
+            self.refresh_steps, self.refresh_lr = int(refresh_steps), float(refresh_lr)
+            self.refreshes = 0
         for obj, what in ((surrogate, "surrogate"), (training_set, "training_set")):
             if obj is None:
                 continue
@@ -846,6 +877,8 @@ class HMC:
                 g = self._proposal_base + self._done
                 nxt = -(-g // self.exchange_interval) * self.exchange_interval
                 n = min(n, nxt - g + 1)
+            if self.refresh_interval is not None:
+                n = min(n, self.refresh_interval - self._done % self.refresh_interval)
             self._load_streams(self._done, n)
             if self._persistent is not None:
                 self._persistent.run(n, h)
@@ -876,7 +909,25 @@ class HMC:
                 self._drain(self._done, n)
             self._done += n
             issued += n
+            if self.refresh_interval is not None and self._done % self.refresh_interval == 0 and self._done < self.proposals:
+                self._refresh(h)
         return issued
+
+    def _refresh(self, h):
+        """Exact gradient (and misfit) at every chain's current position into
+        the training set, then more training of the surrogate (see
+        `refresh_interval`)."""
+        dist, dt = self.distribution, self.dtype
+        dist._device_gradient(self.q_cur, self.g, False, dt, h)
+        tx = None
+        if self.training_set.with_values:
+            tx = self._training_x
+            dist._device_misfit_after_gradient(self.q_cur, tx, False, dt, h)
+        if not self.training_set.record(self.q_cur, self.g, h, tx):
+            return  # the training set is full: keep the network as it is
+        self.surrogate.refresh(self.training_set, steps=self.refresh_steps, lr=self.refresh_lr,
+                               seed=self.refreshes, stream=self.stream)
+        self.refreshes += 1
 
     def get_diagnostics(self):
         """The phase timers of diagnostic_mode (reference `Samplers.py:759-764`)."""

@@ -98,23 +98,45 @@ class _Surrogate:
             ok &= torch.isfinite(data.x[:n])
         return _np.flatnonzero(ok.cpu().numpy())
 
-    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None):
+    def train(self, data: TrainingSet, steps=2000, batch=256, lr=1e-3, seed=0, lr_decay=True, stream=None, rows=None,
+              recent=None):
         """Fit the network with Adam on the first `rows` pairs of data (all by
-        default; pairs with non-finite entries are skipped); returns the loss
-        history (host)."""
+        default; pairs with non-finite entries are skipped); with `recent`,
+        half of every minibatch comes from the last `recent` usable pairs.
+        Returns the loss history (host)."""
         rng = _np.random.default_rng(seed)
         n = data.count if rows is None else min(int(rows), data.count)
         usable = self._finite_rows(data, n)
         assert len(usable) >= batch, "not enough (finite) training pairs"
+        tail = usable[-int(recent):] if recent else None
         history = []
         for s in range(steps):
             rate = lr * (0.5 * (1 + _np.cos(_np.pi * s / steps)) if lr_decay else 1.0)
-            idx = usable[rng.integers(0, len(usable), size=batch)]
+            if tail is not None:
+                h = batch // 2
+                idx = _np.concatenate([usable[rng.integers(0, len(usable), size=batch - h)],
+                                       tail[rng.integers(0, len(tail), size=h)]])
+            else:
+                idx = usable[rng.integers(0, len(usable), size=batch)]
             loss = self.train_step(data, idx, lr=float(rate), stream=stream)
             if s % 50 == 0 or s == steps - 1:
                 history.append((s, float(loss[0].item())))
         self.check_status()
         return history
+
+    def refresh(self, data: TrainingSet, steps=300, lr=2e-4, recent=640, seed=0, stream=None):
+        """Continue training on pairs appended since the fit (for example
+        exact gradients at the chains' current positions) with the fit's
+        normalisation kept, then freeze again.  Used between blocks of
+        surrogate-driven proposals: every block runs with a fixed network,
+        so each block's kernel leaves the exact posterior invariant."""
+        self.frozen = False
+        self._extend_targets(data)
+        self.train(data, steps=steps, lr=lr, seed=seed, lr_decay=False, stream=stream, recent=recent)
+        return self.freeze()
+
+    def _extend_targets(self, data: TrainingSet):
+        """Per-pair targets that depend on the stored pairs (none here)."""
 
     def fit(self, data: TrainingSet, steps=3000, batch=256, lr=1e-3, holdout_fraction=0.1, check_every=200,
             seed=0, stream=None):
@@ -672,19 +694,35 @@ class PotentialSurrogate(_Surrogate):
         import torch
 
         self._vt = None
+        self._quad_host = (A, beta)
         if not (self.value_weight > 0 and data.with_values):
             return
         n = data.count
-        q = data.q[:n].double().cpu().numpy()
-        x = (q - self.mu_q.double().cpu().numpy()) * self.inv_q.double().cpu().numpy()
-        U = data.x[:n].cpu().numpy()
-        quad = 0.5 * _np.einsum("bi,ij,bj->b", x, A, x) + x @ beta
-        t = U - quad
+        t = self._targets_host(data, 0, n)
         sel = _np.arange(n) if rows is None else _np.asarray(rows)
         sel = sel[_np.isfinite(t[sel])]
         var = float(_np.var(t[sel])) if sel.size > 1 else 1.0
         self._vt_w = float(self.value_weight / max(var, 1e-300))
         self._vt = torch.from_numpy(_np.where(_np.isfinite(t), t, 0.0)).to(self.device)
+
+    def _targets_host(self, data: TrainingSet, start, stop):
+        """Exact misfit minus the quadratic part at stored pairs [start, stop)."""
+        A, beta = self._quad_host
+        q = data.q[start:stop].double().cpu().numpy()
+        x = (q - self.mu_q.double().cpu().numpy()) * self.inv_q.double().cpu().numpy()
+        U = data.x[start:stop].cpu().numpy()
+        return U - (0.5 * _np.einsum("bi,ij,bj->b", x, A, x) + x @ beta)
+
+    def _extend_targets(self, data: TrainingSet):
+        """Value targets of pairs stored after the fit (the quadratic part and
+        the normalisation stay those of the fit)."""
+        import torch
+
+        if self._vt is None or data.count <= self._vt.numel():
+            return
+        t = self._targets_host(data, self._vt.numel(), data.count)
+        t = torch.from_numpy(_np.where(_np.isfinite(t), t, 0.0)).to(self.device)
+        self._vt = torch.cat([self._vt, t])
 
     def value_error(self, data: TrainingSet, rows, stream=None):
         """Standard deviation over the given stored pairs (at most 1024) of

@@ -137,3 +137,42 @@ def test_surrogate_cheapens_small_fwi_proposals():
     assert fit["best_heldout"] < 0.05
     assert t_sur < t_plain / 3.0
     assert acc_sur > 0.5 * acc_plain
+
+
+def test_refresh_appends_exact_pairs_and_retrains_between_blocks():
+    """refresh_interval: after every block the exact gradient and misfit at
+    each chain's position join the training set (checked against the
+    target), the potential trains further with its values matched, and the
+    chains stay on the exact posterior."""
+    import hmclab_gb300 as H
+    from hmclab_gb300 import surrogate as S
+
+    post, mean, cov = linear_problem()
+    d, C, L = 32, 512, 5
+    rng = np.random.default_rng(7)
+    Lc = np.linalg.cholesky(cov)
+    q0 = mean + Lc @ rng.normal(size=(d, C))
+    data = S.TrainingSet(d, 3 * L * C + 3 * C, values=True)
+    kw = dict(stepsize=0.1, amount_of_steps=L, chains=C, dtype="float32")
+    burn = H.Samplers.HMC(seed=1).sample(None, post, initial_model=q0, proposals=3, training_set=data, **kw)
+    n0 = data.count
+    assert n0 == 3 * L * C and torch.isfinite(data.x[:n0]).all()
+    x_ref = post.misfit_batch(data.q[:n0].t().contiguous())
+    assert torch.allclose(data.x[:n0], x_ref, rtol=1e-5)
+    net = S.PotentialSurrogate(d, hidden=(64, 64), seed=0)
+    net.value_weight = 1.0
+    net.fit(data, steps=400, batch=256)
+    steps0 = net.steps
+    smp = H.Samplers.HMC(seed=2).sample(None, post, initial_model=burn.current_model, proposals=40,
+                                        surrogate=net.freeze(), training_set=data, refresh_interval=10,
+                                        refresh_steps=50, keep_samples=True, **kw)
+    assert smp.refreshes == 3  # after proposals 10, 20, 30 (not after the last)
+    assert data.count == n0 + 3 * C and net.steps == steps0 + 150 and net.frozen
+    g_ref = post.gradient_batch(data.q[n0:data.count].t().contiguous())
+    err = (data.g[n0:data.count].t() - g_ref).abs().max().item()
+    assert err <= 1e-5 * g_ref.abs().max().item()
+    assert net._vt.numel() == data.count
+    q = smp.samples_numpy()[:, :-1, :]  # C, d, N
+    z = (q[:, :, -1].mean(axis=0) - mean[:, 0]) / (np.sqrt(np.diag(cov)) / np.sqrt(C))
+    assert np.abs(z).max() < 5.0
+    assert 0.2 < np.mean(np.atleast_1d(smp.accepted_proposals)) / 40
