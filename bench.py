@@ -980,8 +980,12 @@ def run_fwi_arm(args, wl):
     t_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     t_step = forward_step_timing(lik, smp_s)
     smp_s.finish()
-    qs = smp_s.samples_device[0][W * B:]  # [K*B][d][C]
+    qall = smp_s.samples_device[0]  # [(W+K)*B][d][C]
+    qs = qall[W * B:]
     N = qs.shape[0]
+    # acceptance per block, read from the samples (a chain accepted when its position changed)
+    moved = (qall[1:] != qall[:-1]).any(dim=1).double().mean(dim=1).cpu().numpy()
+    acc_blocks = [round(float(moved[max(0, k * B - 1):(k + 1) * B - 1].mean()), 4) for k in range(W + K)]
     ess_s_raw = diagnostics.ess(qs, lags=min(N // 2, 200))
     acc_s = float(np.mean(smp_s.accepted_proposals) / ((W + K) * B))
     bulk_s = np.abs(diagnostics.ess(qs, lags=min(N // 2, 200), rank_normalize=True))
@@ -1048,7 +1052,8 @@ def run_fwi_arm(args, wl):
         "refresh": {"interval": R, "adam_steps": args.refresh_steps if R else 0, "refreshes": refreshes_timed,
                     "note": "after every block: exact gradient and misfit at the chains' current positions appended "
                             "to the training set, then more training; inside the timed region"},
-        "acceptance": acc_s, "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
+        "acceptance": acc_s, "acceptance_per_block": acc_blocks,
+        "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
                                                       "pilot": [[L_, e_, round(a_, 4)] for _, L_, e_, a_ in pilot]},
         "plain": {"value": plain_value, "proposals_timed": Kp, "ms_per_proposal": 1e3 * t_p / Kp,
                   "acceptance": acc_p, "ess_per_chain_proposal": e_plain,

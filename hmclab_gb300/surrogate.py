@@ -130,9 +130,18 @@ class _Surrogate:
         normalisation kept, then freeze again.  Used between blocks of
         surrogate-driven proposals: every block runs with a fixed network,
         so each block's kernel leaves the exact posterior invariant."""
+        import contextlib
+
+        import torch
+
+        if stream is not None:
+            stream.synchronize()  # the appended pairs were written on the sampler's stream; host reads follow
         self.frozen = False
         self._extend_targets(data)
-        self.train(data, steps=steps, lr=lr, seed=seed, lr_decay=False, stream=stream, recent=recent)
+        # every launch and copy of the training (index uploads included) on
+        # the one stream, ordered after the sampler's work
+        with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
+            self.train(data, steps=steps, lr=lr, seed=seed, lr_decay=False, recent=recent)
         return self.freeze()
 
     def _extend_targets(self, data: TrainingSet):
