@@ -408,7 +408,7 @@ class FwiWorkload:
     # chain; 20 steps = 320 proposals, so that the ESS lag windows of the
     # surrogate run can reach past its slowest parameters' autocorrelation
     default_steps, default_warmup = 20, 3
-    block = 16
+    block = 32
     burn_in = 12  # exact proposals recording (position, gradient) training pairs
 
     def __init__(self, seed=0, chains=None):
@@ -907,7 +907,7 @@ def run_fwi_arm(args, wl):
 
     # ---- exact proposals from the start states, recording training pairs --
     R = args.refresh_interval if args.refresh_interval > 0 else None
-    extra = 2 * (W + K) * B // R * C if R else 0  # rows the refreshes of the timed and e2e runs append
+    extra = (W + K) * B // R * C if R else 0  # rows the refreshes of the surrogate run append
     data = S.TrainingSet(d, Nb * L * C + extra, values=args.value_weight > 0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -928,7 +928,6 @@ def run_fwi_arm(args, wl):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     net.freeze()
-    fitted, n_fit = net.state_arrays(), data.count
 
     # ---- pilot (untimed): the surrogate run's trajectory ------------------
     # A few proposals per (L, stepsize) from the start states; the setting
@@ -953,7 +952,13 @@ def run_fwi_arm(args, wl):
     kw_s = dict(kw, amount_of_steps=L_best, stepsize=eps_best)
 
     # ---- surrogate-driven HMC: W untimed blocks, then K timed blocks -------
+    # The run goes through the public API from host arrays to host arrays:
+    # `e2e` is its wall time from the upload of the start states (prepare) to
+    # the samples back on the host; `value` uses the device time of the K
+    # timed blocks (CUDA events on the sampler's stream).
     refresh_kw = dict(training_set=data, refresh_interval=R, refresh_steps=args.refresh_steps) if R else {}
+    torch.cuda.synchronize()
+    t_e2e0 = time.perf_counter()
     smp_s = H.Samplers.HMC(seed=sharding.rank_seed(200, rank))
     smp_s.prepare(None, post, initial_model=q_start, proposals=(W + K) * B, keep_samples=True, surrogate=net,
                   **refresh_kw, **kw_s)
@@ -978,8 +983,10 @@ def run_fwi_arm(args, wl):
         torch.distributed.barrier()
     clk = clocks.stop()
     t_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-    t_step = forward_step_timing(lik, smp_s)
     smp_s.finish()
+    host_q, host_x = smp_s.samples_host()
+    t_e2e = time.perf_counter() - t_e2e0
+    t_step = forward_step_timing(lik, smp_s)
     qall = smp_s.samples_device[0]  # [(W+K)*B][d][C]
     qs = qall[W * B:]
     N = qs.shape[0]
@@ -1016,20 +1023,9 @@ def run_fwi_arm(args, wl):
     e_plain = float(ref["ess_per_chain_proposal"]) if ref is not None else None
     plain_value = e_plain * C * world * Kp / t_p if e_plain is not None else None
 
-    # ---- end to end through the public API with host buffers -------------
-    # the same method from the fitted network: the timed run's refreshes are undone
+    # ---- end to end: the same run, wall clock, host arrays in and out ------
     refreshes_timed = getattr(smp_s, "refreshes", 0)
-    net.load_state_arrays(fitted)
-    data.count = n_fit
-    if getattr(net, "_vt", None) is not None:
-        net._vt = net._vt[:n_fit]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    smp_e = H.Samplers.HMC(seed=sharding.rank_seed(400, rank)).sample(
-        None, post, initial_model=q_start, proposals=K * B, keep_samples=True, surrogate=net, **refresh_kw, **kw_s)
-    host_q, host_x = smp_e.samples_host()
-    t_e2e = time.perf_counter() - t0
-    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(K * B // 2, 200)))
+    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(host_q.shape[0] // 2, 200)))
     e2e_measured = float(ess_e.min() / t_e2e)
 
     hbm, bf16, bf16s, src = peaks()
@@ -1071,8 +1067,10 @@ def run_fwi_arm(args, wl):
                       "best_step": fit["best_step"]},
         "setup_seconds": t_setup,
         "e2e": {"value": e2e_measured if not reasons else None, "value_measured": e2e_measured, "unit": UNIT,
-                "h2d_bytes_per_step": int(q_start.size * 8 / K), "d2h_bytes_per_step": int(B * (d * C * 4 + C * 8)),
-                "seconds": t_e2e},
+                "h2d_bytes_per_step": int(q_start.size * 8 / (W + K)), "d2h_bytes_per_step": int(B * (d * C * 4 + C * 8)),
+                "seconds": t_e2e, "note": "wall time of the timed run itself through the public API (prepare from "
+                                          "host start states, W + K blocks, samples back to the host); ESS over "
+                                          "all its draws"},
         "gpu_launches": int(launches),
         "roofline": {"kernel": "fwi forward time step: velocity_tma_kernel + stress_tma_kernel (the exact misfit)",
                      "bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
@@ -1245,7 +1243,7 @@ def main():
     ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
     ap.add_argument("--value-weight", type=float, default=1.0,
                     help="fwi: weight of the misfit-value matching loss of the potential surrogate (0: gradients only)")
-    ap.add_argument("--refresh-interval", type=int, default=16,
+    ap.add_argument("--refresh-interval", type=int, default=32,
                     help="fwi: surrogate proposals between refreshes of the network on exact gradients at the chains' "
                          "positions (0: never)")
     ap.add_argument("--refresh-steps", type=int, default=300, help="fwi: Adam steps per refresh")
