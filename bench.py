@@ -405,10 +405,10 @@ class FwiWorkload:
     noise_fraction = 10.0  # data noise std / RMS of the true records
     hidden = (512, 512)
     # a step is one block of `block` surrogate-driven proposals of every
-    # chain; 20 steps = 320 proposals, so that the ESS lag windows of the
-    # surrogate run can reach past its slowest parameters' autocorrelation
+    # chain; 20 steps = 2000 proposals, so that the ESS lag windows of the
+    # surrogate run (autocorrelation times near 200 proposals) truncate
     default_steps, default_warmup = 20, 3
-    block = 32
+    block = 100
     burn_in = 12  # exact proposals recording (position, gradient) training pairs
 
     def __init__(self, seed=0, chains=None):
@@ -993,11 +993,18 @@ def run_fwi_arm(args, wl):
     # acceptance per block, read from the samples (a chain accepted when its position changed)
     moved = (qall[1:] != qall[:-1]).any(dim=1).double().mean(dim=1).cpu().numpy()
     acc_blocks = [round(float(moved[max(0, k * B - 1):(k + 1) * B - 1].mean()), 4) for k in range(W + K)]
-    ess_s_raw = diagnostics.ess(qs, lags=min(N // 2, 200))
+    # lag windows up to half the run: the surrogate chains decorrelate over
+    # hundreds of proposals
+    ess_s_raw = diagnostics.ess(qs, lags=min(N // 2, 1000))
     acc_s = float(np.mean(smp_s.accepted_proposals) / ((W + K) * B))
-    bulk_s = np.abs(diagnostics.ess(qs, lags=min(N // 2, 200), rank_normalize=True))
+    # rank normalisation compares every pooled draw with every other (S^2 per
+    # parameter); reported when that stays below the library's limit
+    S_pool = N * C
+    bulk_s = (np.abs(diagnostics.ess(qs, lags=min(N // 2, 1000), rank_normalize=True))
+              if S_pool * S_pool * d <= 1.0e12 else None)
     ess_s, t_s = sharding.combine_ess(np.abs(ess_s_raw), t_s)
-    bulk_s, _ = sharding.combine_ess(bulk_s, t_s)
+    if bulk_s is not None:
+        bulk_s, _ = sharding.combine_ess(bulk_s, t_s)
     mean_s, std_s = sharding.combine_moments(*diagnostics.moments(qs), N * C)
     mc = moment_check(mean_s, std_s, ess_s, ref) if ref is not None else None
     reasons = fwi_validity(ess_s_raw, mc)
@@ -1025,7 +1032,7 @@ def run_fwi_arm(args, wl):
 
     # ---- end to end: the same run, wall clock, host arrays in and out ------
     refreshes_timed = getattr(smp_s, "refreshes", 0)
-    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(host_q.shape[0] // 2, 200)))
+    ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(host_q.shape[0] // 2, 1000)))
     e2e_measured = float(ess_e.min() / t_e2e)
 
     hbm, bf16, bf16s, src = peaks()
@@ -1044,7 +1051,9 @@ def run_fwi_arm(args, wl):
             "value": float(ess_s.min() / (t_burn + t_train + t_s)),
             "note": "min-ESS over (exact training-pair proposals + surrogate training + sampling) seconds"},
         "ess_window_truncated": float(np.mean(ess_s_raw >= 0)), "proposals_per_chain": N,
-        "rank_normalised_bulk": {"value": float(bulk_s.min() / t_s)},
+        "rank_normalised_bulk": ({"value": float(bulk_s.min() / t_s)} if bulk_s is not None else
+                                 {"value": None, "note": "skipped: pooled rank normalisation of this many draws "
+                                                         "exceeds the library's comparison limit"}),
         "refresh": {"interval": R, "adam_steps": args.refresh_steps if R else 0, "refreshes": refreshes_timed,
                     "note": "after every block: exact gradient and misfit at the chains' current positions appended "
                             "to the training set, then more training; inside the timed region"},
