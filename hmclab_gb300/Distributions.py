@@ -359,6 +359,39 @@ class Laplace(_AbstractDistribution):
         return Laplace(_numpy.random.rand(dimensions, 1), 10 ** _numpy.random.rand(dimensions, 1))
 
 
+class Uniform(_AbstractDistribution):
+    """Uniform distribution between `lower_bounds` and `upper_bounds`
+    (reference `base.py:747-800`): misfit and gradient are zero inside the
+    bounds (one memset on the device), +inf outside through misfit_bounds;
+    the sampler keeps every chain inside them by reflection."""
+
+    def __init__(self, lower_bounds, upper_bounds):
+        self.name = "uniform distribution"
+        lower = _numpy.asarray(lower_bounds, dtype=_numpy.float64)
+        lower = _numpy.resize(lower, (lower.size, 1))
+        upper = _numpy.asarray(upper_bounds, dtype=_numpy.float64)
+        upper = _numpy.resize(upper, (upper.size, 1))
+        self.dimensions = int(lower.size)
+        self.update_bounds(lower, upper)
+
+    def _device_misfit(self, M, out, accumulate, dtype, stream):
+        if not accumulate:
+            _lib.call("hmc_fill_zero", out.data_ptr(), out.numel() * out.element_size(), stream)
+
+    def _device_gradient(self, M, out, accumulate, dtype, stream):
+        if not accumulate:
+            _lib.call("hmc_fill_zero", out.data_ptr(), out.numel() * out.element_size(), stream)
+
+    def generate(self, repeat=1, rng=_numpy.random.default_rng()) -> _numpy.ndarray:
+        return rng.uniform(self.lower_bounds, self.upper_bounds, (self.dimensions, repeat))
+
+    @staticmethod
+    def create_default(dimensions: int) -> "Uniform":
+        lower = _numpy.random.rand(dimensions, 1) * 5 - 10
+        upper = _numpy.random.rand(dimensions, 1) * 5 + 10
+        return Uniform(lower, upper)
+
+
 class AdditiveDistribution(_AbstractDistribution):
     """Sum of misfits and gradients of several distributions, with bounds
     collapsed to the tightest set (reference `base.py:1005-1142`)."""
@@ -688,15 +721,20 @@ class ElasticFullWaveform2D(_AbstractDistribution):
     `ElasticFullWaveform2D.py:12-226`), computed by the project's own FP32
     finite-difference kernels instead of psvWave, for C chains at once.
 
-    `_input` is an `hmclab_gb300.fwi.ElasticConfig` (the reference takes a
-    psvWave .ini file) or another ElasticFullWaveform2D to copy.  Observed
-    records `ux_obs`, `uz_obs` are [shots][nt][receivers].  The misfit is
-    0.5 * sum (u - u_obs)^2 / data_std^2 / temperature.  The model is
-    parametrised by Gaussian blobs (`free_parameter_grid=[nx, nz]`,
-    `make_blob`), m = [vp blobs | vs blobs | rho blobs], fine fields =
-    basis @ m + background.  The gradient is the exact derivative of the
-    discrete misfit (chain rule through the basis); `gradient_projection=
-    "least_squares"` instead applies the reference's (C^T C)^-1 C^T map
+    `_input` is the path of a psvWave .ini file (read by
+    `hmclab_gb300.fwi.read_ini`, as the reference hands it to psvWave), an
+    `hmclab_gb300.fwi.ElasticConfig`, or another ElasticFullWaveform2D to
+    copy; anything else raises ValueError, and so does a new object without
+    observed data.  Observed records `ux_obs`, `uz_obs` are
+    [shots][nt][receivers].  The misfit is 0.5 * sum (u - u_obs)^2 /
+    data_std^2 / temperature.  Without `free_parameter_grid` the model vector
+    is psvWave's: absolute (vp, vs, rho) of every cell (or npx x npz block)
+    of the free-parameter region (`fwi.CellBasis`); `free_parameter_grid=
+    [nx, nz]` / `make_blob` switches to Gaussian-blob amplitudes relative to
+    the background (`fwi.BlobBasis`), m = [vp | vs | rho] either way.  The
+    gradient is the exact derivative of the discrete misfit (chain rule
+    through the parametrisation); `gradient_projection="least_squares"`
+    applies the reference's (C^T C)^-1 C^T map to blob gradients instead
     (ElasticFullWaveform2D.py:159, 329-330)."""
 
     temperature: float = 1.0
@@ -722,11 +760,12 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             uz_obs = src.uz_obs if uz_obs is None else uz_obs
             temperature = src.temperature if temperature is None else temperature
             data_std = src.data_std
-            free_parameter_grid = free_parameter_grid or ([src.blob.nbx, src.blob.nbz] if src.blob else None)
+            if free_parameter_grid is None and isinstance(src.blob, _fwi.BlobBasis):
+                free_parameter_grid = [src.blob.nbx, src.blob.nbz]
             gradient_projection = src.gradient_projection
-        elif isinstance(_input, _fwi.ElasticConfig):
-            self.config = _input
-            self.background = background if background is not None else _fwi.layered_model(_input, anomalies=False)
+        elif isinstance(_input, (str, _fwi.ElasticConfig)) or hasattr(_input, "__fspath__"):
+            self.config = _input if isinstance(_input, _fwi.ElasticConfig) else _fwi.ElasticConfig.from_ini(_input)
+            self.background = background if background is not None else _fwi.background_model(self.config)
         else:
             raise ValueError(f"Incorrect initialization. Passed argument `{_input}` can not create an FWI object.")
         if ux_obs is None or uz_obs is None:
@@ -737,10 +776,17 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         self.temperature = 1.0 if temperature is None else float(temperature)
         self.data_std = float(data_std)
         self.gradient_projection = gradient_projection
-        self.blob = None
-        self.dimensions = 3 * cfg.nx * cfg.nz
         if free_parameter_grid is not None:
             self.make_blob(*free_parameter_grid)
+        else:
+            self.blob = _fwi.CellBasis(cfg, *cfg.cell_block)
+            self.dimensions = self.blob.free_parameters
+
+    @property
+    def use_blob_par(self):
+        from hmclab_gb300 import fwi as _fwi
+
+        return isinstance(self.blob, _fwi.BlobBasis)
 
     def make_blob(self, nx, nz):
         from hmclab_gb300 import fwi as _fwi
@@ -755,35 +801,62 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         return 1.0 / (self.data_std**2 * self.temperature)
 
     def fine_model(self, m):
-        """Physical (vp, vs, rho) fields [nz][nx] of a blob model vector (host)."""
+        """Physical (vp, vs, rho) fields [nz][nx] of a model vector (host)."""
         m = _numpy.asarray(m, dtype=_numpy.float64).reshape(3, -1)
         cfg = self.config
-        return tuple((self.blob.B @ m[f]).reshape(cfg.nz, cfg.nx) + self.background[f] for f in range(3))
+        return tuple((self.blob.to_physical(m[f]) + self.blob.base_field(self.background[f]).reshape(-1))
+                     .reshape(cfg.nz, cfg.nx) for f in range(3))
 
     # ---- device parameters ------------------------------------------------
     def _make_params(self, dtype):
-        if self.blob is None:
-            raise NotImplementedError("the device path needs the blob parametrisation (make_blob)")
         cfg = self.config
-        Bs = self.blob.simulation_basis()  # [cells][blobs]
-        bg = [cfg.extend(self.background[f]).reshape(-1) for f in range(3)]  # vp, vs, rho
+        # the fields the parameters add to, on the simulation grid
+        rows = cfg.extension_matrix_rows()
+        bg = []
+        for f in range(3):
+            base = self.blob.base_field(self.background[f]).reshape(-1)
+            full = cfg.extend(_numpy.asarray(self.background[f], _numpy.float64)).reshape(-1)
+            bg.append(_numpy.where(rows >= 0, base[_numpy.maximum(rows, 0)], full))
         obs = _numpy.stack([self.ux_obs, self.uz_obs], axis=-1)  # shots, nt, rec, 2
         rec_map = -_numpy.ones((cfg.nzc, cfg.nxc), _numpy.int32)
         for r, (x, z) in enumerate(zip(cfg.rec_x, cfg.rec_z)):
             rec_map[z, x] = r
         p = {
-            "B": _dev.upload(Bs, "float32"),
-            "Bt": _dev.upload(_numpy.ascontiguousarray(Bs.T), "float32"),
             "bg": [_dev.upload(b, "float32") for b in bg],
             "taper": _dev.upload(cfg.taper(), "float32"),
             "rec_map": _dev.upload_int32(rec_map),
             "obs": _dev.upload(obs, "float32"),
             "stf_host": _numpy.ascontiguousarray(cfg.ricker(), dtype=_numpy.float32),
+            # per shot: the source records (kept alive beside the wavelets
+            # they point to) of configurations with more than one explosion
+            "sources": [self._source_array(k) for k in range(cfg.n_shots)],
         }
-        if self.gradient_projection == "least_squares":
-            B = self.blob.B
-            p["proj"] = _dev.upload(_numpy.linalg.inv(B.T @ B), "float32")
+        if self.use_blob_par:
+            Bs = self.blob.simulation_basis()  # [cells][blobs]
+            p["B"] = _dev.upload(Bs, "float32")
+            p["Bt"] = _dev.upload(_numpy.ascontiguousarray(Bs.T), "float32")
+            if self.gradient_projection == "least_squares":
+                B = self.blob.B
+                p["proj"] = _dev.upload(_numpy.linalg.inv(B.T @ B), "float32")
+        else:
+            ptr, cells = self.blob.gradient_segments()
+            p["map"] = _dev.upload_int32(self.blob.simulation_map())
+            p["seg_ptr"] = _dev.upload_int32(ptr)
+            p["seg_cells"] = _dev.upload_int32(cells)
         return p
+
+    def _source_array(self, shot):
+        """(hmc_fwi_source array, wavelets) of one shot."""
+        import ctypes
+
+        srcs = self.config.shots[shot]
+        stf = _numpy.ascontiguousarray(self.config.shot_wavelets(shot), dtype=_numpy.float32)
+        arr = (_lib.HmcFwiSource * len(srcs))()
+        for k, q in enumerate(srcs):
+            arr[k].x, arr[k].z = q.x, q.z
+            arr[k].mxx, arr[k].mzz, arr[k].mxz = q.mxx, q.mzz, q.mxz
+            arr[k].stf_host = stf[k].ctypes.data_as(ctypes.c_void_p).value
+        return arr, stf
 
     def _workspace(self, C, device, with_gradient):
         import torch
@@ -808,8 +881,9 @@ class ElasticFullWaveform2D(_AbstractDistribution):
                 ws[name] = z(cells, C)
             ws["store"] = z(cfg.nt * 2 * cells * C)
             ws["resid"] = z(cfg.nt * cfg.n_rec * 2 * C)
-            ws["gtmp"] = z(self.blob.n_blobs, C)
-            ws["proj_work"] = z(64 * self.blob.n_blobs * C)  # split-k partial products
+            if self.use_blob_par:
+                ws["gtmp"] = z(self.blob.n_blobs, C)
+                ws["proj_work"] = z(64 * self.blob.n_blobs * C)  # split-k partial products
         return ws
 
     def _descriptor(self, ws, C):
@@ -833,13 +907,17 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         return d
 
     def _set_model(self, M, ws, stream):
-        """Blob amplitudes (3*nb, C) FP32 -> simulation-grid fields."""
+        """Model vectors (3*nb, C) FP32 -> simulation-grid fields."""
         p = self._params("float32")
         nb, C = self.blob.n_blobs, M.shape[1]
         cells = self.config.nzc * self.config.nxc
         for f, name in enumerate(("vp", "vs", "rho")):
-            _lib.call("hmc_gemm", _lib.HMC_F32, cells, C, nb, 1.0, p["B"].data_ptr(), M[f * nb:(f + 1) * nb].data_ptr(),
-                      p["bg"][f].data_ptr(), ws[name].data_ptr(), 0, stream)
+            if self.use_blob_par:
+                _lib.call("hmc_gemm", _lib.HMC_F32, cells, C, nb, 1.0, p["B"].data_ptr(),
+                          M[f * nb:(f + 1) * nb].data_ptr(), p["bg"][f].data_ptr(), ws[name].data_ptr(), 0, stream)
+            else:
+                _lib.call("hmc_fwi_cell_model", cells, C, p["map"].data_ptr(), M[f * nb:(f + 1) * nb].data_ptr(),
+                          p["bg"][f].data_ptr(), ws[name].data_ptr(), stream)
 
     def _shot_graph(self, ws, C, shot, store_and_adjoint):
         """CUDA graph of one shot's 2*nt half-step launches (and its adjoint),
@@ -855,12 +933,16 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             d = self._descriptor(ws, C)
             ws.setdefault("descriptors", []).append(d)  # keep the struct alive with the graph
             ref = ctypes.byref(d)
-            sx, sz = self.config.src[shot]
             cap = torch.cuda.Stream()
             h = cap.cuda_stream
             _lib.call("hmc_graph_begin", h)
             try:
-                _lib.call("hmc_fwi_forward_shot", ref, shot, sx, sz, int(store_and_adjoint), h)
+                if self.config.explosive_shots:
+                    sx, sz = self.config.src[shot]
+                    _lib.call("hmc_fwi_forward_shot", ref, shot, sx, sz, int(store_and_adjoint), h)
+                else:
+                    arr, _ = self._params("float32")["sources"][shot]
+                    _lib.call("hmc_fwi_forward_shot_sources", ref, shot, arr, len(arr), int(store_and_adjoint), h)
                 if store_and_adjoint:
                     _lib.call("hmc_fwi_adjoint_shot", ref, shot, h)
             finally:
@@ -934,6 +1016,10 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         cells = self.config.nzc * self.config.nxc
         for f, name in enumerate(("g_vp", "g_vs", "g_rho")):
             dst = out[f * nb:(f + 1) * nb]
+            if not self.use_blob_par:
+                _lib.call("hmc_fwi_cell_gradient", nb, C, p["seg_ptr"].data_ptr(), p["seg_cells"].data_ptr(),
+                          ws[name].data_ptr(), dst.data_ptr(), int(accumulate), stream)
+                continue
             work, nwork = ws["proj_work"].data_ptr(), ws["proj_work"].numel()
             if self.gradient_projection == "least_squares":
                 _lib.call("hmc_gemm_splitk", _lib.HMC_F32, nb, C, cells, 1.0, p["Bt"].data_ptr(), ws[name].data_ptr(),
@@ -969,8 +1055,34 @@ class ElasticFullWaveform2D(_AbstractDistribution):
                   _dev.stream_handle(stream))
 
     def get_model_vector(self):
-        return _numpy.zeros((self.dimensions, 1))
+        """Model vector of the background (reference
+        `ElasticFullWaveform2D.py:186-190`): the background's vp, vs, rho per
+        free cell, or zero blob amplitudes."""
+        return self.blob.background_vector(self.background)[:, None]
+
+    def generate(self, repeat=1, rng=_numpy.random.default_rng()) -> _numpy.ndarray:
+        raise _InvalidCaseError("Can't generate samples from non-analytic distributions.")
 
     @staticmethod
-    def create_default(dimensions: int, ini_file=None, omp_threads_override: int = 0):
-        raise _InvalidCaseError("construct ElasticFullWaveform2D from an hmclab_gb300.fwi.ElasticConfig")
+    def create_default(dimensions: int, ini_file=None, omp_threads_override: int = 0) -> "ElasticFullWaveform2D":
+        """The reference's default problem (`ElasticFullWaveform2D.py:85-128`):
+        the configuration of `ini_file` (a psvWave .ini; default: this
+        package's 200 x 100-cell ElasticConfig), a target with a circular
+        anomaly of radius 15 (in the grid's length unit) at the middle of
+        the model (vp and vs -10 %, rho +10 %) and its noise-free records,
+        simulated on the GPU, as observed data.  `dimensions` must equal the
+        free parameters of the cell parametrisation (else InvalidCaseError)."""
+        from hmclab_gb300 import fwi as _fwi
+
+        cfg = _fwi.ElasticConfig() if ini_file is None else _fwi.ElasticConfig.from_ini(ini_file)
+        zeros = _numpy.zeros((cfg.n_shots, cfg.nt, cfg.n_rec))
+        model = ElasticFullWaveform2D(cfg, zeros, zeros, omp_threads_override=omp_threads_override)
+        if model.dimensions != dimensions:
+            raise _InvalidCaseError(f"{model.dimensions} is not equal to {dimensions}")
+        X, Z = cfg.cell_centres()
+        circle = _numpy.hypot(X - 0.5 * (X.max() + X.min()), Z - 0.5 * (Z.max() + Z.min())) < 15
+        vp, vs, rho = (_numpy.asarray(f, _numpy.float64) for f in model.background)
+        target = (vp * (1 - 0.1 * circle), vs * (1 - 0.1 * circle), rho * (1 + 0.1 * circle))
+        m_target = _numpy.concatenate([model.blob.fit(target[f]) for f in range(3)])
+        ux, uz = model.synthetic_records(m_target)
+        return ElasticFullWaveform2D(cfg, ux, uz, omp_threads_override=omp_threads_override)

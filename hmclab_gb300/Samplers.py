@@ -329,7 +329,10 @@ class HMC:
         chains = 1 if chains is None else int(chains)
         assert chains > 0, "The number of chains should be a positive integer."
         self.chains = chains
-        self.dtype = _dev.normalise_dtype(dtype) if dtype is not None else ("float64" if chains == 1 else "float32")
+        # default: FP64 for a single chain (the reference's arithmetic) unless
+        # the target's kernels are FP32 only, FP32 for batches of chains
+        single = getattr(distribution, "single_dtype", "float64")
+        self.dtype = _dev.normalise_dtype(dtype) if dtype is not None else (single if chains == 1 else "float32")
         # step size: scalar or one per chain
         eps = _numpy.asarray(stepsize, dtype=_numpy.float64).reshape(-1)
         assert eps.size in (1, chains), "stepsize must be a scalar or one value per chain"

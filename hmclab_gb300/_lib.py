@@ -108,6 +108,19 @@ class HmcFwi(_ct.Structure):
         "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial", "status")]
 
 
+class HmcFwiSource(_ct.Structure):
+    """Mirror of `hmc_fwi_source` in include/hmclab_gb300.h."""
+
+    _fields_ = [
+        ("x", c_int32),
+        ("z", c_int32),
+        ("mxx", _ct.c_float),
+        ("mzz", _ct.c_float),
+        ("mxz", _ct.c_float),
+        ("stf_host", c_void_p),
+    ]
+
+
 HMC_SCHEDULE_MAX = 64
 
 
@@ -242,6 +255,10 @@ SIGNATURES = {
     "hmc_pot_scale_columns": [I64, I64, P, I64, P, P, I64, S],
     "hmc_fwi_prepare": [P, S],
     "hmc_fwi_forward_shot": [P, I, I, I, I, S],
+    "hmc_fwi_forward_shot_sources": [P, I, P, I, I, S],
+    "hmc_fill_zero": [P, I64, S],
+    "hmc_fwi_cell_model": [I64, I64, P, P, P, P, S],
+    "hmc_fwi_cell_gradient": [I64, I64, P, P, P, P, I, S],
     "hmc_fwi_misfit": [P, I, P, I, S],
     "hmc_fwi_zero_gradients": [P, S],
     "hmc_fwi_adjoint_shot": [P, I, S],

@@ -104,6 +104,31 @@ inline dim3 cell_grid(int nx, int nz, int64_t C) {
 }
 inline dim3 cell_block() { return dim3(TX, TY, TZ); }
 
+// Source injection of one time step: up to MAX_SRC_TERMS stress increments
+// (cell index j * nx + i, and the amounts added to sxx, szz and sxz there),
+// passed by value with every stress launch, and their bounding box so that
+// cells away from the sources test four integers only.  A moment-tensor point
+// source at cell (i, j) adds Mxx s and Mzz s to sxx and szz of that cell and
+// Mxz s / 4 to each of the four sxz nodes around it ((i -/+ 1/2, j -/+ 1/2):
+// flat cells (j-1, i-1), (j-1, i), (j, i-1), (j, i)), s = stf[n] dt / h^2.
+constexpr int MAX_SRC_TERMS = 32;
+struct SourceStep {
+  int n, i0, i1, j0, j1;
+  int cell[MAX_SRC_TERMS];
+  float a_xx[MAX_SRC_TERMS], a_zz[MAX_SRC_TERMS], a_xz[MAX_SRC_TERMS];
+};
+__device__ __forceinline__ void add_sources(const SourceStep& s, int nx, int i, int j, float& sxx, float& szz,
+                                            float& sxz) {
+  if (i < s.i0 || i > s.i1 || j < s.j0 || j > s.j1) return;
+  const int cell = j * nx + i;
+  for (int t = 0; t < s.n; ++t)
+    if (s.cell[t] == cell) {
+      sxx += s.a_xx[t];
+      szz += s.a_zz[t];
+      sxz += s.a_xz[t];
+    }
+}
+
 __global__ void derive_params_kernel(Grid g, const float* __restrict__ rho, const float* __restrict__ vp,
                                      const float* __restrict__ vs, float* bx, float* bz, float* l2m, float* lam,
                                      float* muxz) {
@@ -158,7 +183,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) velocity_kernel(Grid g, Fields f, 
 }
 
 __global__ void __launch_bounds__(TX* TY* TZ) stress_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
-                                                          int src_i, int src_j, float src_value) {
+                                                          const __grid_constant__ SourceStep src) {
   step_dependency_wait();
   step_dependents_go();
   const Cell e = cell_of(g);
@@ -171,10 +196,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) stress_kernel(Grid g, Fields f, Pa
     szz += g.dt * (p.lam[k] * exx + p.l2m[k] * ezz);
     sxz += g.dt * p.muxz[k] * (dxp(f.vx, k, sz, g.inv_h) + dxp(f.vz, k, sx, g.inv_h));
   }
-  if (e.i == src_i && e.j == src_j) {
-    sxx += src_value;
-    szz += src_value;
-  }
+  add_sources(src, g.nx, e.i, e.j, sxx, szz, sxz);
   const float t = taper[e.j * g.nx + e.i];
   f.sxx[k] = sxx * t;
   f.szz[k] = szz * t;
@@ -357,7 +379,8 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
 __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_constant__ CUtensorMap m_vx,
                                                                const __grid_constant__ CUtensorMap m_vz, Grid g,
                                                                Fields f, Params p, const float* __restrict__ taper,
-                                                               int src_i, int src_j, float src_value, int* status) {
+                                                               const __grid_constant__ SourceStep src,
+                                                               int* status) {
   __shared__ __align__(128) float t_vx[TT_Z + 3][TT_X + 3][32];  // rows j0-1.., cells i0-2..
   __shared__ __align__(128) float t_vz[TT_Z + 3][TT_X + 3][32];  // rows j0-2.., cells i0-1..
   __shared__ __align__(8) uint64_t bar;
@@ -416,10 +439,7 @@ __global__ void __launch_bounds__(32 * TT_X) stress_tma_kernel(const __grid_cons
                                t_vz[zz + 2][tx][l]);
       sxz += g.dt * r_mu[zz] * (dvx + dvz);
     }
-    if (i == src_i && j == src_j) {
-      sxx += src_value;
-      szz += src_value;
-    }
+    add_sources(src, g.nx, i, j, sxx, szz, sxz);
     const float t = r_tp[zz];
     f.sxx[k] = sxx * t;
     f.szz[k] = szz * t;
@@ -750,6 +770,31 @@ __global__ void misfit_final_kernel(int64_t C, const double* __restrict__ partia
   out[c] = accumulate ? out[c] + v : v;
 }
 
+// Cell parametrisation.  Model: out[cell][c] = base[cell] + M[map[cell]][c]
+// (map -1: base only), one thread per (cell, chain), chains fastest.
+__global__ void cell_model_kernel(int64_t cells, int64_t C, const int32_t* __restrict__ map,
+                                  const float* __restrict__ M, const float* __restrict__ base, float* __restrict__ out) {
+  const int64_t n = cells * C;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = t / C, c = t - cell * C;
+    const int32_t p = map[cell];
+    out[t] = base[cell] + (p >= 0 ? M[(int64_t)p * C + c] : 0.f);
+  }
+}
+// Gradient: out[p][c] (+)= sum over the cells ptr[p] <= k < ptr[p+1] of
+// g[cells[k]][c], in segment order; one thread per (parameter, chain).
+__global__ void cell_gradient_kernel(int64_t P, int64_t C, const int32_t* __restrict__ ptr,
+                                     const int32_t* __restrict__ cells, const float* __restrict__ g,
+                                     float* __restrict__ out, int accumulate) {
+  const int64_t n = P * C;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / C, c = t - p * C;
+    float acc = 0.f;
+    for (int32_t k = ptr[p]; k < ptr[p + 1]; ++k) acc += g[(int64_t)cells[k] * C + c];
+    out[t] = accumulate ? out[t] + acc : acc;
+  }
+}
+
 // (bx, bz, l+2m, l, muxz) gradients -> (rho, vp, vs) gradients, all cells.
 __global__ void param_gradient_kernel(Grid g, Grads gr, const float* __restrict__ rho, const float* __restrict__ vp,
                                       const float* __restrict__ vs, float* g_rho, float* g_vp, float* g_vs,
@@ -858,9 +903,58 @@ HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream) {
 }
 
 HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_z, int store, void* stream) {
-  HMC_TRY(check_fwi(s, "hmc_fwi_forward_shot"));
-  HMC_REQUIRE(src_x >= 0 && src_x < s->nx && src_z >= 0 && src_z < s->nz, "hmc_fwi_forward_shot: source off grid");
-  HMC_REQUIRE(!store || s->store, "hmc_fwi_forward_shot: storing needs the store buffer");
+  HMC_REQUIRE(s != nullptr, "hmc_fwi_forward_shot: null descriptor");
+  const hmc_fwi_source explosive{src_x, src_z, 1.f, 1.f, 0.f, s->stf_host};
+  return hmc_fwi_forward_shot_sources(s, shot, &explosive, 1, store, stream);
+}
+
+HMC_API int hmc_fwi_forward_shot_sources(const hmc_fwi* s, int shot, const hmc_fwi_source* src, int n_src,
+                                         int store, void* stream) {
+  HMC_TRY(check_fwi(s, "hmc_fwi_forward_shot_sources"));
+  HMC_REQUIRE(src != nullptr && n_src >= 1, "hmc_fwi_forward_shot_sources: no source");
+  int n_terms = 0;
+  for (int q = 0; q < n_src; ++q) {
+    HMC_REQUIRE(src[q].x >= 1 && src[q].x < s->nx && src[q].z >= 1 && src[q].z < s->nz,
+                "hmc_fwi_forward_shot_sources: source %d off the grid's interior", q);
+    HMC_REQUIRE(src[q].stf_host != nullptr, "hmc_fwi_forward_shot_sources: source %d has no wavelet", q);
+    n_terms += src[q].mxz != 0.f ? 4 : 1;
+  }
+  HMC_REQUIRE(n_terms <= MAX_SRC_TERMS,
+              "hmc_fwi_forward_shot_sources: %d stress terms (a moment tensor with Mxz takes 4), at most %d", n_terms,
+              MAX_SRC_TERMS);
+  HMC_REQUIRE(!store || s->store, "hmc_fwi_forward_shot_sources: storing needs the store buffer");
+  // the stress increments of step n; the wavelets are read on the host (a
+  // handful of floats per step)
+  const float src_scale = s->dt / (s->h * s->h);
+  auto source_step = [&](int n) {
+    SourceStep ss{};
+    ss.i0 = s->nx;
+    ss.j0 = s->nz;
+    ss.i1 = ss.j1 = -1;
+    auto term = [&](int i, int j, float axx, float azz, float axz) {
+      ss.cell[ss.n] = j * s->nx + i;
+      ss.a_xx[ss.n] = axx;
+      ss.a_zz[ss.n] = azz;
+      ss.a_xz[ss.n] = axz;
+      ++ss.n;
+      ss.i0 = i < ss.i0 ? i : ss.i0;
+      ss.i1 = i > ss.i1 ? i : ss.i1;
+      ss.j0 = j < ss.j0 ? j : ss.j0;
+      ss.j1 = j > ss.j1 ? j : ss.j1;
+    };
+    for (int q = 0; q < n_src; ++q) {
+      const float v = src[q].stf_host[n] * src_scale;
+      const int i = src[q].x, j = src[q].z;
+      const float xz = 0.25f * src[q].mxz * v;
+      term(i, j, src[q].mxx * v, src[q].mzz * v, xz);
+      if (src[q].mxz != 0.f) {
+        term(i - 1, j - 1, 0.f, 0.f, xz);
+        term(i, j - 1, 0.f, 0.f, xz);
+        term(i - 1, j, 0.f, 0.f, xz);
+      }
+    }
+    return ss;
+  };
   cudaStream_t st = as_stream(stream);
   const Grid g = grid_of(s);
   const int64_t cells = (int64_t)s->nx * s->nz * s->chains;
@@ -873,7 +967,6 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
   Fields f{s->vx, s->vz, s->sxx, s->szz, s->sxz};
   Params p{s->bx, s->bz, s->l2m, s->lam, s->muxz};
   const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block = cell_block();
-  const float src_scale = s->dt / (s->h * s->h);
   float* rec_shot = s->rec + (int64_t)shot * s->nt * s->nrec * 2 * s->chains;
   // tiles staged by the tensor memory accelerator: whole 32-chain tiles and
   // 16-byte row pitches (C a multiple of 32), and a status word for the
@@ -893,14 +986,13 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
                                   s->taper, s->rec_map, rec_n, store_n, s->status);
       if (e != cudaSuccess) return cuda_fail(e, "launch velocity_tma_kernel");
       HMC_TRY(check_launch("velocity_tma_kernel"));
-      e = launch_step(true, stress_tma_kernel, tgrid, tblock, st, m_vx, m_vz, g, f, p, s->taper, src_x, src_z,
-                      s->stf_host[n] * src_scale, s->status);
+      e = launch_step(true, stress_tma_kernel, tgrid, tblock, st, m_vx, m_vz, g, f, p, s->taper, source_step(n),
+                      s->status);
       if (e != cudaSuccess) return cuda_fail(e, "launch stress_tma_kernel");
       HMC_TRY(check_launch("stress_tma_kernel"));
     }
     return HMC_OK;
   }
-  // the source wavelet is read on the host: it is a handful of floats per step
   for (int n = 0; n < s->nt; ++n) {
     float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
     float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
@@ -909,8 +1001,7 @@ HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x, int src_
                                 store_n);
     if (e != cudaSuccess) return cuda_fail(e, "launch velocity_kernel");
     HMC_TRY(check_launch("velocity_kernel"));
-    e = launch_step(true, stress_kernel, grid, block, st, g, f, p, s->taper, src_x, src_z,
-                    s->stf_host[n] * src_scale);
+    e = launch_step(true, stress_kernel, grid, block, st, g, f, p, s->taper, source_step(n));
     if (e != cudaSuccess) return cuda_fail(e, "launch stress_kernel");
     HMC_TRY(check_launch("stress_kernel"));
   }
@@ -1016,6 +1107,22 @@ HMC_API int hmc_fwi_param_gradient(const hmc_fwi* s, float* g_rho, float* g_vp, 
   param_gradient_kernel<<<cell_grid(s->nx, s->nz, s->chains), cell_block(), 0, as_stream(stream)>>>(
       g, gr, s->rho, s->vp, s->vs, g_rho, g_vp, g_vs, accumulate);
   return check_launch("param_gradient_kernel");
+}
+
+HMC_API int hmc_fwi_cell_model(int64_t cells, int64_t C, const int32_t* map, const float* M, const float* base,
+                               float* out, void* stream) {
+  HMC_REQUIRE(cells > 0 && C > 0, "hmc_fwi_cell_model: bad sizes");
+  HMC_REQUIRE(map && M && base && out, "hmc_fwi_cell_model: null buffer");
+  cell_model_kernel<<<blocks_for(cells * C, 256), 256, 0, as_stream(stream)>>>(cells, C, map, M, base, out);
+  return check_launch("cell_model_kernel");
+}
+
+HMC_API int hmc_fwi_cell_gradient(int64_t P, int64_t C, const int32_t* ptr, const int32_t* cells, const float* g,
+                                  float* out, int accumulate, void* stream) {
+  HMC_REQUIRE(P > 0 && C > 0, "hmc_fwi_cell_gradient: bad sizes");
+  HMC_REQUIRE(ptr && cells && g && out, "hmc_fwi_cell_gradient: null buffer");
+  cell_gradient_kernel<<<blocks_for(P * C, 256), 256, 0, as_stream(stream)>>>(P, C, ptr, cells, g, out, accumulate);
+  return check_launch("cell_gradient_kernel");
 }
 
 }  // extern "C"

@@ -133,6 +133,14 @@ int hmc_stream_capturing(void* stream, int* capturing) {
   return HMC_OK;
 }
 
+int hmc_fill_zero(void* ptr, int64_t bytes, void* stream) {
+  HMC_REQUIRE(bytes >= 0 && (ptr != nullptr || bytes == 0), "hmc_fill_zero: bad buffer");
+  if (bytes == 0) return HMC_OK;
+  cudaError_t e = cudaMemsetAsync(ptr, 0, (size_t)bytes, as_stream(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return HMC_OK;
+}
+
 int hmc_graph_begin(void* stream) {
   HMC_REQUIRE(stream != nullptr, "hmc_graph_begin: capture needs a non-default stream");
   cudaError_t e = cudaStreamBeginCapture(as_stream(stream), cudaStreamCaptureModeThreadLocal);

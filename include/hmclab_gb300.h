@@ -70,6 +70,10 @@ HMC_API int hmc_set_wait_limits(uint64_t wait_ns, int withhold);
 /* *capturing = 1 while `stream` is being captured into a CUDA graph (the
  * launch-shape autotuner times nothing then).  No reference counterpart. */
 HMC_API int hmc_stream_capturing(void* stream, int* capturing);
+/* Zero `bytes` of device memory on `stream` (capturable): the misfit and
+ * gradient of a Uniform distribution inside its bounds (reference
+ * hmclab/Distributions/base.py:780-786).                                   */
+HMC_API int hmc_fill_zero(void* ptr, int64_t bytes, void* stream);
 
 /* ---- counter-based RNG (Philox4x32-10, Salmon et al. 2011) ---------------
  * Replaces the numpy Generator draws of MassMatrices.py:142,227,314 and
@@ -574,14 +578,43 @@ typedef struct hmc_fwi {
 
 /* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */
 HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream);
-/* One shot with an explosive source at (src_x, src_z); records into
- * rec[shot]; stores the velocities of every step when store != 0.          */
+/* One shot with an explosive source at (src_x, src_z) and the wavelet
+ * stf_host; records into rec[shot]; stores the velocities of every step when
+ * store != 0.  (psvWave fdModel.forward_simulate, called at
+ * hmclab/Distributions/ElasticFullWaveform2D.py:175-178.)                   */
 HMC_API int hmc_fwi_forward_shot(const hmc_fwi* s, int shot, int src_x,
                                  int src_z, int store, void* stream);
+/* A point source of a shot: moment tensor (Mxx, Mzz, Mxz) at simulation cell
+ * (x, z) of sxx/szz, fed by its own wavelet.  Per step, sxx and szz of the
+ * cell gain M.. * stf[n] * dt / h^2 and each of the four sxz nodes around it
+ * gains Mxz * stf[n] * dt / (4 h^2).  An explosion is (1, 1, 0).           */
+typedef struct hmc_fwi_source {
+  int32_t x, z;             /* 1 <= x < nx, 1 <= z < nz                     */
+  float mxx, mzz, mxz;
+  const float* stf_host;    /* [nt] wavelet, HOST memory                    */
+} hmc_fwi_source;
+/* One shot fired by n_src sources at once (the sources of psvWave's
+ * which_source_to_fire_in_which_shot; moment tensors from moment_angles,
+ * tests/configurations/default_testing_configuration.ini:20-28 of the
+ * reference); at most 32 stress terms: 1 per source, 4 with Mxz != 0.       */
+HMC_API int hmc_fwi_forward_shot_sources(const hmc_fwi* s, int shot,
+                                         const hmc_fwi_source* src, int n_src,
+                                         int store, void* stream);
 /* out_x[c] (+)= 0.5 * w * sum over shots < nshots of (rec - obs)^2, FP64.   */
 HMC_API int hmc_fwi_misfit(const hmc_fwi* s, int nshots, double* out_x,
                            int accumulate, void* stream);
 HMC_API int hmc_fwi_zero_gradients(const hmc_fwi* s, void* stream);
+/* Cell parametrisation (psvWave's own model vector of absolute vp, vs, rho
+ * per cell or block of cells, reference ElasticFullWaveform2D.py:57,194-210):
+ * out[cell][c] = base[cell] + (map[cell] >= 0 ? M[map[cell]][c] : 0), and the
+ * gradient's segmented sum out[p][c] (+)= sum_{ptr[p] <= k < ptr[p+1]}
+ * g[cells[k]][c].  All device memory, [rows][C] chain-fastest.             */
+HMC_API int hmc_fwi_cell_model(int64_t cells, int64_t C, const int32_t* map,
+                               const float* M, const float* base, float* out,
+                               void* stream);
+HMC_API int hmc_fwi_cell_gradient(int64_t P, int64_t C, const int32_t* ptr,
+                                  const int32_t* cells, const float* g,
+                                  float* out, int accumulate, void* stream);
 /* Adjoint of the shot just simulated with store != 0; accumulates into the
  * gradient accumulators.                                                   */
 HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream);

@@ -23,6 +23,11 @@ class _Shot(ctypes.Structure):
         ("nrec", ctypes.c_int),
         ("rec_x", ctypes.c_void_p),
         ("rec_z", ctypes.c_void_p),
+        ("nsrc", ctypes.c_int),
+        ("msrc_x", ctypes.c_void_p),
+        ("msrc_z", ctypes.c_void_p),
+        ("moment", ctypes.c_void_p),
+        ("mstf", ctypes.c_void_p),
     ]
 
 
@@ -42,13 +47,27 @@ def _p(a):
 
 
 class Shot:
-    def __init__(self, nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z):
+    """One shot.  `src` is an explosive source's simulation cell (x, z) fed
+    by `stf`, or, with `sources` = [(x, z, Mxx, Mzz, Mxz), ...] and `stf` of
+    shape [len(sources)][nt], moment-tensor point sources (src unused)."""
+
+    def __init__(self, nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z, sources=None):
         self.taper = np.ascontiguousarray(taper, np.float64)
         self.stf = np.ascontiguousarray(stf, np.float64)
         self.rec_x = np.ascontiguousarray(rec_x, np.int32)
         self.rec_z = np.ascontiguousarray(rec_z, np.int32)
-        self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, _p(self.stf).value, int(src[0]), int(src[1]),
-                       len(self.rec_x), _p(self.rec_x).value, _p(self.rec_z).value)
+        if sources is None:
+            self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, _p(self.stf).value, int(src[0]), int(src[1]),
+                           len(self.rec_x), _p(self.rec_x).value, _p(self.rec_z).value, 0, None, None, None, None)
+        else:
+            srcs = np.asarray(sources, np.float64).reshape(-1, 5)
+            assert self.stf.shape == (len(srcs), nt)
+            self.msrc_x = np.ascontiguousarray(srcs[:, 0], np.int32)
+            self.msrc_z = np.ascontiguousarray(srcs[:, 1], np.int32)
+            self.moment = np.ascontiguousarray(srcs[:, 2:5], np.float64)
+            self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, None, 0, 0, len(self.rec_x),
+                           _p(self.rec_x).value, _p(self.rec_z).value, len(srcs), _p(self.msrc_x).value,
+                           _p(self.msrc_z).value, _p(self.moment).value, _p(self.stf).value)
         self.nt, self.nrec = nt, len(self.rec_x)
 
     def forward(self, rho, vp, vs):

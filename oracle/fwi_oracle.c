@@ -8,7 +8,8 @@
  * hmclab/Distributions/ElasticFullWaveform2D.py:150-184.  Its arithmetic is
  * restated from the published methods it names: Virieux (1986) velocity-stress
  * staggered grid, Levander (1988) fourth-order differences (9/8, -1/24),
- * Cerjan et al. (1985) sponge, explosive point sources with a Ricker wavelet,
+ * Cerjan et al. (1985) sponge, explosive or moment-tensor point sources (a
+ * stress glut) with Ricker wavelets,
  * an L2 waveform misfit and the gradient by the exact transpose (reverse mode)
  * of the discrete time stepping.  No reference numbers exist for this path
  * (the reference's FWI test is skipped without psvWave), so parity is pinned
@@ -26,7 +27,9 @@
  *   3. record vx, vz at the receivers
  *   4. sxx += dt ((l+2m) Dx- vx + l Dz- vz), szz += dt (l Dx- vx + (l+2m) Dz- vz),
  *      sxz += dt muxz (Dz+ vx + Dx+ vz)
- *   5. sxx, szz at the source += stf[n] * dt / h^2
+ *   5. sxx, szz at the source += stf[n] * dt / h^2 (an explosion); for a
+ *      moment tensor M: sxx += Mxx s, szz += Mzz s at the source node and
+ *      each of the four surrounding sxz nodes += Mxz s / 4, s = stf[n] dt / h^2
  *   6. sxx, szz, sxz *= taper
  * with Dx+ f[i] = (c1 (f[i+1] - f[i]) + c2 (f[i+2] - f[i-1])) / h and
  *      Dx- f[i] = (c1 (f[i] - f[i-1]) + c2 (f[i+1] - f[i-2])) / h, c1 = 9/8, c2 = -1/24.
@@ -47,6 +50,13 @@ typedef struct {
   int nrec;
   const int* rec_x;
   const int* rec_z;
+  /* nsrc > 0: the shot is fired by nsrc moment-tensor point sources instead
+   * of the explosive source above (src_x, src_z, stf unused) */
+  int nsrc;
+  const int* msrc_x;
+  const int* msrc_z;
+  const double* moment; /* [nsrc][3]: Mxx, Mzz, Mxz */
+  const double* mstf;   /* [nsrc][nt] wavelets */
 } fwi_shot;
 
 #define IDX(j, i) ((size_t)(j) * (size_t)nx + (size_t)(i))
@@ -123,9 +133,25 @@ int fwi_forward(const fwi_shot* s, const double* rho, const double* vp, const do
         szz[k] += dt * (lam[k] * exx + l2m[k] * ezz);
         sxz[k] += dt * muxz[k] * (dzp(vx, nx, j, i, h) + dxp(vz, nx, j, i, h));
       }
-    const size_t ks = IDX(s->src_z, s->src_x);
-    sxx[ks] += s->stf[n] * dt / (h * h);
-    szz[ks] += s->stf[n] * dt / (h * h);
+    if (s->nsrc > 0) {
+      /* stress glut of a moment tensor M at the sxx/szz node (i, j): Mxx and
+       * Mzz there, Mxz shared by the four sxz nodes (i -/+ 1/2, j -/+ 1/2) */
+      for (int q = 0; q < s->nsrc; ++q) {
+        const int i = s->msrc_x[q], j = s->msrc_z[q];
+        const double v = s->mstf[(size_t)q * s->nt + n] * dt / (h * h);
+        const double* M = s->moment + 3 * q;
+        sxx[IDX(j, i)] += M[0] * v;
+        szz[IDX(j, i)] += M[1] * v;
+        sxz[IDX(j - 1, i - 1)] += 0.25 * M[2] * v;
+        sxz[IDX(j - 1, i)] += 0.25 * M[2] * v;
+        sxz[IDX(j, i - 1)] += 0.25 * M[2] * v;
+        sxz[IDX(j, i)] += 0.25 * M[2] * v;
+      }
+    } else {
+      const size_t ks = IDX(s->src_z, s->src_x);
+      sxx[ks] += s->stf[n] * dt / (h * h);
+      szz[ks] += s->stf[n] * dt / (h * h);
+    }
     for (size_t k = 0; k < N; ++k) {
       sxx[k] *= s->taper[k];
       szz[k] *= s->taper[k];

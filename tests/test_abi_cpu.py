@@ -68,7 +68,8 @@ def test_invalid_arguments_fail_before_any_launch(lib):
 @pytest.mark.parametrize("cname, cls", [("hmc_chains", _lib.HmcChains), ("hmc_fwi", _lib.HmcFwi),
                                          ("hmc_mlp_out", _lib.HmcMlpOut), ("hmc_schedule", _lib.HmcSchedule),
                                          ("hmc_dense_group", _lib.HmcDenseGroup),
-                                         ("hmc_csr_slabs", _lib.HmcCsrSlabs)])
+                                         ("hmc_csr_slabs", _lib.HmcCsrSlabs),
+                                         ("hmc_fwi_source", _lib.HmcFwiSource)])
 def test_struct_layout_matches_c(tmp_path, cname, cls):
     """Compile a probe with gcc that prints sizeof/offsetof of the C struct
     and compare with the ctypes Structure."""
