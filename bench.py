@@ -404,9 +404,9 @@ class FwiWorkload:
     stepsize = 0.12  # prior-whitened units: the mass matrix is the prior precision
     noise_fraction = 10.0  # data noise std / RMS of the true records
     hidden = (512, 512)
-    # a step is one block of `block` surrogate-driven proposals of every
-    # chain; 20 steps = 2000 proposals, so that the ESS lag windows of the
-    # surrogate run (autocorrelation times near 200 proposals) truncate
+    # a step is one block of proposals of every chain: `block` surrogate-
+    # driven ones (20 steps = 2000 proposals), or, when the screen falls back
+    # to plain HMC, enough exact ones for 40 timed proposals in all
     default_steps, default_warmup = 20, 3
     block = 100
     burn_in = 12  # exact proposals recording (position, gradient) training pairs
@@ -879,6 +879,20 @@ def choose_trajectory(pilot, min_acceptance=0.25):
     return L_best, eps_best
 
 
+def esjd_min(q, std):
+    """Smallest per-parameter expected squared jump between consecutive
+    draws, in units of the posterior variance: min_i mean_(t,c)
+    (q[t+1,i,c] - q[t,i,c])^2 / std_i^2, for draws q [N][d][C] (device).
+    It measures how far the slowest direction moves per proposal, the same
+    way for both samplers; for chains that diffuse, ESS per draw is about
+    half of it."""
+    import torch
+
+    s = torch.as_tensor(np.asarray(std, np.float64), device=q.device)[:, None]
+    dq = (q[1:].double() - q[:-1].double()) / s
+    return float((dq * dq).mean(dim=(0, 2)).min())
+
+
 def run_fwi_arm(args, wl):
     import torch
 
@@ -896,26 +910,29 @@ def run_fwi_arm(args, wl):
     wl.build()
     post, lik = wl.posterior(), wl.pb["likelihood"]
     d, C, L = wl.d, wl.chains, wl.L
-    K, W, B, Kp, Nb = args.steps, args.warmup, args.block, args.plain_steps, args.burn_in
+    K, W, Nb = args.steps, args.warmup, args.burn_in
     ref, ref_why = load_fwi_reference(wl)
     # chains start at the reference run's final states (posterior draws): a
     # converged exact burn-in, which this bench cannot afford to repeat
     q_init = ref["q_final"] if ref is not None else wl.q0
+    post_std = ref["std"] if ref is not None else wl.pb["prior_std"]
     kw = wl.sampler_kwargs()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t_setup = time.perf_counter() - t_setup
 
     # ---- exact proposals from the start states, recording training pairs --
     R = args.refresh_interval if args.refresh_interval > 0 else None
-    extra = (W + K) * B // R * C if R else 0  # rows the refreshes of the surrogate run append
-    data = S.TrainingSet(d, Nb * L * C + extra, values=args.value_weight > 0)
+    B_s = args.block
+    extra = (W + K) * B_s // R * C if R else 0  # rows the refreshes of a surrogate run append
+    data = S.TrainingSet(d, Nb * L * C + extra + 4 * C, values=args.value_weight > 0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     burn = H.Samplers.HMC(seed=sharding.rank_seed(100, rank)).sample(None, post, initial_model=q_init, proposals=Nb,
-                                                                     training_set=data, **kw)
+                                                                     training_set=data, keep_samples=True, **kw)
     t_burn = time.perf_counter() - t0
     q_start = burn.current_model
     acc_burn = float(np.mean(burn.accepted_proposals) / Nb)
+    jump_plain = esjd_min(burn.samples_device[0], post_std)
 
     # ---- surrogate training on the device ---------------------------------
     kind = S.PotentialSurrogate if args.surrogate == "potential" else S.MLPSurrogate
@@ -932,8 +949,8 @@ def run_fwi_arm(args, wl):
     # ---- pilot (untimed): the surrogate run's trajectory ------------------
     # A few proposals per (L, stepsize) from the start states; the setting
     # with the largest acceptance x (trajectory length)^2 — the diffusive-
-    # regime gain per proposal, length capped at the plain run's — is used
-    # for the timed run.  --surrogate-L / --surrogate-stepsize fix it.
+    # regime gain per proposal, length capped at the plain run's — is used.
+    # --surrogate-L / --surrogate-stepsize fix it.
     pilot = []
     if args.surrogate_L is None or args.surrogate_stepsize is None:
         tau_max = args.pilot_max_length * wl.stepsize * wl.L
@@ -950,18 +967,60 @@ def run_fwi_arm(args, wl):
     else:
         L_best, eps_best = args.surrogate_L, args.surrogate_stepsize
     kw_s = dict(kw, amount_of_steps=L_best, stepsize=eps_best)
+    refresh_kw = dict(training_set=data, refresh_interval=R, refresh_steps=args.refresh_steps) if R else {}
 
-    # ---- surrogate-driven HMC: W untimed blocks, then K timed blocks -------
+    # ---- screen (untimed): surrogate against plain HMC ---------------------
+    # A short surrogate run (with its refreshes) measures its cost per
+    # proposal and how far its slowest direction moves (esjd_min); the exact
+    # burn-in gives plain HMC's.  Plain HMC is the fallback: with
+    # --sampler auto the timed run uses the surrogate only when its jump rate
+    # per second beats plain HMC's.  (A short run's ESS is no guide: its lag
+    # windows end long before the surrogate chains decorrelate.)
+    screen = H.Samplers.HMC(seed=sharding.rank_seed(170, rank))
+    n_screen = args.screen_proposals
+    screen.prepare(None, post, initial_model=q_start, proposals=n_screen, keep_samples=True, surrogate=net,
+                   **dict(refresh_kw, refresh_interval=min(R, n_screen // 2) if R else None), **kw_s)
+    ev_a, ev_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_a.record(screen.stream)
+    screen.run(n_screen)
+    ev_b.record(screen.stream)
+    screen.stream.synchronize()
+    t_screen = ev_a.elapsed_time(ev_b) / 1e3 / n_screen
+    screen.finish()
+    jump_sur = esjd_min(screen.samples_device[0], post_std)
+    acc_screen = float(np.mean(screen.accepted_proposals) / n_screen)
+    t_plain_burn = t_burn / Nb  # wall seconds per exact proposal (recording included)
+    rate_sur, rate_plain = jump_sur / t_screen, jump_plain / t_plain_burn
+    if args.sampler == "auto":
+        sampler = "surrogate" if rate_sur > rate_plain else "plain"
+    else:
+        sampler = args.sampler
+    choice = {"rule": "surrogate when its slowest-direction jump per second (esjd_min / s) beats plain HMC's",
+              "sampler": sampler, "forced": args.sampler != "auto",
+              "surrogate": {"proposals": n_screen, "ms_per_proposal": 1e3 * t_screen, "acceptance": acc_screen,
+                            "esjd_min": jump_sur, "esjd_min_per_s": rate_sur},
+              "plain": {"proposals": Nb, "ms_per_proposal": 1e3 * t_plain_burn, "acceptance": acc_burn,
+                        "esjd_min": jump_plain, "esjd_min_per_s": rate_plain,
+                        "note": "from the exact burn-in (wall time, pair recording included)"},
+              "estimated_speedup_of_surrogate": rate_sur / rate_plain if rate_plain > 0 else None}
+
+    # ---- the timed run: W untimed blocks, then K timed blocks --------------
     # The run goes through the public API from host arrays to host arrays:
     # `e2e` is its wall time from the upload of the start states (prepare) to
     # the samples back on the host; `value` uses the device time of the K
     # timed blocks (CUDA events on the sampler's stream).
-    refresh_kw = dict(training_set=data, refresh_interval=R, refresh_steps=args.refresh_steps) if R else {}
+    if sampler == "surrogate":
+        B = B_s
+        run_kw = dict(kw_s, surrogate=net, **refresh_kw)
+    else:
+        # at least 40 timed proposals: plain HMC's lag windows (autocorrelation
+        # time near 4 proposals) then truncate
+        B = args.plain_block if args.plain_block else max(2, -(-40 // K))
+        run_kw = dict(kw)
     torch.cuda.synchronize()
     t_e2e0 = time.perf_counter()
     smp_s = H.Samplers.HMC(seed=sharding.rank_seed(200, rank))
-    smp_s.prepare(None, post, initial_model=q_start, proposals=(W + K) * B, keep_samples=True, surrogate=net,
-                  **refresh_kw, **kw_s)
+    smp_s.prepare(None, post, initial_model=q_start, proposals=(W + K) * B, keep_samples=True, **run_kw)
     smp_s.run(W * B)
     smp_s.stream.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
@@ -993,8 +1052,7 @@ def run_fwi_arm(args, wl):
     # acceptance per block, read from the samples (a chain accepted when its position changed)
     moved = (qall[1:] != qall[:-1]).any(dim=1).double().mean(dim=1).cpu().numpy()
     acc_blocks = [round(float(moved[max(0, k * B - 1):(k + 1) * B - 1].mean()), 4) for k in range(W + K)]
-    # lag windows up to half the run: the surrogate chains decorrelate over
-    # hundreds of proposals
+    # lag windows up to half the run
     ess_s_raw = diagnostics.ess(qs, lags=min(N // 2, 1000))
     acc_s = float(np.mean(smp_s.accepted_proposals) / ((W + K) * B))
     # rank normalisation compares every pooled draw with every other (S^2 per
@@ -1012,28 +1070,37 @@ def run_fwi_arm(args, wl):
         reasons.insert(0, ref_why)
     value_measured = float(ess_s.min() / t_s)
     value = value_measured if not reasons else None
-
-    # ---- plain HMC (exact gradients): its cost per proposal, timed ---------
-    smp_p = H.Samplers.HMC(seed=sharding.rank_seed(300, rank))
-    smp_p.prepare(None, post, initial_model=q_start, proposals=Kp, keep_samples=False, **kw)
-    evp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kp)]
-    for k in range(Kp):
-        with torch.cuda.stream(smp_p.stream):
-            flush.fill_(float(k))
-            evp[k][0].record(smp_p.stream)
-        smp_p.run(1)
-        evp[k][1].record(smp_p.stream)
-    smp_p.stream.synchronize()
-    t_p = sum(a.elapsed_time(b) for a, b in evp) / 1e3
-    smp_p.finish()
-    acc_p = float(np.mean(smp_p.accepted_proposals) / Kp)
     e_plain = float(ref["ess_per_chain_proposal"]) if ref is not None else None
-    plain_value = e_plain * C * world * Kp / t_p if e_plain is not None else None
+    if sampler == "plain":
+        plain = {"value": value_measured, "source": "the timed run itself", "ms_per_proposal": 1e3 * t_s / (K * B),
+                 "acceptance": acc_s, "ess_per_chain_proposal": float(ess_s.min()) / (N * C * world)}
+    else:
+        # plain HMC's cost per proposal timed here; its ESS per chain-proposal
+        # from the reference run
+        Kp = args.plain_steps
+        smp_p = H.Samplers.HMC(seed=sharding.rank_seed(300, rank))
+        smp_p.prepare(None, post, initial_model=q_start, proposals=Kp, keep_samples=False, **kw)
+        evp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kp)]
+        for k in range(Kp):
+            with torch.cuda.stream(smp_p.stream):
+                flush.fill_(float(k))
+                evp[k][0].record(smp_p.stream)
+            smp_p.run(1)
+            evp[k][1].record(smp_p.stream)
+        smp_p.stream.synchronize()
+        t_p = sum(a.elapsed_time(b) for a, b in evp) / 1e3
+        smp_p.finish()
+        plain = {"value": e_plain * C * world * Kp / t_p if e_plain is not None else None,
+                 "source": f"{Kp} timed proposals x the reference run's ESS per chain-proposal",
+                 "ms_per_proposal": 1e3 * t_p / Kp, "acceptance": float(np.mean(smp_p.accepted_proposals) / Kp),
+                 "ess_per_chain_proposal": e_plain}
 
     # ---- end to end: the same run, wall clock, host arrays in and out ------
     refreshes_timed = getattr(smp_s, "refreshes", 0)
     ess_e = np.abs(diagnostics.ess(torch.from_numpy(host_q).to("cuda"), lags=min(host_q.shape[0] // 2, 1000)))
     e2e_measured = float(ess_e.min() / t_e2e)
+    step_text = (f"{B} surrogate-driven proposals of every chain" if sampler == "surrogate" else
+                 f"{B} plain HMC proposals of every chain (the fallback the screen chose)")
 
     hbm, bf16, bf16s, src = peaks()
     achieved = wl.stencil_bytes_per_step() / t_step / 1e9
@@ -1042,11 +1109,13 @@ def run_fwi_arm(args, wl):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded; records from the device forward of the true model + noise)",
-        "config": {**wl.config(), "step": f"{B} surrogate-driven proposals of every chain",
+        "config": {**wl.config(), "step": step_text, "sampler": sampler,
                    "start": "posterior draws: final states of the reference plain-HMC run"
                             if ref is not None else "m_true + 0.3 prior std (no reference run)"},
         "valid": not reasons, "invalid_reasons": reasons, "value_measured": value_measured,
-        "speedup_vs_plain": float(value_measured / plain_value) if plain_value else None,
+        "sampler": sampler, "sampler_choice": choice,
+        "speedup_vs_plain": (float(value_measured / plain["value"]) if sampler == "surrogate" and plain["value"]
+                             else 1.0 if sampler == "plain" else None),
         "including_burn_in_and_training": {
             "value": float(ess_s.min() / (t_burn + t_train + t_s)),
             "note": "min-ESS over (exact training-pair proposals + surrogate training + sampling) seconds"},
@@ -1054,17 +1123,19 @@ def run_fwi_arm(args, wl):
         "rank_normalised_bulk": ({"value": float(bulk_s.min() / t_s)} if bulk_s is not None else
                                  {"value": None, "note": "skipped: pooled rank normalisation of this many draws "
                                                          "exceeds the library's comparison limit"}),
-        "refresh": {"interval": R, "adam_steps": args.refresh_steps if R else 0, "refreshes": refreshes_timed,
+        "refresh": {"interval": R if sampler == "surrogate" else None,
+                    "adam_steps": args.refresh_steps if R and sampler == "surrogate" else 0,
+                    "refreshes": refreshes_timed,
                     "note": "after every block: exact gradient and misfit at the chains' current positions appended "
                             "to the training set, then more training; inside the timed region"},
         "acceptance": acc_s, "acceptance_per_block": acc_blocks,
         "surrogate_trajectory": {"leapfrog_steps": L_best, "stepsize": eps_best,
                                                       "pilot": [[L_, e_, round(a_, 4)] for _, L_, e_, a_ in pilot]},
-        "plain": {"value": plain_value, "proposals_timed": Kp, "ms_per_proposal": 1e3 * t_p / Kp,
-                  "acceptance": acc_p, "ess_per_chain_proposal": e_plain,
-                  "ess_source": "reference plain-HMC run (tests/golden/fwi_reference.npz): "
-                                f"{int(ref['proposals']) if ref is not None else 0} proposals x {C} chains, "
-                                "lag windows truncated"},
+        "plain": plain,
+        "reference_run": {"ess_per_chain_proposal": e_plain,
+                          "source": "reference plain-HMC run (tests/golden/fwi_reference.npz): "
+                                    f"{int(ref['proposals']) if ref is not None else 0} proposals x {C} chains, "
+                                    "lag windows truncated"},
         "moment_error_vs_reference": mc,
         "training_proposals": {"proposals": Nb, "seconds": t_burn, "acceptance": acc_burn, "pairs": data.count},
         "surrogate": {"kind": args.surrogate, "train_steps": args.train_steps, "train_seconds": t_train,
@@ -1076,7 +1147,8 @@ def run_fwi_arm(args, wl):
                       "best_step": fit["best_step"]},
         "setup_seconds": t_setup,
         "e2e": {"value": e2e_measured if not reasons else None, "value_measured": e2e_measured, "unit": UNIT,
-                "h2d_bytes_per_step": int(q_start.size * 8 / (W + K)), "d2h_bytes_per_step": int(B * (d * C * 4 + C * 8)),
+                "h2d_bytes_per_step": int(q_start.size * 8 / (W + K)),
+                "d2h_bytes_per_step": int(B * (d * C * 4 + C * 8)),
                 "seconds": t_e2e, "note": "wall time of the timed run itself through the public API (prepare from "
                                           "host start states, W + K blocks, samples back to the host); ESS over "
                                           "all its draws"},
@@ -1248,8 +1320,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
-    ap.add_argument("--plain-steps", type=int, default=3, help="fwi: timed proposals of plain HMC (its cost)")
+    ap.add_argument("--sampler", default="auto", choices=["auto", "surrogate", "plain"],
+                    help="fwi: sampler of the timed run; auto: the surrogate when the screen finds its jump rate above "
+                         "plain HMC's, else plain HMC (the fallback)")
+    ap.add_argument("--screen-proposals", type=int, default=64,
+                    help="fwi: surrogate proposals of the untimed screen against plain HMC")
+    ap.add_argument("--plain-steps", type=int, default=3,
+                    help="fwi: timed plain proposals giving plain HMC's cost when the surrogate runs")
     ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
+    ap.add_argument("--plain-block", type=int, default=None,
+                    help="fwi: plain proposals per step when plain HMC runs (default: at least 40 timed proposals)")
     ap.add_argument("--value-weight", type=float, default=1.0,
                     help="fwi: weight of the misfit-value matching loss of the potential surrogate (0: gradients only)")
     ap.add_argument("--refresh-interval", type=int, default=32,
