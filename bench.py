@@ -410,14 +410,18 @@ class FwiWorkload:
     default_steps, default_warmup = 20, 3
     block = 100
     burn_in = 12  # exact proposals recording (position, gradient) training pairs
+    # gradient correlation at every k-th time step (psvWave's snapshot_interval)
+    snapshot_interval = 1
 
-    def __init__(self, seed=0, chains=None):
+    def __init__(self, seed=0, chains=None, snapshot_interval=None):
         from hmclab_gb300 import fwi as F
 
         if chains is not None:
             self.chains = chains
+        if snapshot_interval is not None:
+            self.snapshot_interval = int(snapshot_interval)
         self.seed = seed
-        self.cfg = F.ElasticConfig()
+        self.cfg = F.ElasticConfig(snapshot_interval=self.snapshot_interval)
         self.cells = self.cfg.nxc * self.cfg.nzc
         self.built = False
 
@@ -464,6 +468,7 @@ class FwiWorkload:
                 "surrogate": ("scalar potential w3 . GELU(W2 GELU(W1 x + b1) + b2) + quadratic, 600-512-512-1, its "
                               "gradient drives the leapfrog; BF16 weights, FP32 accumulate"),
                 "precision": "FP32 state and stencils, FP64 dH", "l2": "flushed between timed steps (256 MiB write)",
+                "snapshot_interval": self.snapshot_interval,
                 "start": "end states of the exact burn-in"}
 
 
@@ -1210,14 +1215,14 @@ def run_fwi_arm(args, wl):
 PROFILE_CASES = ("fwi-gradient", "fwi-misfit", "mlp", "potential", "persistent", "tomo", "srcloc")
 
 
-def _profile_fwi(nt, chains):
+def _profile_fwi(nt, chains, snapshot_interval=1):
     import numpy as np
     import torch
 
     from hmclab_gb300 import fwi as F
     from hmclab_gb300 import problems
 
-    cfg = F.ElasticConfig(nt=nt)
+    cfg = F.ElasticConfig(nt=nt, snapshot_interval=snapshot_interval)
     pb = problems.elastic_fwi(cfg, 20, 10, prior_fraction=0.1, noise_fraction=10.0, seed=0)
     rng = np.random.default_rng(1)
     q = pb["m_true"][:, None] + 0.3 * pb["prior_std"][:, None] * rng.normal(size=(pb["m_true"].size, chains))
@@ -1234,7 +1239,7 @@ def run_profile_case(a):
                             else 8192 if a.profile_case == "srcloc" else 64)
     a.case = a.profile_case
     if a.case.startswith("fwi"):
-        post, q = _profile_fwi(a.nt, a.chains)
+        post, q = _profile_fwi(a.nt, a.chains, a.snapshot_interval or 1)
         out = torch.empty_like(q)
         x = torch.empty(a.chains, dtype=torch.float64, device="cuda")
         t0 = time.perf_counter()
@@ -1338,6 +1343,9 @@ def main():
     ap.add_argument("--refresh-steps", type=int, default=300, help="fwi: Adam steps per refresh")
     ap.add_argument("--pilot-max-length", type=float, default=2.0,
                     help="fwi: longest surrogate trajectory the pilot tries, in units of plain HMC's")
+    ap.add_argument("--snapshot-interval", type=int, default=None,
+                    help="fwi and the FWI profiling cases: the gradient correlates forward and adjoint fields at every "
+                         "k-th time step (psvWave's snapshot_interval; 1: every step, the exact discrete gradient)")
     ap.add_argument("--burn-in", type=int, default=None,
                     help="fwi: exact proposals recording the surrogate's training pairs (independent of --warmup)")
     ap.add_argument("--train-steps", type=int, default=10000, help="fwi: Adam steps of the surrogate")
@@ -1359,7 +1367,8 @@ def main():
     if args.profile_case:
         run_profile_case(args)
         return
-    wl = WORKLOADS[args.workload]()
+    wl = (WORKLOADS[args.workload](snapshot_interval=args.snapshot_interval) if args.workload == "fwi"
+          else WORKLOADS[args.workload]())
     args.steps = wl.default_steps if args.steps is None else args.steps
     args.warmup = wl.default_warmup if args.warmup is None else args.warmup
     if args.workload == "fwi":

@@ -735,7 +735,13 @@ class ElasticFullWaveform2D(_AbstractDistribution):
     gradient is the exact derivative of the discrete misfit (chain rule
     through the parametrisation); `gradient_projection="least_squares"`
     applies the reference's (C^T C)^-1 C^T map to blob gradients instead
-    (ElasticFullWaveform2D.py:159, 329-330)."""
+    (ElasticFullWaveform2D.py:159, 329-330).  With the configuration's
+    `snapshot_interval` k > 1 (psvWave's; set before the first evaluation)
+    the forward pass keeps the wavefield of every k-th step only and the
+    gradient correlates at those steps, weighted by k: a k-times smaller
+    store and cheaper adjoint steps, and a gradient that is exact up to the
+    aliasing of the correlation's spectrum above 1 / (2 k dt) (the misfit
+    stays exact, so HMC still targets the exact posterior)."""
 
     temperature: float = 1.0
     # the stencils run in FP32 only; single-vector calls use one FP32 chain
@@ -879,7 +885,9 @@ class ElasticFullWaveform2D(_AbstractDistribution):
             for name in ("avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz", "g_l2m", "g_lam", "g_muxz", "g_vp",
                          "g_vs", "g_rho", "t1", "t2", "t3", "t4", "t5"):
                 ws[name] = z(cells, C)
-            ws["store"] = z(cfg.nt * 2 * cells * C)
+            k = max(int(cfg.snapshot_interval), 1)
+            planes = 2 * cfg.nt if k == 1 else 4 * (-(-cfg.nt // k))
+            ws["store"] = z(planes * cells * C)
             ws["resid"] = z(cfg.nt * cfg.n_rec * 2 * C)
             if self.use_blob_par:
                 ws["gtmp"] = z(self.blob.n_blobs, C)
@@ -893,6 +901,7 @@ class ElasticFullWaveform2D(_AbstractDistribution):
         d = L.HmcFwi()
         d.nx, d.nz, d.nt, d.nrec, d.chains = cfg.nxc, cfg.nzc, cfg.nt, cfg.n_rec, C
         d.h, d.dt, d.w = cfg.h, cfg.dt, self.weight
+        d.snapshot_interval = max(int(cfg.snapshot_interval), 1)
         d.taper, d.rec_map, d.obs = p["taper"].data_ptr(), p["rec_map"].data_ptr(), p["obs"].data_ptr()
         d.stf_host = p["stf_host"].ctypes.data
         for name in ("rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx", "szz", "sxz", "rec",

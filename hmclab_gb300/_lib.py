@@ -105,7 +105,8 @@ class HmcFwi(_ct.Structure):
     ] + [(n, c_void_p) for n in (
         "taper", "stf_host", "rec_map", "rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz", "sxx",
         "szz", "sxz", "store", "rec", "obs", "resid", "avx", "avz", "asxx", "aszz", "asxz", "g_bx", "g_bz",
-        "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial", "status")]
+        "g_l2m", "g_lam", "g_muxz", "t1", "t2", "t3", "t4", "t5", "partial", "status")] + [
+        ("snapshot_interval", c_int32)]
 
 
 class HmcFwiSource(_ct.Structure):

@@ -154,13 +154,17 @@ struct Params {
 
 __global__ void __launch_bounds__(TX* TY* TZ) velocity_kernel(Grid g, Fields f, Params p, const float* __restrict__ taper,
                                                             const int32_t* __restrict__ rec_map, float* rec_n,
-                                                            float* store_n) {
+                                                            float* store_n, float* store_p) {
   step_dependency_wait();
   step_dependents_go();
   const Cell e = cell_of(g);
   if (!e.in) return;
   const int k = e.k, sx = g.C, sz = g.nx * g.C;
   float vx = f.vx[k], vz = f.vz[k];
+  if (store_p) {  // a snapshot keeps the velocities of the step before too
+    store_p[k] = vx;
+    store_p[g.nx * g.nz * g.C + k] = vz;
+  }
   if (g.valid(e.i, e.j)) {
     vx += g.dt * p.bx[k] * (dxp(f.sxx, k, sx, g.inv_h) + dxm(f.sxz, k, sz, g.inv_h));
     vz += g.dt * p.bz[k] * (dxm(f.sxz, k, sx, g.inv_h) + dxp(f.szz, k, sz, g.inv_h));
@@ -299,7 +303,7 @@ inline dim3 tile_grid(int nx, int nz, int64_t C, int rows = TT_Z) {
 __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
     const __grid_constant__ CUtensorMap m_sxx, const __grid_constant__ CUtensorMap m_sxz,
     const __grid_constant__ CUtensorMap m_szz, Grid g, Fields f, Params p, const float* __restrict__ taper,
-    const int32_t* __restrict__ rec_map, float* rec_n, float* store_n, int* status) {
+    const int32_t* __restrict__ rec_map, float* rec_n, float* store_n, float* store_p, int* status) {
   __shared__ __align__(128) float t_sxx[TT_Z][TT_X + 3][32];      // rows j0.., cells i0-1..
   __shared__ __align__(128) float t_sxz[TT_Z + 3][TT_X + 3][32];  // rows j0-2.., cells i0-2..
   __shared__ __align__(128) float t_szz[TT_Z + 3][TT_X][32];      // rows j0-1.., cells i0..
@@ -349,6 +353,10 @@ __global__ void __launch_bounds__(32 * TT_X) velocity_tma_kernel(
     if (j >= g.nz) break;
     const int k = g.at(j, i) + c;
     float vx = r_vx[zz], vz = r_vz[zz];
+    if (store_p) {  // a snapshot keeps the velocities of the step before too
+      store_p[k] = vx;
+      store_p[g.nx * g.nz * g.C + k] = vz;
+    }
     if (xin && j >= 2 && j < g.nz - 2) {
       const float dsxx = HMC_DP(t_sxx[zz][tx + 2][l], t_sxx[zz][tx + 1][l], t_sxx[zz][tx + 3][l], t_sxx[zz][tx][l]);
       const float dsxz_z =
@@ -462,12 +470,16 @@ struct Temps {
 // Adjoint velocity pass of step n: reverse of stress step 4 (adjoint
 // velocities and stiffness gradients), receivers 3, taper 2, and the
 // buoyancy gradients of velocity step 1; writes t4, t5 for the stress pass.
+// CORR: the step correlates the forward and adjoint fields into the gradient
+// accumulators, each contribution weighted by w (the snapshot interval; 1
+// at every step); without it the pass only propagates the adjoint fields.
+template <bool CORR>
 __global__ void __launch_bounds__(TX* TY* TZ) adj_velocity_kernel(Grid g, Fields a, Params p, Grads gr, Temps tm,
                                                                 const float* __restrict__ taper,
                                                                 const int32_t* __restrict__ rec_map,
                                                                 const float* __restrict__ resid_n,
                                                                 const float* __restrict__ vn,
-                                                                const float* __restrict__ vprev) {
+                                                                const float* __restrict__ vprev, float w) {
   step_dependency_wait();
   step_dependents_go();
   const Cell e = cell_of(g);
@@ -477,36 +489,39 @@ __global__ void __launch_bounds__(TX* TY* TZ) adj_velocity_kernel(Grid g, Fields
   const int cell = e.j * g.nx + e.i;
   // every load first: the stores below may alias them as far as the
   // compiler knows, and would otherwise hold later loads back
-  const float* vxn = vn;
-  const float* vzn = vn + plane;
   const float avx = a.vx[k], avz = a.vz[k];
-  const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
-  const float g_l2m = gr.l2m[k], g_lam = gr.lam[k], g_mu = gr.muxz[k], g_bx = gr.bx[k], g_bz = gr.bz[k];
   const float bx = p.bx[k], bz = p.bz[k];
   const float tp = taper[cell];
   const int r = rec_map[cell];
-  const float vxk = vxn[k], vzk = vzn[k];
-  const float vxp = vprev ? vprev[k] : 0.f, vzp = vprev ? vprev[plane + k] : 0.f;
   // (Dx+)^T = -Dx-, etc.: -Dx+ t1 - Dz- t3 and -Dz+ t2 - Dx- t3
   float ax = avx - dxp(tm.t1, k, sx, ih) - dxm(tm.t3, k, sz, ih);
   float az = avz - dxp(tm.t2, k, sz, ih) - dxm(tm.t3, k, sx, ih);
-  const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
-  const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
   if (r >= 0) {
     ax += resid_n[(r * 2 + 0) * g.C + e.c];
     az += resid_n[(r * 2 + 1) * g.C + e.c];
   }
   ax *= tp;
   az *= tp;
-  gr.l2m[k] = g_l2m + g.dt * (exx * asxx + ezz * aszz);
-  gr.lam[k] = g_lam + g.dt * (ezz * asxx + exx * aszz);
-  gr.muxz[k] = g_mu + g.dt * exz * asxz;
+  if constexpr (CORR) {
+    const float* vxn = vn;
+    const float* vzn = vn + plane;
+    const float asxx = a.sxx[k], aszz = a.szz[k], asxz = a.sxz[k];
+    const float g_l2m = gr.l2m[k], g_lam = gr.lam[k], g_mu = gr.muxz[k], g_bx = gr.bx[k], g_bz = gr.bz[k];
+    const float vxk = vxn[k], vzk = vzn[k];
+    const float vxp = vprev ? vprev[k] : 0.f, vzp = vprev ? vprev[plane + k] : 0.f;
+    const float exx = dxm(vxn, k, sx, ih), ezz = dxm(vzn, k, sz, ih);
+    const float exz = dxp(vxn, k, sz, ih) + dxp(vzn, k, sx, ih);
+    const float wdt = w * g.dt;
+    gr.l2m[k] = g_l2m + wdt * (exx * asxx + ezz * aszz);
+    gr.lam[k] = g_lam + wdt * (ezz * asxx + exx * aszz);
+    gr.muxz[k] = g_mu + wdt * exz * asxz;
+    const float dvx = (vxk / tp - vxp) * w;
+    const float dvz = (vzk / tp - vzp) * w;
+    gr.bx[k] = g_bx + dvx / bx * ax;
+    gr.bz[k] = g_bz + dvz / bz * az;
+  }
   a.vx[k] = ax;
   a.vz[k] = az;
-  const float dvx = vxk / tp - vxp;
-  const float dvz = vzk / tp - vzp;
-  gr.bx[k] = g_bx + dvx / bx * ax;
-  gr.bz[k] = g_bz + dvz / bz * az;
   tm.t4[k] = g.dt * bx * ax;
   tm.t5[k] = g.dt * bz * az;
 }
@@ -555,30 +570,35 @@ __global__ void __launch_bounds__(TX* TY* TZ) adj_stress_kernel(Grid g, Fields a
 constexpr int AR_V = HMC_FWI_ADJ_ROWS_V, AR_S = HMC_FWI_ADJ_ROWS_S;
 #define HMC_DP(a, b, c, d) ((C1 * ((a) - (b)) + C2 * ((c) - (d))) * g.inv_h)
 
-template <int R>
+template <int R, bool CORR>
 __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
     const __grid_constant__ CUtensorMap m_t1, const __grid_constant__ CUtensorMap m_t2,
     const __grid_constant__ CUtensorMap m_t3, const __grid_constant__ CUtensorMap m_store, int row_vx, int row_vz,
     Grid g, Fields a, Params p, Grads gr, Temps tm, const float* __restrict__ taper,
-    const int32_t* __restrict__ rec_map, const float* __restrict__ resid_n, const float* __restrict__ vprev,
+    const int32_t* __restrict__ rec_map, const float* __restrict__ resid_n, const float* __restrict__ vprev, float w,
     int* status) {
+  // the stored forward velocities are staged only when the step correlates
+  constexpr int SR = CORR ? R + 3 : 1;
   __shared__ __align__(128) float t_t1[R][TT_X + 3][32];      // rows j0.., cells i0-1..
   __shared__ __align__(128) float t_t3[R + 3][TT_X + 3][32];  // rows j0-2.., cells i0-2..
   __shared__ __align__(128) float t_t2[R + 3][TT_X][32];      // rows j0-1.., cells i0..
-  __shared__ __align__(128) float t_vx[R + 3][TT_X + 3][32];  // rows j0-1.., cells i0-2..
-  __shared__ __align__(128) float t_vz[R + 3][TT_X + 3][32];  // rows j0-2.., cells i0-1..
+  __shared__ __align__(128) float t_vx[SR][TT_X + 3][32];     // rows j0-1.., cells i0-2..
+  __shared__ __align__(128) float t_vz[SR][TT_X + 3][32];     // rows j0-2.., cells i0-1..
   __shared__ __align__(8) uint64_t bar;
   step_dependency_wait();
   step_dependents_go();
   const TileOrigin o = tile_of(g, R);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    if (tile_barrier_arm(&bar, (uint32_t)(sizeof(t_t1) + sizeof(t_t3) + sizeof(t_t2) + sizeof(t_vx) + sizeof(t_vz)),
-                         g)) {
+    const uint32_t bytes =
+        (uint32_t)(sizeof(t_t1) + sizeof(t_t3) + sizeof(t_t2) + (CORR ? sizeof(t_vx) + sizeof(t_vz) : 0));
+    if (tile_barrier_arm(&bar, bytes, g)) {
       tile_load_3d(t_t1, &m_t1, &bar, o.c0, o.i0 - 1, o.j0);
       tile_load_3d(t_t3, &m_t3, &bar, o.c0, o.i0 - 2, o.j0 - 2);
       tile_load_3d(t_t2, &m_t2, &bar, o.c0, o.i0, o.j0 - 1);
-      tile_load_3d(t_vx, &m_store, &bar, o.c0, o.i0 - 2, row_vx + o.j0 - 1);
-      tile_load_3d(t_vz, &m_store, &bar, o.c0, o.i0 - 1, row_vz + o.j0 - 2);
+      if constexpr (CORR) {
+        tile_load_3d(t_vx, &m_store, &bar, o.c0, o.i0 - 2, row_vx + o.j0 - 1);
+        tile_load_3d(t_vz, &m_store, &bar, o.c0, o.i0 - 1, row_vz + o.j0 - 2);
+      }
     }
   }
   const int c = o.c0 + o.lane, i = o.i0 + o.tx, tx = o.tx, l = o.lane;
@@ -594,20 +614,22 @@ __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
       const int k = g.at(j, i) + c, cell = j * g.nx + i;
       r_avx[zz] = a.vx[k];
       r_avz[zz] = a.vz[k];
-      r_sxx[zz] = a.sxx[k];
-      r_szz[zz] = a.szz[k];
-      r_sxz[zz] = a.sxz[k];
-      r_gl2m[zz] = gr.l2m[k];
-      r_glam[zz] = gr.lam[k];
-      r_gmu[zz] = gr.muxz[k];
-      r_gbx[zz] = gr.bx[k];
-      r_gbz[zz] = gr.bz[k];
       r_bx[zz] = p.bx[k];
       r_bz[zz] = p.bz[k];
       r_tp[zz] = taper[cell];
       r_rec[zz] = rec_map[cell];
-      r_vxp[zz] = vprev ? vprev[k] : 0.f;
-      r_vzp[zz] = vprev ? vprev[plane + k] : 0.f;
+      if constexpr (CORR) {
+        r_sxx[zz] = a.sxx[k];
+        r_szz[zz] = a.szz[k];
+        r_sxz[zz] = a.sxz[k];
+        r_gl2m[zz] = gr.l2m[k];
+        r_glam[zz] = gr.lam[k];
+        r_gmu[zz] = gr.muxz[k];
+        r_gbx[zz] = gr.bx[k];
+        r_gbz[zz] = gr.bz[k];
+        r_vxp[zz] = vprev ? vprev[k] : 0.f;
+        r_vzp[zz] = vprev ? vprev[plane + k] : 0.f;
+      }
     }
   }
   __syncthreads();
@@ -628,14 +650,6 @@ __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
     float az = r_avz[zz] -
                HMC_DP(t_t2[zz + 2][tx][l], t_t2[zz + 1][tx][l], t_t2[zz + 3][tx][l], t_t2[zz][tx][l]) -
                HMC_DP(t_t3[zz + 2][tx + 2][l], t_t3[zz + 2][tx + 1][l], t_t3[zz + 2][tx + 3][l], t_t3[zz + 2][tx][l]);
-    const float exx = HMC_DP(t_vx[zz + 1][tx + 2][l], t_vx[zz + 1][tx + 1][l], t_vx[zz + 1][tx + 3][l],
-                             t_vx[zz + 1][tx][l]);
-    const float ezz = HMC_DP(t_vz[zz + 2][tx + 1][l], t_vz[zz + 1][tx + 1][l], t_vz[zz + 3][tx + 1][l],
-                             t_vz[zz][tx + 1][l]);
-    const float exz = HMC_DP(t_vx[zz + 2][tx + 2][l], t_vx[zz + 1][tx + 2][l], t_vx[zz + 3][tx + 2][l],
-                             t_vx[zz][tx + 2][l]) +
-                      HMC_DP(t_vz[zz + 2][tx + 2][l], t_vz[zz + 2][tx + 1][l], t_vz[zz + 2][tx + 3][l],
-                             t_vz[zz + 2][tx][l]);
     const int r = r_rec[zz];
     if (r >= 0) {
       ax += resid_n[(r * 2 + 0) * g.C + c];
@@ -644,17 +658,28 @@ __global__ void __launch_bounds__(32 * TT_X) adj_velocity_tma_kernel(
     const float tp = r_tp[zz];
     ax *= tp;
     az *= tp;
-    const float asxx = r_sxx[zz], aszz = r_szz[zz], asxz = r_sxz[zz];
-    gr.l2m[k] = r_gl2m[zz] + g.dt * (exx * asxx + ezz * aszz);
-    gr.lam[k] = r_glam[zz] + g.dt * (ezz * asxx + exx * aszz);
-    gr.muxz[k] = r_gmu[zz] + g.dt * exz * asxz;
+    const float bx = r_bx[zz], bz = r_bz[zz];
+    if constexpr (CORR) {
+      const float exx = HMC_DP(t_vx[zz + 1][tx + 2][l], t_vx[zz + 1][tx + 1][l], t_vx[zz + 1][tx + 3][l],
+                               t_vx[zz + 1][tx][l]);
+      const float ezz = HMC_DP(t_vz[zz + 2][tx + 1][l], t_vz[zz + 1][tx + 1][l], t_vz[zz + 3][tx + 1][l],
+                               t_vz[zz][tx + 1][l]);
+      const float exz = HMC_DP(t_vx[zz + 2][tx + 2][l], t_vx[zz + 1][tx + 2][l], t_vx[zz + 3][tx + 2][l],
+                               t_vx[zz][tx + 2][l]) +
+                        HMC_DP(t_vz[zz + 2][tx + 2][l], t_vz[zz + 2][tx + 1][l], t_vz[zz + 2][tx + 3][l],
+                               t_vz[zz + 2][tx][l]);
+      const float asxx = r_sxx[zz], aszz = r_szz[zz], asxz = r_sxz[zz];
+      const float wdt = w * g.dt;
+      gr.l2m[k] = r_gl2m[zz] + wdt * (exx * asxx + ezz * aszz);
+      gr.lam[k] = r_glam[zz] + wdt * (ezz * asxx + exx * aszz);
+      gr.muxz[k] = r_gmu[zz] + wdt * exz * asxz;
+      const float dvx = (t_vx[zz + 1][tx + 2][l] / tp - r_vxp[zz]) * w;
+      const float dvz = (t_vz[zz + 2][tx + 1][l] / tp - r_vzp[zz]) * w;
+      gr.bx[k] = r_gbx[zz] + dvx / bx * ax;
+      gr.bz[k] = r_gbz[zz] + dvz / bz * az;
+    }
     a.vx[k] = ax;
     a.vz[k] = az;
-    const float dvx = t_vx[zz + 1][tx + 2][l] / tp - r_vxp[zz];
-    const float dvz = t_vz[zz + 2][tx + 1][l] / tp - r_vzp[zz];
-    const float bx = r_bx[zz], bz = r_bz[zz];
-    gr.bx[k] = r_gbx[zz] + dvx / bx * ax;
-    gr.bz[k] = r_gbz[zz] + dvz / bz * az;
     tm.t4[k] = g.dt * bx * ax;
     tm.t5[k] = g.dt * bz * az;
   }
@@ -892,6 +917,29 @@ static Grid grid_of(const hmc_fwi* s) {
   return g;
 }
 
+// Where the forward pass stores step n's velocities for the adjoint: every
+// step ([nt][2] planes) at snapshot interval 1; else only at the snapshot
+// steps n = 0, k, 2k, ..., which keep the velocities after step n - 1 too
+// ([ceil(nt / k)][4] planes).
+struct StoreSlot {
+  float* now;   // vx, vz after step n (nullptr: not stored)
+  float* prev;  // vx, vz after step n - 1 (nullptr: the plane before `now`)
+  int64_t row;  // first row of `now` in the [planes x nz] view of the store
+};
+static int snapshot_interval(const hmc_fwi* s) { return s->snapshot_interval > 1 ? s->snapshot_interval : 1; }
+static int64_t stored_planes(const hmc_fwi* s) {
+  const int k = snapshot_interval(s);
+  return k == 1 ? 2ll * s->nt : 4ll * ((s->nt + k - 1) / k);
+}
+static StoreSlot store_slot(const hmc_fwi* s, int n) {
+  const int64_t cells = (int64_t)s->nx * s->nz * s->chains;
+  const int k = snapshot_interval(s);
+  if (k == 1) return {s->store + (int64_t)n * 2 * cells, nullptr, 2ll * n * s->nz};
+  if (n % k != 0) return {nullptr, nullptr, 0};
+  float* base = s->store + (int64_t)(n / k) * 4 * cells;
+  return {base, base + 2 * cells, 4ll * (n / k) * s->nz};
+}
+
 extern "C" {
 
 HMC_API int hmc_fwi_prepare(const hmc_fwi* s, void* stream) {
@@ -981,9 +1029,9 @@ HMC_API int hmc_fwi_forward_shot_sources(const hmc_fwi* s, int shot, const hmc_f
     const dim3 tgrid = tile_grid(s->nx, s->nz, s->chains), tblock(32, TT_X);
     for (int n = 0; n < s->nt; ++n) {
       float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
-      float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
+      const StoreSlot slot = store ? store_slot(s, n) : StoreSlot{nullptr, nullptr, 0};
       cudaError_t e = launch_step(n > 0, velocity_tma_kernel, tgrid, tblock, st, m_sxx, m_sxz, m_szz, g, f, p,
-                                  s->taper, s->rec_map, rec_n, store_n, s->status);
+                                  s->taper, s->rec_map, rec_n, slot.now, slot.prev, s->status);
       if (e != cudaSuccess) return cuda_fail(e, "launch velocity_tma_kernel");
       HMC_TRY(check_launch("velocity_tma_kernel"));
       e = launch_step(true, stress_tma_kernel, tgrid, tblock, st, m_vx, m_vz, g, f, p, s->taper, source_step(n),
@@ -995,10 +1043,10 @@ HMC_API int hmc_fwi_forward_shot_sources(const hmc_fwi* s, int shot, const hmc_f
   }
   for (int n = 0; n < s->nt; ++n) {
     float* rec_n = rec_shot + (int64_t)n * s->nrec * 2 * s->chains;
-    float* store_n = store ? s->store + (int64_t)n * 2 * cells : nullptr;
+    const StoreSlot slot = store ? store_slot(s, n) : StoreSlot{nullptr, nullptr, 0};
     // the first launch follows the memsets: ordinary stream order
     cudaError_t e = launch_step(n > 0, velocity_kernel, grid, block, st, g, f, p, s->taper, s->rec_map, rec_n,
-                                store_n);
+                                slot.now, slot.prev);
     if (e != cudaSuccess) return cuda_fail(e, "launch velocity_kernel");
     HMC_TRY(check_launch("velocity_kernel"));
     e = launch_step(true, stress_kernel, grid, block, st, g, f, p, s->taper, source_step(n));
@@ -1045,24 +1093,37 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   Grads gr{s->g_bx, s->g_bz, s->g_l2m, s->g_lam, s->g_muxz};
   Temps tm{s->t1, s->t2, s->t3, s->t4, s->t5};
   // staged tiles, as in the forward pass (C a multiple of 32, a status word)
+  const int k = snapshot_interval(s);
+  const float w = (float)k;  // weight of a correlating step
+  // the velocities after step n - 1 (nullptr before the first step)
+  auto prev_of = [&](int n, const StoreSlot& slot) -> const float* {
+    if (slot.prev) return slot.prev;
+    return n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
+  };
   if (s->chains % 32 == 0 && s->status) {
-    HMC_REQUIRE((int64_t)s->nt * 2 * s->nz < INT32_MAX, "hmc_fwi_adjoint_shot: too many stored rows");
+    HMC_REQUIRE(stored_planes(s) * s->nz < INT32_MAX, "hmc_fwi_adjoint_shot: too many stored rows");
     CUtensorMap m_t1, m_t2, m_t3, m_t4, m_t5, m_store;
     HMC_TRY(field_map(&m_t1, s->t1, s->nx, s->nz, s->chains, TT_X + 3, AR_V));
     HMC_TRY(field_map(&m_t2, s->t2, s->nx, s->nz, s->chains, TT_X, AR_V + 3));
     HMC_TRY(field_map(&m_t3, s->t3, s->nx, s->nz, s->chains, TT_X + 3, AR_V + 3));
-    HMC_TRY(field_map(&m_store, s->store, s->nx, s->nt * 2 * s->nz, s->chains, TT_X + 3, AR_V + 3));
+    HMC_TRY(field_map(&m_store, s->store, s->nx, (int)(stored_planes(s) * s->nz), s->chains, TT_X + 3, AR_V + 3));
     HMC_TRY(field_map(&m_t4, s->t4, s->nx, s->nz, s->chains, TT_X + 3, AR_S + 3));
     HMC_TRY(field_map(&m_t5, s->t5, s->nx, s->nz, s->chains, TT_X + 3, AR_S + 3));
     const dim3 gv = tile_grid(s->nx, s->nz, s->chains, AR_V), gs = tile_grid(s->nx, s->nz, s->chains, AR_S);
     const dim3 tblock(32, TT_X);
     for (int n = s->nt - 1; n >= 0; --n) {
-      const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
+      const StoreSlot slot = store_slot(s, n);
+      const float* resid_n = s->resid + (int64_t)n * s->nrec * 2 * s->chains;
       // the first launch follows the residual kernel and memsets: ordinary stream order
-      cudaError_t e = launch_step(n < s->nt - 1, adj_velocity_tma_kernel<AR_V>, gv, tblock, st, m_t1, m_t2, m_t3,
-                                  m_store, 2 * n * s->nz, (2 * n + 1) * s->nz, g, a, p, gr, tm, s->taper,
-                                  s->rec_map, (const float*)(s->resid + (int64_t)n * s->nrec * 2 * s->chains), vp,
-                                  s->status);
+      cudaError_t e;
+      if (slot.now)
+        e = launch_step(n < s->nt - 1, adj_velocity_tma_kernel<AR_V, true>, gv, tblock, st, m_t1, m_t2, m_t3,
+                        m_store, (int)slot.row, (int)(slot.row + s->nz), g, a, p, gr, tm, s->taper, s->rec_map,
+                        resid_n, prev_of(n, slot), w, s->status);
+      else
+        e = launch_step(n < s->nt - 1, adj_velocity_tma_kernel<AR_V, false>, gv, tblock, st, m_t1, m_t2, m_t3,
+                        m_store, 0, 0, g, a, p, gr, tm, s->taper, s->rec_map, resid_n, (const float*)nullptr, w,
+                        s->status);
       if (e != cudaSuccess) return cuda_fail(e, "launch adj_velocity_tma_kernel");
       HMC_TRY(check_launch("adj_velocity_tma_kernel"));
       e = launch_step(true, adj_stress_tma_kernel<AR_S>, gs, tblock, st, m_t4, m_t5, g, a, p, tm, s->taper,
@@ -1074,11 +1135,16 @@ HMC_API int hmc_fwi_adjoint_shot(const hmc_fwi* s, int shot, void* stream) {
   }
   const dim3 grid = cell_grid(s->nx, s->nz, s->chains), block = cell_block();
   for (int n = s->nt - 1; n >= 0; --n) {
-    const float* vn = s->store + (int64_t)n * 2 * cells;
-    const float* vp = n > 0 ? s->store + (int64_t)(n - 1) * 2 * cells : nullptr;
+    const StoreSlot slot = store_slot(s, n);
+    const float* resid_n = s->resid + (int64_t)n * s->nrec * 2 * s->chains;
     // the first launch follows the residual kernel and memsets: ordinary stream order
-    cudaError_t e = launch_step(n < s->nt - 1, adj_velocity_kernel, grid, block, st, g, a, p, gr, tm, s->taper,
-                                s->rec_map, (const float*)(s->resid + (int64_t)n * s->nrec * 2 * s->chains), vn, vp);
+    cudaError_t e;
+    if (slot.now)
+      e = launch_step(n < s->nt - 1, adj_velocity_kernel<true>, grid, block, st, g, a, p, gr, tm, s->taper,
+                      s->rec_map, resid_n, (const float*)slot.now, prev_of(n, slot), w);
+    else
+      e = launch_step(n < s->nt - 1, adj_velocity_kernel<false>, grid, block, st, g, a, p, gr, tm, s->taper,
+                      s->rec_map, resid_n, (const float*)nullptr, (const float*)nullptr, w);
     if (e != cudaSuccess) return cuda_fail(e, "launch adj_velocity_kernel");
     HMC_TRY(check_launch("adj_velocity_kernel"));
     e = launch_step(true, adj_stress_kernel, grid, block, st, g, a, p, tm, s->taper);

@@ -552,7 +552,12 @@ typedef struct hmc_fwi {
   float* sxx;
   float* szz;
   float* sxz;
-  float* store;             /* [nt][2][nz][nx][C] forward velocities       */
+  float* store;             /* forward velocities for the adjoint: every
+                               step [nt][2][nz][nx][C] (vx, vz after step n)
+                               when snapshot_interval <= 1, else per
+                               snapshot s = n / k of the steps n = 0, k, 2k,
+                               ... [ceil(nt / k)][4][nz][nx][C] (vx, vz after
+                               step n, then after step n - 1)               */
   float* rec;               /* [shots][nt][nrec][2][C] synthetic records    */
   const float* obs;         /* [shots][nt][nrec][2] observed records        */
   float* resid;             /* [nt][nrec][2][C] weighted residuals (work)   */
@@ -574,6 +579,11 @@ typedef struct hmc_fwi {
   double* partial;          /* [64][C] misfit partial sums (work)           */
   int* status;              /* set to 1 when a tile load timed out (nullable:
                                then the stencils read without staged tiles) */
+  int32_t snapshot_interval; /* k: the adjoint correlates the forward and
+                               adjoint fields at steps n = 0, k, 2k, ...
+                               only, weighted by k (psvWave's
+                               snapshot_interval); 0 or 1: every step (the
+                               exact discrete gradient)                     */
 } hmc_fwi;
 
 /* rho, vp, vs -> buoyancies and moduli on the staggered grid.               */

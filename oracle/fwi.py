@@ -28,6 +28,7 @@ class _Shot(ctypes.Structure):
         ("msrc_z", ctypes.c_void_p),
         ("moment", ctypes.c_void_p),
         ("mstf", ctypes.c_void_p),
+        ("snapshot_interval", ctypes.c_int),
     ]
 
 
@@ -49,16 +50,18 @@ def _p(a):
 class Shot:
     """One shot.  `src` is an explosive source's simulation cell (x, z) fed
     by `stf`, or, with `sources` = [(x, z, Mxx, Mzz, Mxz), ...] and `stf` of
-    shape [len(sources)][nt], moment-tensor point sources (src unused)."""
+    shape [len(sources)][nt], moment-tensor point sources (src unused).
+    `snapshot_interval` k > 1 correlates the gradient at every k-th step."""
 
-    def __init__(self, nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z, sources=None):
+    def __init__(self, nx, nz, nt, h, dt, taper, stf, src, rec_x, rec_z, sources=None, snapshot_interval=1):
         self.taper = np.ascontiguousarray(taper, np.float64)
         self.stf = np.ascontiguousarray(stf, np.float64)
         self.rec_x = np.ascontiguousarray(rec_x, np.int32)
         self.rec_z = np.ascontiguousarray(rec_z, np.int32)
         if sources is None:
             self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, _p(self.stf).value, int(src[0]), int(src[1]),
-                           len(self.rec_x), _p(self.rec_x).value, _p(self.rec_z).value, 0, None, None, None, None)
+                           len(self.rec_x), _p(self.rec_x).value, _p(self.rec_z).value, 0, None, None, None, None,
+                           int(snapshot_interval))
         else:
             srcs = np.asarray(sources, np.float64).reshape(-1, 5)
             assert self.stf.shape == (len(srcs), nt)
@@ -67,7 +70,7 @@ class Shot:
             self.moment = np.ascontiguousarray(srcs[:, 2:5], np.float64)
             self.s = _Shot(nx, nz, nt, h, dt, _p(self.taper).value, None, 0, 0, len(self.rec_x),
                            _p(self.rec_x).value, _p(self.rec_z).value, len(srcs), _p(self.msrc_x).value,
-                           _p(self.msrc_z).value, _p(self.moment).value, _p(self.stf).value)
+                           _p(self.msrc_z).value, _p(self.moment).value, _p(self.stf).value, int(snapshot_interval))
         self.nt, self.nrec = nt, len(self.rec_x)
 
     def forward(self, rho, vp, vs):

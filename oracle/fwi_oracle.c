@@ -11,7 +11,9 @@
  * Cerjan et al. (1985) sponge, explosive or moment-tensor point sources (a
  * stress glut) with Ricker wavelets,
  * an L2 waveform misfit and the gradient by the exact transpose (reverse mode)
- * of the discrete time stepping.  No reference numbers exist for this path
+ * of the discrete time stepping, optionally with the forward/adjoint
+ * correlation taken at every k-th step only and weighted by k (psvWave's
+ * snapshot_interval).  No reference numbers exist for this path
  * (the reference's FWI test is skipped without psvWave), so parity is pinned
  * by finite differences and by the CUDA implementation agreeing with this one.
  *
@@ -57,6 +59,10 @@ typedef struct {
   const int* msrc_z;
   const double* moment; /* [nsrc][3]: Mxx, Mzz, Mxz */
   const double* mstf;   /* [nsrc][nt] wavelets */
+  /* k > 1: the gradient correlates forward and adjoint fields at the steps
+   * n = 0, k, 2k, ... only, each weighted by k (psvWave's snapshot_interval);
+   * 0 or 1: at every step (the exact discrete gradient) */
+  int snapshot_interval;
 } fwi_shot;
 
 #define IDX(j, i) ((size_t)(j) * (size_t)nx + (size_t)(i))
@@ -187,9 +193,12 @@ double fwi_gradient(const fwi_shot* s, const double* rho, const double* vp, cons
   double *g_muxz = buf + 14 * N, *t1 = buf + 15 * N, *t2 = buf + 16 * N, *t3 = buf + 17 * N;
   derived(nx, nz, rho, vp, vs, bx, bz, l2m, lam, muxz);
   const double dt = s->dt, h = s->h;
+  const int ksnap = s->snapshot_interval > 1 ? s->snapshot_interval : 1;
   for (int n = nt - 1; n >= 0; --n) {
     const double* vxn = svx + (size_t)n * N;
     const double* vzn = svz + (size_t)n * N;
+    /* weight of this step's correlation: k at snapshot steps, else none */
+    const double wk = n % ksnap == 0 ? (double)ksnap : 0.0;
     /* reverse of 6 */
     for (size_t k = 0; k < N; ++k) {
       asxx[k] *= s->taper[k];
@@ -205,9 +214,9 @@ double fwi_gradient(const fwi_shot* s, const double* rho, const double* vp, cons
         const size_t k = IDX(j, i);
         const double exx = dxm(vxn, nx, j, i, h), ezz = dzm(vzn, nx, j, i, h);
         const double exz = dzp(vxn, nx, j, i, h) + dxp(vzn, nx, j, i, h);
-        g_l2m[k] += dt * (exx * asxx[k] + ezz * aszz[k]);
-        g_lam[k] += dt * (ezz * asxx[k] + exx * aszz[k]);
-        g_muxz[k] += dt * exz * asxz[k];
+        g_l2m[k] += wk * dt * (exx * asxx[k] + ezz * aszz[k]);
+        g_lam[k] += wk * dt * (ezz * asxx[k] + exx * aszz[k]);
+        g_muxz[k] += wk * dt * exz * asxz[k];
         t1[k] = dt * (l2m[k] * asxx[k] + lam[k] * aszz[k]); /* pairs with Dx- vx */
         t2[k] = dt * (lam[k] * asxx[k] + l2m[k] * aszz[k]); /* pairs with Dz- vz */
         t3[k] = dt * muxz[k] * asxz[k];                      /* pairs with Dz+ vx, Dx+ vz */
@@ -242,8 +251,8 @@ double fwi_gradient(const fwi_shot* s, const double* rho, const double* vp, cons
         /* velocity before the taper of step n minus the velocity after step n-1 */
         const double dvx = vxn[k] / s->taper[k] - (vxp ? vxp[k] : 0.0);
         const double dvz = vzn[k] / s->taper[k] - (vzp ? vzp[k] : 0.0);
-        g_bx[k] += dvx / bx[k] * ax[k];
-        g_bz[k] += dvz / bz[k] * az[k];
+        g_bx[k] += wk * dvx / bx[k] * ax[k];
+        g_bz[k] += wk * dvz / bz[k] * az[k];
         t1[k] = dt * bx[k] * ax[k];
         t2[k] = dt * bz[k] * az[k];
       }

@@ -3,10 +3,12 @@ multi-source shots, the cell parametrisation (psvWave's own model vector)
 and the Uniform prior the reference's FWI sampling test uses.
 
 CPU: the reader against the file's values; the oracle's adjoint with
-moment-tensor sources against finite differences (1e-6, FP64); cell-basis
-ordering and segments; the constructor's error paths (reference
+moment-tensor sources against finite differences (1e-6, FP64); the gradient
+correlated at every k-th step (psvWave's snapshot_interval) against the
+exact one; cell-basis ordering and segments; the constructor's error paths (reference
 tests/test_elasticFWI.py:18-52).  GPU: records and cell-space gradients of a
-multi-source moment-tensor configuration against the FP64 oracle (1e-5);
+multi-source moment-tensor configuration with snapshot interval 5 against
+the FP64 oracle (1e-5);
 create_default on the .ini, a gradient step that lowers the misfit, and a
 short HMC run under a Uniform prior (reference tests/test_elasticFWI.py:
 55-122)."""
@@ -27,10 +29,11 @@ def ini_config():
     return FW.ElasticConfig.from_ini(INI)
 
 
-def oracle_shots(cfg):
-    return [OF.Shot(cfg.nxc, cfg.nzc, cfg.nt, cfg.h, cfg.dt, cfg.taper(), cfg.shot_wavelets(k), None, cfg.rec_x,
-                    cfg.rec_z, sources=[(q.x, q.z, q.mxx, q.mzz, q.mxz) for q in cfg.shots[k]])
-            for k in range(cfg.n_shots)]
+def oracle_shots(cfg, snapshot_interval=None):
+    k = cfg.snapshot_interval if snapshot_interval is None else snapshot_interval
+    return [OF.Shot(cfg.nxc, cfg.nzc, cfg.nt, cfg.h, cfg.dt, cfg.taper(), cfg.shot_wavelets(s), None, cfg.rec_x,
+                    cfg.rec_z, sources=[(q.x, q.z, q.mxx, q.mzz, q.mxz) for q in cfg.shots[s]], snapshot_interval=k)
+            for s in range(cfg.n_shots)]
 
 
 def test_ini_reader_values():
@@ -101,7 +104,7 @@ def test_cell_basis_order_and_segments():
 
 def test_oracle_adjoint_with_moment_tensor_sources_matches_finite_differences():
     cfg = ini_config()
-    shot = oracle_shots(cfg)[0]
+    shot = oracle_shots(cfg, snapshot_interval=1)[0]
     vp, vs, rho = (cfg.extend(f) for f in FW.background_model(cfg))
     X, Z = np.meshgrid(np.arange(cfg.nxc), np.arange(cfg.nzc))
     bump = np.exp(-((X - 28) ** 2 + (Z - 25) ** 2) / 20.0)
@@ -123,6 +126,27 @@ def test_oracle_adjoint_with_moment_tensor_sources_matches_finite_differences():
         fd = (mis(1) - mis(-1)) / 2
         an = np.sum(grads[k] * dm)
         assert abs(fd - an) <= 1e-6 * abs(fd), (k, fd, an)
+
+
+def test_snapshot_correlation_approximates_the_exact_gradient():
+    """Correlating forward and adjoint fields at every k-th step only (weight
+    k) leaves the misfit unchanged and, for k well below the wavelet's
+    period (83 steps here), the gradient within a few 1e-3 of the exact one
+    (aliasing of the correlation's spectrum above 1 / (2 k dt))."""
+    cfg = ini_config()
+    vp, vs, rho = (cfg.extend(f) for f in FW.background_model(cfg))
+    X, Z = np.meshgrid(np.arange(cfg.nxc), np.arange(cfg.nzc))
+    bump = np.exp(-((X - 28) ** 2 + (Z - 25) ** 2) / 20.0)
+    exact = oracle_shots(cfg, 1)[0]
+    ovx, ovz = exact.forward(rho * (1 + 0.05 * bump), vp * (1 - 0.05 * bump), vs * (1 - 0.05 * bump))
+    w = 1.0 / np.mean(ovx**2 + ovz**2)
+    c1, g1 = exact.gradient(rho, vp, vs, ovx, ovz, w)
+    for k, tol in ((2, 1e-3), (5, 5e-3)):
+        ck, gk = oracle_shots(cfg, k)[0].gradient(rho, vp, vs, ovx, ovz, w)
+        assert ck == c1
+        errs = [np.abs(gk[f] - g1[f]).max() / np.abs(g1[f]).max() for f in range(3)]
+        print(f"snapshot interval {k}: max relative gradient error (rho, vp, vs) {np.round(errs, 5)}")
+        assert max(errs) < tol
 
 
 def test_explosive_sources_are_the_single_source_special_case():
