@@ -884,18 +884,19 @@ def choose_trajectory(pilot, min_acceptance=0.25):
     return L_best, eps_best
 
 
-def esjd_min(q, std):
-    """Smallest per-parameter expected squared jump between consecutive
-    draws, in units of the posterior variance: min_i mean_(t,c)
-    (q[t+1,i,c] - q[t,i,c])^2 / std_i^2, for draws q [N][d][C] (device).
-    It measures how far the slowest direction moves per proposal, the same
-    way for both samplers; for chains that diffuse, ESS per draw is about
-    half of it."""
+def variogram_min(q, std, lag=1):
+    """Smallest per-parameter mean squared displacement over `lag` draws, in
+    units of the posterior variance: min_i mean_(t,c) (q[t+lag,i,c] -
+    q[t,i,c])^2 / (2 std_i^2), for draws q [N][d][C] (device) and the
+    posterior std from a long reference run.  It equals 1 - rho_i(lag) (the
+    autocorrelation at that lag) without estimating the variance from the
+    short run itself, so a short run that has not yet decorrelated reads low
+    instead of looking converged."""
     import torch
 
     s = torch.as_tensor(np.asarray(std, np.float64), device=q.device)[:, None]
-    dq = (q[1:].double() - q[:-1].double()) / s
-    return float((dq * dq).mean(dim=(0, 2)).min())
+    dq = (q[lag:].double() - q[:-lag].double()) / s
+    return float((dq * dq).mean(dim=(0, 2)).min() / 2.0)
 
 
 def run_fwi_arm(args, wl):
@@ -937,7 +938,7 @@ def run_fwi_arm(args, wl):
     t_burn = time.perf_counter() - t0
     q_start = burn.current_model
     acc_burn = float(np.mean(burn.accepted_proposals) / Nb)
-    jump_plain = esjd_min(burn.samples_device[0], post_std)
+    decor_plain = variogram_min(burn.samples_device[0], post_std, 1)
 
     # ---- surrogate training on the device ---------------------------------
     kind = S.PotentialSurrogate if args.surrogate == "potential" else S.MLPSurrogate
@@ -976,11 +977,15 @@ def run_fwi_arm(args, wl):
 
     # ---- screen (untimed): surrogate against plain HMC ---------------------
     # A short surrogate run (with its refreshes) measures its cost per
-    # proposal and how far its slowest direction moves (esjd_min); the exact
-    # burn-in gives plain HMC's.  Plain HMC is the fallback: with
-    # --sampler auto the timed run uses the surrogate only when its jump rate
-    # per second beats plain HMC's.  (A short run's ESS is no guide: its lag
-    # windows end long before the surrogate chains decorrelate.)
+    # proposal; with it, the number of surrogate proposals `lag` that cost
+    # one plain proposal.  How far each sampler decorrelates its slowest
+    # parameter in that time (variogram_min: plain HMC over one proposal of
+    # the exact burn-in, the surrogate over `lag` proposals) decides: plain
+    # HMC is the fallback, and with --sampler auto the timed run uses the
+    # surrogate only when it decorrelates further.  (The jump of a single
+    # surrogate proposal over-predicts: its successive jumps partly undo each
+    # other, and a short run's ESS windows end long before its chains
+    # decorrelate.)
     screen = H.Samplers.HMC(seed=sharding.rank_seed(170, rank))
     n_screen = args.screen_proposals
     screen.prepare(None, post, initial_model=q_start, proposals=n_screen, keep_samples=True, surrogate=net,
@@ -992,22 +997,27 @@ def run_fwi_arm(args, wl):
     screen.stream.synchronize()
     t_screen = ev_a.elapsed_time(ev_b) / 1e3 / n_screen
     screen.finish()
-    jump_sur = esjd_min(screen.samples_device[0], post_std)
-    acc_screen = float(np.mean(screen.accepted_proposals) / n_screen)
     t_plain_burn = t_burn / Nb  # wall seconds per exact proposal (recording included)
-    rate_sur, rate_plain = jump_sur / t_screen, jump_plain / t_plain_burn
+    lag = int(min(max(round(t_plain_burn / t_screen), 1), n_screen // 2))
+    q_screen = screen.samples_device[0]
+    decor_sur = variogram_min(q_screen, post_std, lag)
+    acc_screen = float(np.mean(screen.accepted_proposals) / n_screen)
     if args.sampler == "auto":
-        sampler = "surrogate" if rate_sur > rate_plain else "plain"
+        sampler = "surrogate" if decor_sur > decor_plain * (lag * t_screen / t_plain_burn) else "plain"
     else:
         sampler = args.sampler
-    choice = {"rule": "surrogate when its slowest-direction jump per second (esjd_min / s) beats plain HMC's",
+    choice = {"rule": "surrogate when, per second, it decorrelates its slowest parameter further than plain HMC "
+                      "(1 - autocorrelation over the surrogate proposals that cost one plain proposal, against plain "
+                      "HMC's over one proposal; posterior std from the reference run)",
               "sampler": sampler, "forced": args.sampler != "auto",
               "surrogate": {"proposals": n_screen, "ms_per_proposal": 1e3 * t_screen, "acceptance": acc_screen,
-                            "esjd_min": jump_sur, "esjd_min_per_s": rate_sur},
+                            "lag": lag, "decorrelation_over_lag": decor_sur,
+                            "single_proposal_decorrelation": variogram_min(q_screen, post_std, 1)},
               "plain": {"proposals": Nb, "ms_per_proposal": 1e3 * t_plain_burn, "acceptance": acc_burn,
-                        "esjd_min": jump_plain, "esjd_min_per_s": rate_plain,
+                        "decorrelation_over_one_proposal": decor_plain,
                         "note": "from the exact burn-in (wall time, pair recording included)"},
-              "estimated_speedup_of_surrogate": rate_sur / rate_plain if rate_plain > 0 else None}
+              "estimated_speedup_of_surrogate": (decor_sur / (lag * t_screen)) / (decor_plain / t_plain_burn)
+              if decor_plain > 0 else None}
 
     # ---- the timed run: W untimed blocks, then K timed blocks --------------
     # The run goes through the public API from host arrays to host arrays:
@@ -1326,9 +1336,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="fwi", choices=sorted(WORKLOADS))
     ap.add_argument("--sampler", default="auto", choices=["auto", "surrogate", "plain"],
-                    help="fwi: sampler of the timed run; auto: the surrogate when the screen finds its jump rate above "
-                         "plain HMC's, else plain HMC (the fallback)")
-    ap.add_argument("--screen-proposals", type=int, default=64,
+                    help="fwi: sampler of the timed run; auto: the surrogate when the screen finds that it "
+                         "decorrelates faster per second than plain HMC, else plain HMC (the fallback)")
+    ap.add_argument("--screen-proposals", type=int, default=96,
                     help="fwi: surrogate proposals of the untimed screen against plain HMC")
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="fwi: timed plain proposals giving plain HMC's cost when the surrogate runs")
