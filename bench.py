@@ -406,7 +406,7 @@ class FwiWorkload:
     hidden = (512, 512)
     # a step is one block of proposals of every chain: `block` surrogate-
     # driven ones (20 steps = 2000 proposals), or, when the screen falls back
-    # to plain HMC, enough exact ones for 40 timed proposals in all
+    # to plain HMC, enough exact ones for 100 timed proposals in all
     default_steps, default_warmup = 20, 3
     block = 100
     burn_in = 12  # exact proposals recording (position, gradient) training pairs
@@ -1028,9 +1028,11 @@ def run_fwi_arm(args, wl):
         B = B_s
         run_kw = dict(kw_s, surrogate=net, **refresh_kw)
     else:
-        # at least 40 timed proposals: plain HMC's lag windows (autocorrelation
-        # time near 4 proposals) then truncate
-        B = args.plain_block if args.plain_block else max(2, -(-40 // K))
+        # at least 100 timed proposals: the split-chain ESS windows (half the
+        # run) then reach 50 lags, where plain HMC's autocorrelation (about 4
+        # proposals) has died out for nearly every parameter; 40 proposals
+        # truncated only 29 % of them
+        B = args.plain_block if args.plain_block else max(2, -(-100 // K))
         run_kw = dict(kw)
     torch.cuda.synchronize()
     t_e2e0 = time.perf_counter()
@@ -1344,7 +1346,7 @@ def main():
                     help="fwi: timed plain proposals giving plain HMC's cost when the surrogate runs")
     ap.add_argument("--block", type=int, default=None, help="fwi: surrogate-driven proposals per step")
     ap.add_argument("--plain-block", type=int, default=None,
-                    help="fwi: plain proposals per step when plain HMC runs (default: at least 40 timed proposals)")
+                    help="fwi: plain proposals per step when plain HMC runs (default: at least 100 timed proposals)")
     ap.add_argument("--value-weight", type=float, default=1.0,
                     help="fwi: weight of the misfit-value matching loss of the potential surrogate (0: gradients only)")
     ap.add_argument("--refresh-interval", type=int, default=32,

@@ -600,21 +600,62 @@ __global__ void srcloc_kernel(int64_t E, int64_t S, int64_t C, const T* __restri
 }
 
 // FP32 source location with the per-pair work cut to the arithmetic that
-// matters (the kernel above is issue-bound, so instructions are the lever):
-//   - stations staged as float4 (x, y, z, -) and the pair data of 16 events x
-//     a chunk of stations as float2 (w, o) = (1 / std^2, observed time), both
-//     in shared memory; a NaN observation or weight is staged as (0, 0), which
-//     makes every term of that pair zero — the nansum of the reference
-//     (SourceLocation.py:495-540) without a NaN test per pair;
-//   - one reciprocal square root per pair of the distance clamped below by
-//     1e-30 (an event on a station then contributes zero partials, nansum's
-//     treatment of 0 / 0);
+// matters (the kernel above is issue-bound, so instructions are the lever),
+// two stations per instruction on Blackwell's packed FP32 pipe:
+//   - stations staged in pairs, (x_a, x_b, y_a, y_b) and (z_a, z_b), and the
+//     pair data of 16 events x a chunk of stations as (w_a, w_b, o_a, o_b),
+//     (w, o) = (1 / std^2, observed time), in shared memory; a NaN
+//     observation or weight, and the padding of an odd chunk, is staged as
+//     (0, 0), which makes every term of that pair zero — the nansum of the
+//     reference (SourceLocation.py:495-540) without a NaN test per pair;
+//   - every arithmetic step runs on both stations at once with the f32x2
+//     add / sub / mul / fma instructions (sm_100 and later), one reciprocal
+//     square root per station; the squared distance starts from 1e-30, so
+//     an event on a station contributes zero partials (nansum's 0 / 0);
 //   - 1 / v is factored out of the x, y, z partials and 1 / v^2 out of the
 //     velocity partial: per pair k = (t_calc - o) w / dist, and the thread
-//     accumulates k dx, k dy, k dz, (t_calc - o) w and (t_calc - o) w dist;
+//     accumulates k dx, k dy, k dz, (t_calc - o) w and (t_calc - o) w dist in
+//     two lanes (even and odd stations), added at the end;
 //   - misfit terms are summed in FP32 over at most SL_CHUNK stations, then in
 //     FP64.
 constexpr int SL_CHUNK = 512;
+constexpr int SL_PAIRS = SL_CHUNK / 2;
+
+// two FP32 values in one 64-bit register: element a in the low half
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 x2_pack(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void x2_unpack(f32x2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ float x2_sum(f32x2 v) {
+  float a, b;
+  x2_unpack(v, a, b);
+  return a + b;
+}
 
 template <bool GRAD>
 __global__ void srcloc_f32_kernel(int64_t E, int64_t S, int64_t C, const float* __restrict__ M,
@@ -623,14 +664,16 @@ __global__ void srcloc_f32_kernel(int64_t E, int64_t S, int64_t C, const float* 
                                   const float* __restrict__ iv, int infer_v, float v_fixed, double* out_x,
                                   float* out_g, int accumulate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float4* st = (float4*)smem_raw;                 // [SL_CHUNK]
-  float2* pw = (float2*)(st + SL_CHUNK);          // [SL_EY][SL_CHUNK]
+  ulonglong2* sxy = (ulonglong2*)smem_raw;             // [SL_PAIRS] (x_a, x_b), (y_a, y_b)
+  f32x2* sz = (f32x2*)(sxy + SL_PAIRS);                // [SL_PAIRS] (z_a, z_b)
+  ulonglong2* swo = (ulonglong2*)(sz + SL_PAIRS);      // [SL_EY][SL_PAIRS] (w_a, w_b), (o_a, o_b)
   __shared__ double red[SL_EY][RED_X + 1];
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int64_t c = blockIdx.x * (int64_t)RED_X + threadIdx.x;
   const bool live = c < C;
   const float v = live ? (infer_v ? M[(4 * E) * C + c] : v_fixed) : 1.f;
   const float inv_v = 1.f / v;
+  const f32x2 IV = x2_pack(inv_v, inv_v), EPS = x2_pack(1e-30f, 1e-30f);
   double mis = 0.0, gvd_total = 0.0;
   for (int64_t e0 = 0; e0 < E; e0 += SL_EY) {
     const int64_t e = e0 + threadIdx.y;
@@ -642,64 +685,78 @@ __global__ void srcloc_f32_kernel(int64_t E, int64_t S, int64_t C, const float* 
       z = M[(4 * e + 2) * C + c];
       t0 = M[(4 * e + 3) * C + c];
     }
-    float gx = 0.f, gy = 0.f, gz = 0.f, gT = 0.f, gvd = 0.f;
+    const f32x2 X = x2_pack(x, x), Y = x2_pack(y, y), Z = x2_pack(z, z), T0 = x2_pack(t0, t0);
+    const f32x2 zero = x2_pack(0.f, 0.f);
+    f32x2 gx = zero, gy = zero, gz = zero, gT = zero, gvd = zero;
     for (int64_t s0 = 0; s0 < S; s0 += SL_CHUNK) {
       const int sn = (int)(S - s0 < SL_CHUNK ? S - s0 : SL_CHUNK);
+      const int np = (sn + 1) / 2;
       __syncthreads();  // the previous chunk is consumed
-      for (int k = tid; k < sn; k += nthr) st[k] = make_float4(rx[s0 + k], ry[s0 + k], rz[s0 + k], 0.f);
-      for (int k = tid; k < SL_EY * sn; k += nthr) {
-        const int ye = k / sn, ks = k - ye * sn;
+      for (int k = tid; k < np; k += nthr) {
+        const int a = 2 * k, b = 2 * k + 1;
+        const bool hb = b < sn;
+        sxy[k] = make_ulonglong2(x2_pack(rx[s0 + a], hb ? rx[s0 + b] : 0.f),
+                                 x2_pack(ry[s0 + a], hb ? ry[s0 + b] : 0.f));
+        sz[k] = x2_pack(rz[s0 + a], hb ? rz[s0 + b] : 0.f);
+      }
+      for (int k = tid; k < SL_EY * np; k += nthr) {
+        const int ye = k / np, kp = k - ye * np;
         const int64_t ee = e0 + ye;
-        float w = 0.f, o = 0.f;
-        if (ee < E) {
-          w = iv[ee * S + s0 + ks];
-          o = obs[ee * S + s0 + ks];
-          if (isnan(w) || isnan(o)) w = o = 0.f;
+        float w[2] = {0.f, 0.f}, o[2] = {0.f, 0.f};
+        for (int h = 0; h < 2; ++h) {
+          const int ks = 2 * kp + h;
+          if (ee < E && ks < sn) {
+            w[h] = iv[ee * S + s0 + ks];
+            o[h] = obs[ee * S + s0 + ks];
+            if (isnan(w[h]) || isnan(o[h])) w[h] = o[h] = 0.f;
+          }
         }
-        pw[ye * SL_CHUNK + ks] = make_float2(w, o);
+        swo[ye * SL_PAIRS + kp] = make_ulonglong2(x2_pack(w[0], w[1]), x2_pack(o[0], o[1]));
       }
       __syncthreads();
       if (!ev) continue;
-      const float2* my = pw + threadIdx.y * SL_CHUNK;
-      float ms = 0.f;
+      const ulonglong2* my = swo + threadIdx.y * SL_PAIRS;
+      f32x2 ms = zero;
 #pragma unroll 4
-      for (int k = 0; k < sn; ++k) {
-        const float4 q = st[k];
-        const float2 p = my[k];
-        const float dx = x - q.x, dy = y - q.y, dz = z - q.z;
-        const float r2 = fmaxf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)), 1e-30f);
-        const float inv = rsqrtf(r2);
-        const float dist = r2 * inv;
-        const float res = fmaf(dist, inv_v, t0) - p.y;  // t_calc - obs
+      for (int k = 0; k < np; ++k) {
+        const ulonglong2 q = sxy[k];
+        const ulonglong2 p = my[k];
+        const f32x2 dx = x2_sub(X, q.x), dy = x2_sub(Y, q.y), dz = x2_sub(Z, sz[k]);
+        const f32x2 r2 = x2_fma(dz, dz, x2_fma(dy, dy, x2_fma(dx, dx, EPS)));
+        float ra, rb;
+        x2_unpack(r2, ra, rb);
+        const f32x2 inv = x2_pack(rsqrtf(ra), rsqrtf(rb));
+        const f32x2 dist = x2_mul(r2, inv);
+        const f32x2 res = x2_sub(x2_fma(dist, IV, T0), p.y);  // t_calc - obs
         if (GRAD) {
-          const float mg = res * p.x;
-          const float k2 = mg * inv;
-          gx = fmaf(k2, dx, gx);
-          gy = fmaf(k2, dy, gy);
-          gz = fmaf(k2, dz, gz);
-          gT += mg;
-          gvd = fmaf(mg, dist, gvd);
+          const f32x2 mg = x2_mul(res, p.x);
+          const f32x2 k2 = x2_mul(mg, inv);
+          gx = x2_fma(k2, dx, gx);
+          gy = x2_fma(k2, dy, gy);
+          gz = x2_fma(k2, dz, gz);
+          gT = x2_add(gT, mg);
+          gvd = x2_fma(mg, dist, gvd);
         } else {
-          ms = fmaf(res * res, p.x, ms);
+          ms = x2_fma(x2_mul(res, res), p.x, ms);
         }
       }
-      if (!GRAD) mis += (double)ms;
+      if (!GRAD) mis += (double)x2_sum(ms);
     }
     if (GRAD && ev) {
       const int64_t o0 = (4 * e) * C + c;
-      const float ax = gx * inv_v, ay = gy * inv_v, az = gz * inv_v;
+      const float ax = x2_sum(gx) * inv_v, ay = x2_sum(gy) * inv_v, az = x2_sum(gz) * inv_v, aT = x2_sum(gT);
       if (accumulate) {
         out_g[o0] += ax;
         out_g[o0 + C] += ay;
         out_g[o0 + 2 * C] += az;
-        out_g[o0 + 3 * C] += gT;
+        out_g[o0 + 3 * C] += aT;
       } else {
         out_g[o0] = ax;
         out_g[o0 + C] = ay;
         out_g[o0 + 2 * C] = az;
-        out_g[o0 + 3 * C] = gT;
+        out_g[o0 + 3 * C] = aT;
       }
-      gvd_total += (double)gvd;
+      gvd_total += (double)x2_sum(gvd);
     }
   }
   // Reduce the velocity partial (or the misfit) over the event lanes.
@@ -731,7 +788,7 @@ int srcloc(bool grad, int64_t E, int64_t S, int64_t C, const void* M, const void
   HMC_REQUIRE(M && rx && ry && rz && obs && iv, "%s: null argument", who);
   HMC_REQUIRE(grad ? out_g != nullptr : out_x != nullptr, "%s: null output", who);
   if (sizeof(T) == 4) {
-    const size_t smem = SL_CHUNK * sizeof(float4) + (size_t)SL_EY * SL_CHUNK * sizeof(float2);
+    const size_t smem = SL_PAIRS * (sizeof(ulonglong2) + sizeof(f32x2)) + (size_t)SL_EY * SL_PAIRS * sizeof(ulonglong2);
     auto k32 = grad ? srcloc_f32_kernel<true> : srcloc_f32_kernel<false>;
     static bool attr_set = false;
     if (!attr_set) {
