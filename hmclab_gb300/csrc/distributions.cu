@@ -351,6 +351,11 @@ __global__ void __launch_bounds__(CSR_THREADS, 2)
 // loads of X and stores of out).  The nonzeros of the row are added in CSR
 // order with fused multiply-adds (four rows of X in flight), optionally on
 // the centred operand X - center[col].
+#ifndef HMC_CSR_GATHER_DEPTH
+#define HMC_CSR_GATHER_DEPTH 8
+#endif
+constexpr int GATHER_DEPTH = HMC_CSR_GATHER_DEPTH;
+
 template <int VEC>
 __global__ void csr_gather_kernel(int rows, int C, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
                                   const float* __restrict__ val, const float* __restrict__ X,
@@ -372,21 +377,20 @@ __global__ void csr_gather_kernel(int rows, int C, const int32_t* __restrict__ r
 #pragma unroll
     for (int v = 0; v < VEC; ++v) x[v] = xs[v] - cj;
   };
+  // GATHER_DEPTH rows of X in flight per thread (the product waits on L2
+  // gathers), summed in CSR order
   int k = b;
-  for (; k + 4 <= e; k += 4) {
-    float x0[VEC], x1[VEC], x2[VEC], x3[VEC];
-    load(k, x0);
-    load(k + 1, x1);
-    load(k + 2, x2);
-    load(k + 3, x3);
-    const float v0 = val[k], v1 = val[k + 1], v2 = val[k + 2], v3 = val[k + 3];
+  for (; k + GATHER_DEPTH <= e; k += GATHER_DEPTH) {
+    float x[GATHER_DEPTH][VEC], w[GATHER_DEPTH];
 #pragma unroll
-    for (int v = 0; v < VEC; ++v) {
-      a[v] = fmaf(v0, x0[v], a[v]);
-      a[v] = fmaf(v1, x1[v], a[v]);
-      a[v] = fmaf(v2, x2[v], a[v]);
-      a[v] = fmaf(v3, x3[v], a[v]);
+    for (int u = 0; u < GATHER_DEPTH; ++u) {
+      load(k + u, x[u]);
+      w[u] = val[k + u];
     }
+#pragma unroll
+    for (int v = 0; v < VEC; ++v)
+#pragma unroll
+      for (int u = 0; u < GATHER_DEPTH; ++u) a[v] = fmaf(w[u], x[u][v], a[v]);
   }
   for (; k < e; ++k) {
     float x0[VEC];
