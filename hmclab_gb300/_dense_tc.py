@@ -94,6 +94,10 @@ class DenseOperands:
             raise DeviceTimeoutError(f"tensor-core contraction reported status {s} (a bounded wait expired)")
 
 
+# the fused step and the two-pass step (same arguments, bitwise-equal results)
+_STEP_ENTRIES = ("hmc_tc_step", "hmc_tc_step_split")
+
+
 class FusedDenseStep:
     """One proposal of the sampler for BayesRule([diagonal prior, dense
     premultiplied LinearMatrix]) in FP32 with unit or diagonal mass."""
@@ -114,6 +118,33 @@ class FusedDenseStep:
             pp = prior._params("float32")
             self.kind, self.mean, self.w = PRIOR_LAPLACE, pp["mean"], pp["iw"]
         self.cur = 0
+        self.entry = self._choose_entry()
+
+    def _call(self, entry, kick, drift, cur, nxt, h):
+        o = self.ops
+        _lib.call(entry, self.smp._state_ref, o.gtg_hi.data_ptr(), o.gtg_lo.data_ptr(), o.ld,
+                  o.q_hi[cur].data_ptr(), o.q_lo[cur].data_ptr(), o.q_hi[nxt].data_ptr(), o.q_lo[nxt].data_ptr(),
+                  o.ld, o.center.data_ptr(), o.gtd0.data_ptr(), self.kind, _dev.ptr(self.mean), _dev.ptr(self.w),
+                  float(kick), float(drift), o.status.data_ptr(), h)
+
+    def _choose_entry(self):
+        """The fused step (contraction with the update in its epilogue) or
+        the two-pass step (contraction, then a streaming update), whichever
+        the autotuner times faster for this shape; both give bitwise-equal
+        results.  Timed with zero kick and drift on the current model, which
+        leaves p, q and the flags as they are and only writes the next
+        operand buffer, rewritten by the first real step."""
+        from hmclab_gb300 import autotune as _autotune
+
+        h = self.smp.stream.cuda_stream
+        self.ops.split(self.smp.q_cur, self.cur, h)
+        nxt = 1 - self.cur
+        shape = {"d": int(self.smp.dimensions), "C": int(self.smp.chains), "prior": int(self.kind),
+                 "mass": int(self.smp.mass_matrix.kind)}
+        (v,) = _autotune.choose("tc_step", shape, [(0,), (1,)],
+                                lambda c: self._call(_STEP_ENTRIES[c[0]], 0.0, 0.0, self.cur, nxt, h),
+                                self.smp.device, h)
+        return _STEP_ENTRIES[v]
 
     @staticmethod
     def applies(sampler):
@@ -145,12 +176,7 @@ class FusedDenseStep:
 
     def kick_drift(self, kick, drift, h):
         nxt = 1 - self.cur
-        o = self.ops
-        _lib.call("hmc_tc_step", self.smp._state_ref, o.gtg_hi.data_ptr(), o.gtg_lo.data_ptr(), o.ld,
-                  o.q_hi[self.cur].data_ptr(), o.q_lo[self.cur].data_ptr(), o.q_hi[nxt].data_ptr(),
-                  o.q_lo[nxt].data_ptr(), o.ld, o.center.data_ptr(), o.gtd0.data_ptr(), self.kind,
-                  _dev.ptr(self.mean), _dev.ptr(self.w),
-                  float(kick), float(drift), o.status.data_ptr(), h)
+        self._call(self.entry, kick, drift, self.cur, nxt, h)
         self.cur = nxt
 
     def drift_only(self, drift, h):

@@ -237,6 +237,7 @@ SIGNATURES = {
     "hmc_split_bf16_transpose": [I64, I64, P, P, I64, P, P, S],
     "hmc_tc_gradient": [I64, I64, I64, P, P, I64, P, P, I64, P, P, I, P, S],
     "hmc_tc_step": [P, P, P, I64, P, P, P, P, I64, P, P, I, P, P, D, D, P, S],
+    "hmc_tc_step_split": [P, P, P, I64, P, P, P, P, I64, P, P, I, P, P, D, D, P, S],
     "hmc_tc_resid_misfit": [I64, I64, I64, P, P, I64, P, P, I64, P, P, P, P, I, P, S],
     "hmc_tc_partials_size": [I64, I64],
     "hmc_tc_mlp": [I, I64, I64, I64, P, I64, P, I64, P, P, P, S],

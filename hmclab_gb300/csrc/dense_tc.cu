@@ -513,6 +513,74 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// ---- the leapfrog update as its own pass ------------------------------------
+// The update hmc_tc_step_split runs after an EPI_GRAD contraction wrote
+// g = GtG q - bias: the prior's gradient, kick, drift and bound reflection
+// (the same expressions, in the same order, as the EPI_STEP epilogue, so
+// the results are bitwise equal), then the next operand q - center split
+// into BF16 hi/lo and transposed to chain-major [C][ldq] through a 32 x 32
+// shared-memory tile (rows d..ldq-1 written as zeros).  Every SM streams
+// the state with 8 warps per block instead of the contraction's 8
+// epilogue warps per 128-chain tile.
+__global__ void step_update_kernel(int64_t d, EpiParams ep, const float* __restrict__ g) {
+  __shared__ float tile[32][33];
+  const int64_t C = ep.C;
+  const int64_t i0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  const int64_t c = c0 + threadIdx.x;
+  float eps_k = 0.f, eps_d = 0.f;
+  if (c < C) {
+    const float e = ep.eps_local[c];
+    eps_k = ep.kick * e;
+    eps_d = ep.drift * e;
+  }
+  bool oob = false;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t r = i0 + y;
+    float qs = 0.f;
+    if (r < d && c < C) {
+      const int64_t k = r * C + c;
+      float qv = ep.q[k], pv = ep.p[k];
+      float gv = g[k];
+      if (ep.prior == PRIOR_NORMAL) {
+        gv += ep.prior_w[r] * (qv - ep.prior_mean[r]);
+      } else if (ep.prior == PRIOR_LAPLACE) {
+        const float dq = qv - ep.prior_mean[r];
+        gv += (dq > 0.f ? 1.f : (dq < 0.f ? -1.f : 0.f)) * ep.prior_w[r];
+      }
+      pv = pv - eps_k * gv;
+      if (eps_d != 0.f) {
+        const float mp = ep.minv ? ep.minv[r] * pv : pv;
+        float qn = qv + eps_d * mp;
+        if (ep.lo && qn < ep.lo[r]) {
+          qn += 2.f * (ep.lo[r] - qn);
+          pv = -pv;
+        }
+        if (ep.hi && qn > ep.hi[r]) {
+          qn += 2.f * (ep.hi[r] - qn);
+          pv = -pv;
+        }
+        if ((ep.lo && qn < ep.lo[r]) || (ep.hi && qn > ep.hi[r])) oob = true;
+        qv = qn;
+      }
+      ep.p[k] = pv;
+      if (eps_d != 0.f) ep.q[k] = qv;
+      qs = ep.center != nullptr ? qv - ep.center[r] : qv;
+    }
+    tile[y][threadIdx.x] = qs;
+  }
+  if (oob) atomicOr(&ep.flags[c], HMC_FLAG_OUT_OF_BOUNDS);
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t cc = c0 + y, i = i0 + threadIdx.x;
+    if (cc < C && i < ep.ldq) {
+      const float v = tile[threadIdx.x][y];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      ep.qn_hi[cc * ep.ldq + i] = h;
+      ep.qn_lo[cc * ep.ldq + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+  }
+}
+
 // ---- helpers for the operands ------------------------------------------------
 // hi/lo split of a row-major FP32 matrix into padded [rows][ld] BF16 arrays
 // (columns cols..ld-1 are zero).
@@ -707,6 +775,52 @@ HMC_API int hmc_tc_step(const hmc_chains* s, const void* a_hi, const void* a_lo,
   ep.ldq = ldq;
   ep.status = status;
   return launch<EPI_STEP>(s->chains, s->dims, s->dims, q_hi, q_lo, ldq, a_hi, a_lo, lda, ep, as_stream(stream));
+}
+
+HMC_API int hmc_tc_step_split(const hmc_chains* s, const void* a_hi, const void* a_lo, int64_t lda,
+                              const void* q_hi, const void* q_lo, void* qn_hi, void* qn_lo, int64_t ldq,
+                              const float* center, const float* bias, int prior, const float* prior_mean,
+                              const float* prior_w, double kick, double drift, int* status, void* stream) {
+  HMC_REQUIRE(s != nullptr && s->dtype == HMC_F32, "hmc_tc_step_split: needs an FP32 chain state");
+  HMC_REQUIRE(s->mass_kind == HMC_MASS_UNIT || s->mass_kind == HMC_MASS_DIAG,
+              "hmc_tc_step_split: unit or diagonal mass only");
+  HMC_REQUIRE(bias && s->p && s->q && s->g && s->eps_local && s->flags, "hmc_tc_step_split: missing buffer");
+  HMC_REQUIRE(prior == PRIOR_NONE || (prior_mean && prior_w), "hmc_tc_step_split: prior needs mean and weights");
+  HMC_REQUIRE(prior >= PRIOR_NONE && prior <= PRIOR_LAPLACE, "hmc_tc_step_split: unknown prior kind");
+  HMC_REQUIRE(ldq % 16 == 0 && ldq >= s->dims, "hmc_tc_step_split: operand pitch must be a multiple of 16 >= d");
+  HMC_REQUIRE(qn_hi && qn_lo && qn_hi != q_hi && qn_lo != q_lo,
+              "hmc_tc_step_split: the next operand must exist and not alias the current one");
+  EpiParams eg = {};
+  eg.C = s->chains;
+  eg.rows = s->dims;
+  eg.bias = bias;
+  eg.g = (float*)s->g;
+  eg.accumulate = 0;
+  eg.status = status;
+  cudaStream_t st = as_stream(stream);
+  HMC_TRY(launch<EPI_GRAD>(s->chains, s->dims, s->dims, q_hi, q_lo, ldq, a_hi, a_lo, lda, eg, st));
+  EpiParams ep = {};
+  ep.C = s->chains;
+  ep.rows = s->dims;
+  ep.prior = prior;
+  ep.prior_mean = prior_mean;
+  ep.prior_w = prior_w;
+  ep.p = (float*)s->p;
+  ep.q = (float*)s->q;
+  ep.eps_local = (const float*)s->eps_local;
+  ep.kick = (float)kick;
+  ep.drift = (float)drift;
+  ep.minv = s->mass_kind == HMC_MASS_DIAG ? (const float*)s->mass_inv_diag : nullptr;
+  ep.lo = (const float*)s->lower;
+  ep.hi = (const float*)s->upper;
+  ep.flags = s->flags;
+  ep.center = center;
+  ep.qn_hi = (__nv_bfloat16*)qn_hi;
+  ep.qn_lo = (__nv_bfloat16*)qn_lo;
+  ep.ldq = ldq;
+  const dim3 grid((unsigned)((s->chains + 31) / 32), (unsigned)((ldq + 31) / 32));
+  step_update_kernel<<<grid, dim3(32, 8), 0, st>>>(s->dims, ep, (const float*)s->g);
+  return check_launch("step_update_kernel");
 }
 
 HMC_API int hmc_tc_resid_misfit(int64_t n, int64_t d, int64_t C, const void* g_hi, const void* g_lo, int64_t ldg,

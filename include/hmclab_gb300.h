@@ -384,6 +384,18 @@ HMC_API int hmc_tc_step(const hmc_chains* s, const void* a_hi,
                         const float* bias, int prior,
                         const float* prior_mean, const float* prior_w,
                         double kick, double drift, int* status, void* stream);
+/* The same step in two passes with bitwise-equal results: the contraction
+ * writes g = GtG q - bias into s->g, then one streaming pass applies the
+ * prior, kick, drift and reflection and writes the next operand; the
+ * sampler's launch-shape autotuner picks whichever is faster for the shape. */
+HMC_API int hmc_tc_step_split(const hmc_chains* s, const void* a_hi,
+                              const void* a_lo, int64_t lda, const void* q_hi,
+                              const void* q_lo, void* qn_hi, void* qn_lo,
+                              int64_t ldq, const float* center,
+                              const float* bias, int prior,
+                              const float* prior_mean, const float* prior_w,
+                              double kick, double drift, int* status,
+                              void* stream);
 /* Residual misfit 0.5 sum_r (G m - data)_r^2 inv_var_r per chain
  * (LinearMatrix.py:193-202) with FP64 per-chain sums; partial holds
  * hmc_tc_partials_size(n, C) doubles.                                       */

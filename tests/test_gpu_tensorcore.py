@@ -146,3 +146,33 @@ def test_persistent_fp32_sampler_tracks_fp64_oracle(golden):
     rel = np.abs(got - ref).max() / np.abs(ref).max()
     print(f"persistent FP32 chains vs FP64 oracle: max relative deviation {rel:.2e}")
     assert rel < 1e-5
+
+
+@pytest.mark.parametrize("prior", ["normal", "laplace"])
+def test_two_pass_step_equals_fused_step_bitwise(prior):
+    """hmc_tc_step_split (contraction, then a streaming update) and the fused
+    hmc_tc_step give bitwise-equal chains, bounds reflection included: the
+    autotuner may pick either."""
+    rng = np.random.default_rng(11)
+    n, d, C = 300, 192, 160
+    G = rng.normal(size=(n, d)) / np.sqrt(d)
+    dat = G @ rng.normal(size=(d, 1)) + 0.05 * rng.normal(size=(n, 1))
+    lik = H.Distributions.LinearMatrix(G, dat, 0.05**2)
+    pri = (H.Distributions.Normal(np.zeros((d, 1)), np.ones((d, 1)), lower_bounds=np.full((d, 1), -1.5),
+                                  upper_bounds=np.full((d, 1), 1.5)) if prior == "normal"
+           else H.Distributions.Laplace(np.zeros((d, 1)), np.ones((d, 1))))
+    post = H.Distributions.BayesRule([pri, lik])
+    q0 = np.clip(rng.normal(size=(d, C)) * 0.3, -1.4, 1.4)
+    runs = []
+    for entry in ("hmc_tc_step", "hmc_tc_step_split"):
+        smp = H.Samplers.HMC(seed=5)
+        smp.prepare(None, post, stepsize=0.05, amount_of_steps=8, initial_model=q0, proposals=6, chains=C,
+                    dtype="float32", keep_samples=True, persistent=False, graph=False)
+        assert smp._fused is not None
+        smp._fused.entry = entry
+        smp.run(6)
+        smp.finish()
+        smp._fused.ops.check_status()
+        runs.append((smp.samples_numpy(), np.atleast_1d(smp.accepted_proposals)))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
