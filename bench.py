@@ -140,10 +140,17 @@ class DenseWorkload:
 
     def roofline_spec(self, smp):
         fused = smp._fused is not None
-        return {"kernel": ("chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
-                           if fused else "dense gradient GEMM"),
-                # DRAM read + write of one step launch, ncu capture (54.4 + 2.9 MB)
-                "traffic": 57.3e6 if fused else None,
+        two_pass = fused and smp._fused.entry == "hmc_tc_step_split"
+        if two_pass:
+            kernel = ("leapfrog step in two passes (picked by the autotuner): chain_gemm_kernel<EPI_GRAD> tcgen05 "
+                      "BF16 hi/lo GtG@Q - Gtd0, then step_update_kernel (prior + kick + drift + operand split)")
+        elif fused:
+            kernel = "chain_gemm_kernel<EPI_STEP>: tcgen05 BF16 hi/lo GtG@Q + prior + kick + drift"
+        else:
+            kernel = "dense gradient GEMM"
+        return {"kernel": kernel,
+                # DRAM read + write of one fused step launch, ncu capture (54.4 + 2.9 MB)
+                "traffic": 57.3e6 if fused and not two_pass else None,
                 "bound": "tensor", "unit": "TFLOP/s", "work": self.gemm_flops(),
                 "work_name": "algorithmic_flop_per_launch",
                 "extra": {"executed_flop_per_launch": 3 * self.gemm_flops() if fused else self.gemm_flops()}}

@@ -522,7 +522,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 // shared-memory tile (rows d..ldq-1 written as zeros).  Every SM streams
 // the state with 8 warps per block instead of the contraction's 8
 // epilogue warps per 128-chain tile.
-__global__ void step_update_kernel(int64_t d, EpiParams ep, const float* __restrict__ g) {
+constexpr int UPDATE_ROWS = 8;  // threadIdx.y extent of step_update_kernel
+__global__ void __launch_bounds__(32 * UPDATE_ROWS) step_update_kernel(int64_t d, EpiParams ep,
+                                                                        const float* __restrict__ g) {
   __shared__ float tile[32][33];
   const int64_t C = ep.C;
   const int64_t i0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
@@ -534,13 +536,27 @@ __global__ void step_update_kernel(int64_t d, EpiParams ep, const float* __restr
     eps_d = ep.drift * e;
   }
   bool oob = false;
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+  // every load of the thread's rows first (independent, in flight together)
+  constexpr int RPT = 32 / UPDATE_ROWS;  // rows per thread
+  float qa[RPT], pa[RPT], ga[RPT];
+#pragma unroll
+  for (int u = 0; u < RPT; ++u) {
+    const int64_t r = i0 + threadIdx.y + u * UPDATE_ROWS;
+    const bool in = r < d && c < C;
+    const int64_t k = r * C + c;
+    qa[u] = in ? ep.q[k] : 0.f;
+    pa[u] = in ? ep.p[k] : 0.f;
+    ga[u] = in ? g[k] : 0.f;
+  }
+#pragma unroll
+  for (int u = 0; u < RPT; ++u) {
+    const int y = threadIdx.y + u * UPDATE_ROWS;
     const int64_t r = i0 + y;
     float qs = 0.f;
     if (r < d && c < C) {
       const int64_t k = r * C + c;
-      float qv = ep.q[k], pv = ep.p[k];
-      float gv = g[k];
+      float qv = qa[u], pv = pa[u];
+      float gv = ga[u];
       if (ep.prior == PRIOR_NORMAL) {
         gv += ep.prior_w[r] * (qv - ep.prior_mean[r]);
       } else if (ep.prior == PRIOR_LAPLACE) {
@@ -570,7 +586,9 @@ __global__ void step_update_kernel(int64_t d, EpiParams ep, const float* __restr
   }
   if (oob) atomicOr(&ep.flags[c], HMC_FLAG_OUT_OF_BOUNDS);
   __syncthreads();
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+#pragma unroll
+  for (int u = 0; u < RPT; ++u) {
+    const int y = threadIdx.y + u * UPDATE_ROWS;
     const int64_t cc = c0 + y, i = i0 + threadIdx.x;
     if (cc < C && i < ep.ldq) {
       const float v = tile[threadIdx.x][y];
@@ -819,7 +837,7 @@ HMC_API int hmc_tc_step_split(const hmc_chains* s, const void* a_hi, const void*
   ep.qn_lo = (__nv_bfloat16*)qn_lo;
   ep.ldq = ldq;
   const dim3 grid((unsigned)((s->chains + 31) / 32), (unsigned)((ldq + 31) / 32));
-  step_update_kernel<<<grid, dim3(32, 8), 0, st>>>(s->dims, ep, (const float*)s->g);
+  step_update_kernel<<<grid, dim3(32, UPDATE_ROWS), 0, st>>>(s->dims, ep, (const float*)s->g);
   return check_launch("step_update_kernel");
 }
 
