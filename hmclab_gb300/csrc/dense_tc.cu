@@ -518,11 +518,59 @@ __global__ void __launch_bounds__(THREADS, 1)
 // g = GtG q - bias: the prior's gradient, kick, drift and bound reflection
 // (the same expressions, in the same order, as the EPI_STEP epilogue, so
 // the results are bitwise equal), then the next operand q - center split
-// into BF16 hi/lo and transposed to chain-major [C][ldq] through a 32 x 32
-// shared-memory tile (rows d..ldq-1 written as zeros).  Every SM streams
-// the state with 8 warps per block instead of the contraction's 8
-// epilogue warps per 128-chain tile.
-constexpr int UPDATE_ROWS = 8;  // threadIdx.y extent of step_update_kernel
+// into BF16 hi/lo and transposed to chain-major [C][ldq] through a
+// shared-memory tile (rows d..ldq-1 written as zeros).  A thread first loads
+// everything its rows need (the state and the per-row prior, mass, bound
+// and centre values, bounds absent = -/+inf, which no position crosses)
+// into registers, so no load waits behind a store that might alias it.
+constexpr int UPDATE_ROWS = 8;  // threadIdx.y extent of the update kernels
+constexpr int UPDATE_RPT = 32 / UPDATE_ROWS;  // rows per thread
+
+struct RowParams {
+  float pw, pm, mi, lo, hi, ce;
+};
+__device__ __forceinline__ RowParams row_params(const EpiParams& ep, int64_t r, int64_t d) {
+  RowParams rp{0.f, 0.f, 1.f, -INFINITY, INFINITY, 0.f};
+  if (r < d) {
+    if (ep.prior != PRIOR_NONE) {
+      rp.pw = ep.prior_w[r];
+      rp.pm = ep.prior_mean[r];
+    }
+    if (ep.minv) rp.mi = ep.minv[r];
+    if (ep.lo) rp.lo = ep.lo[r];
+    if (ep.hi) rp.hi = ep.hi[r];
+    if (ep.center) rp.ce = ep.center[r];
+  }
+  return rp;
+}
+
+// One element: returns the next operand's value q - center; updates p, q.
+__device__ __forceinline__ float update_one(const EpiParams& ep, const RowParams& rp, float gv, float& qv, float& pv,
+                                            float eps_k, float eps_d, bool& oob) {
+  if (ep.prior == PRIOR_NORMAL) {
+    gv += rp.pw * (qv - rp.pm);
+  } else if (ep.prior == PRIOR_LAPLACE) {
+    const float dq = qv - rp.pm;
+    gv += (dq > 0.f ? 1.f : (dq < 0.f ? -1.f : 0.f)) * rp.pw;
+  }
+  pv = pv - eps_k * gv;
+  if (eps_d != 0.f) {
+    const float mp = ep.minv ? rp.mi * pv : pv;
+    float qn = qv + eps_d * mp;
+    if (qn < rp.lo) {
+      qn += 2.f * (rp.lo - qn);
+      pv = -pv;
+    }
+    if (qn > rp.hi) {
+      qn += 2.f * (rp.hi - qn);
+      pv = -pv;
+    }
+    if (qn < rp.lo || qn > rp.hi) oob = true;
+    qv = qn;
+  }
+  return ep.center != nullptr ? qv - rp.ce : qv;
+}
+
 __global__ void __launch_bounds__(32 * UPDATE_ROWS) step_update_kernel(int64_t d, EpiParams ep,
                                                                         const float* __restrict__ g) {
   __shared__ float tile[32][33];
@@ -535,63 +583,116 @@ __global__ void __launch_bounds__(32 * UPDATE_ROWS) step_update_kernel(int64_t d
     eps_k = ep.kick * e;
     eps_d = ep.drift * e;
   }
-  bool oob = false;
-  // every load of the thread's rows first (independent, in flight together)
-  constexpr int RPT = 32 / UPDATE_ROWS;  // rows per thread
-  float qa[RPT], pa[RPT], ga[RPT];
+  float qa[UPDATE_RPT], pa[UPDATE_RPT], ga[UPDATE_RPT];
+  RowParams rp[UPDATE_RPT];
 #pragma unroll
-  for (int u = 0; u < RPT; ++u) {
+  for (int u = 0; u < UPDATE_RPT; ++u) {
     const int64_t r = i0 + threadIdx.y + u * UPDATE_ROWS;
     const bool in = r < d && c < C;
     const int64_t k = r * C + c;
     qa[u] = in ? ep.q[k] : 0.f;
     pa[u] = in ? ep.p[k] : 0.f;
     ga[u] = in ? g[k] : 0.f;
+    rp[u] = row_params(ep, r, d);
   }
+  bool oob = false;
 #pragma unroll
-  for (int u = 0; u < RPT; ++u) {
+  for (int u = 0; u < UPDATE_RPT; ++u) {
     const int y = threadIdx.y + u * UPDATE_ROWS;
     const int64_t r = i0 + y;
     float qs = 0.f;
     if (r < d && c < C) {
+      qs = update_one(ep, rp[u], ga[u], qa[u], pa[u], eps_k, eps_d, oob);
       const int64_t k = r * C + c;
-      float qv = qa[u], pv = pa[u];
-      float gv = ga[u];
-      if (ep.prior == PRIOR_NORMAL) {
-        gv += ep.prior_w[r] * (qv - ep.prior_mean[r]);
-      } else if (ep.prior == PRIOR_LAPLACE) {
-        const float dq = qv - ep.prior_mean[r];
-        gv += (dq > 0.f ? 1.f : (dq < 0.f ? -1.f : 0.f)) * ep.prior_w[r];
-      }
-      pv = pv - eps_k * gv;
-      if (eps_d != 0.f) {
-        const float mp = ep.minv ? ep.minv[r] * pv : pv;
-        float qn = qv + eps_d * mp;
-        if (ep.lo && qn < ep.lo[r]) {
-          qn += 2.f * (ep.lo[r] - qn);
-          pv = -pv;
-        }
-        if (ep.hi && qn > ep.hi[r]) {
-          qn += 2.f * (ep.hi[r] - qn);
-          pv = -pv;
-        }
-        if ((ep.lo && qn < ep.lo[r]) || (ep.hi && qn > ep.hi[r])) oob = true;
-        qv = qn;
-      }
-      ep.p[k] = pv;
-      if (eps_d != 0.f) ep.q[k] = qv;
-      qs = ep.center != nullptr ? qv - ep.center[r] : qv;
+      ep.p[k] = pa[u];
+      if (eps_d != 0.f) ep.q[k] = qa[u];
     }
     tile[y][threadIdx.x] = qs;
   }
   if (oob) atomicOr(&ep.flags[c], HMC_FLAG_OUT_OF_BOUNDS);
   __syncthreads();
 #pragma unroll
-  for (int u = 0; u < RPT; ++u) {
+  for (int u = 0; u < UPDATE_RPT; ++u) {
     const int y = threadIdx.y + u * UPDATE_ROWS;
     const int64_t cc = c0 + y, i = i0 + threadIdx.x;
     if (cc < C && i < ep.ldq) {
       const float v = tile[threadIdx.x][y];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      ep.qn_hi[cc * ep.ldq + i] = h;
+      ep.qn_lo[cc * ep.ldq + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+  }
+}
+
+// The same update with 16-byte accesses when C is a multiple of 4: a block
+// owns 32 rows x 128 chains, a thread four consecutive chains of four rows
+// (float4 loads and stores of q, p and g), and the next operand is written
+// from a 32 x 129 shared-memory tile, a warp per chain and a lane per row.
+__global__ void __launch_bounds__(32 * UPDATE_ROWS) step_update4_kernel(int64_t d, EpiParams ep,
+                                                                         const float* __restrict__ g) {
+  __shared__ float tile[32][129];
+  const int64_t C = ep.C;
+  const int64_t i0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 128;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t c = c0 + 4 * tx;  // first of this thread's four chains
+  const bool live = c < C;        // C % 4 == 0: all four or none
+  float eps_k[4] = {0.f, 0.f, 0.f, 0.f}, eps_d[4] = {0.f, 0.f, 0.f, 0.f};
+  if (live) {
+    const float4 e = *(const float4*)(ep.eps_local + c);
+    const float ev[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      eps_k[j] = ep.kick * ev[j];
+      eps_d[j] = ep.drift * ev[j];
+    }
+  }
+  float4 qa[UPDATE_RPT], pa[UPDATE_RPT], ga[UPDATE_RPT];
+  RowParams rp[UPDATE_RPT];
+#pragma unroll
+  for (int u = 0; u < UPDATE_RPT; ++u) {
+    const int64_t r = i0 + ty + u * UPDATE_ROWS;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool in = live && r < d;
+    const int64_t k = r * C + c;
+    qa[u] = in ? *(const float4*)(ep.q + k) : z;
+    pa[u] = in ? *(const float4*)(ep.p + k) : z;
+    ga[u] = in ? *(const float4*)(g + k) : z;
+    rp[u] = row_params(ep, r, d);
+  }
+  bool oob[4] = {false, false, false, false};
+#pragma unroll
+  for (int u = 0; u < UPDATE_RPT; ++u) {
+    const int y = ty + u * UPDATE_ROWS;
+    const int64_t r = i0 + y;
+    float qv[4] = {qa[u].x, qa[u].y, qa[u].z, qa[u].w};
+    float pv[4] = {pa[u].x, pa[u].y, pa[u].z, pa[u].w};
+    const float gin[4] = {ga[u].x, ga[u].y, ga[u].z, ga[u].w};
+    float qs[4] = {0.f, 0.f, 0.f, 0.f};
+    if (live && r < d) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) qs[j] = update_one(ep, rp[u], gin[j], qv[j], pv[j], eps_k[j], eps_d[j], oob[j]);
+      const int64_t k = r * C + c;
+      *(float4*)(ep.p + k) = make_float4(pv[0], pv[1], pv[2], pv[3]);
+      // a chain with zero drift keeps its position (the scalar kernels skip its store)
+      if (eps_d[0] != 0.f && eps_d[1] != 0.f && eps_d[2] != 0.f && eps_d[3] != 0.f) {
+        *(float4*)(ep.q + k) = make_float4(qv[0], qv[1], qv[2], qv[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (eps_d[j] != 0.f) ep.q[k + j] = qv[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tile[y][4 * tx + j] = qs[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (oob[j]) atomicOr(&ep.flags[c + j], HMC_FLAG_OUT_OF_BOUNDS);
+  __syncthreads();
+  for (int cl = ty; cl < 128; cl += UPDATE_ROWS) {
+    const int64_t cc = c0 + cl, i = i0 + tx;
+    if (cc < C && i < ep.ldq) {
+      const float v = tile[tx][cl];
       const __nv_bfloat16 h = __float2bfloat16_rn(v);
       ep.qn_hi[cc * ep.ldq + i] = h;
       ep.qn_lo[cc * ep.ldq + i] = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -836,6 +937,14 @@ HMC_API int hmc_tc_step_split(const hmc_chains* s, const void* a_hi, const void*
   ep.qn_hi = (__nv_bfloat16*)qn_hi;
   ep.qn_lo = (__nv_bfloat16*)qn_lo;
   ep.ldq = ldq;
+  // 16-byte accesses need every row of the [d][C] state 16-byte aligned
+  const bool vec4 = s->chains % 4 == 0 && ((uintptr_t)s->p | (uintptr_t)s->q | (uintptr_t)s->g |
+                                           (uintptr_t)s->eps_local) % 16 == 0;
+  if (vec4) {
+    const dim3 grid((unsigned)((s->chains + 127) / 128), (unsigned)((ldq + 31) / 32));
+    step_update4_kernel<<<grid, dim3(32, UPDATE_ROWS), 0, st>>>(s->dims, ep, (const float*)s->g);
+    return check_launch("step_update4_kernel");
+  }
   const dim3 grid((unsigned)((s->chains + 31) / 32), (unsigned)((ldq + 31) / 32));
   step_update_kernel<<<grid, dim3(32, UPDATE_ROWS), 0, st>>>(s->dims, ep, (const float*)s->g);
   return check_launch("step_update_kernel");

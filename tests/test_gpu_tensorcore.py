@@ -148,13 +148,14 @@ def test_persistent_fp32_sampler_tracks_fp64_oracle(golden):
     assert rel < 1e-5
 
 
-@pytest.mark.parametrize("prior", ["normal", "laplace"])
-def test_two_pass_step_equals_fused_step_bitwise(prior):
-    """hmc_tc_step_split (contraction, then a streaming update) and the fused
+@pytest.mark.parametrize("prior,C", [("normal", 160), ("laplace", 160), ("normal", 162)])
+def test_two_pass_step_equals_fused_step_bitwise(prior, C):
+    """hmc_tc_step_split (contraction, then a streaming update: 16-byte
+    accesses when C is a multiple of 4, scalar otherwise) and the fused
     hmc_tc_step give bitwise-equal chains, bounds reflection included: the
     autotuner may pick either."""
     rng = np.random.default_rng(11)
-    n, d, C = 300, 192, 160
+    n, d = 300, 192
     G = rng.normal(size=(n, d)) / np.sqrt(d)
     dat = G @ rng.normal(size=(d, 1)) + 0.05 * rng.normal(size=(n, 1))
     lik = H.Distributions.LinearMatrix(G, dat, 0.05**2)
