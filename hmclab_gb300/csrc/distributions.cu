@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(CSR_THREADS, 2)
 // order with fused multiply-adds (four rows of X in flight), optionally on
 // the centred operand X - center[col].
 #ifndef HMC_CSR_GATHER_DEPTH
-#define HMC_CSR_GATHER_DEPTH 16
+#define HMC_CSR_GATHER_DEPTH 32
 #endif
 constexpr int GATHER_DEPTH = HMC_CSR_GATHER_DEPTH;
 
