@@ -101,3 +101,33 @@ def test_fwi_headline_validity_gates():
     assert any("moments disagree" in r for r in bench.fwi_validity(ess, mc_b))
     assert bench.fwi_validity(ess, None) == ["no reference moments to check the run against"]
     assert not mc["within_2pct_of_reference_std"]
+
+
+def test_variogram_decorrelation_reads_subdiffusive_chains_low():
+    """variogram_min = 1 - autocorrelation at the lag, from the mean squared
+    displacement over twice the reference variance: an AR(1) chain with
+    rho = 0.9 gives 1 - 0.9^lag; a chain whose successive moves undo each
+    other (x_t = a_t - a_(t-1) added to a slow AR(1)) moves a lot per step
+    but little over many steps."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(0)
+    N, d, C, rho = 4000, 3, 64, 0.9
+    x = np.zeros((N, d, C))
+    x[0] = rng.normal(size=(d, C))
+    for t in range(1, N):
+        x[t] = rho * x[t - 1] + np.sqrt(1 - rho**2) * rng.normal(size=(d, C))
+    q = torch.from_numpy(x)
+    for lag in (1, 5, 20):
+        assert abs(bench.variogram_min(q, np.ones(d), lag) - (1 - rho**lag)) < 0.03
+    slow = np.zeros((N, d, C))
+    rs = 0.999
+    for t in range(1, N):
+        slow[t] = rs * slow[t - 1] + np.sqrt(1 - rs**2) * rng.normal(size=(d, C))
+    a = 0.1 * rng.normal(size=(N, d, C))
+    jitter = a - np.roll(a, 1, axis=0)
+    z = torch.from_numpy(slow + jitter)
+    one, many = bench.variogram_min(z, np.ones(d), 1), bench.variogram_min(z, np.ones(d), 30)
+    # 30 independent moves of the single-step size would reach 30 x `one`
+    assert many < 0.5 * 30 * one
