@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // everything its rows need (the state and the per-row prior, mass, bound
 // and centre values, bounds absent = -/+inf, which no position crosses)
 // into registers, so no load waits behind a store that might alias it.
-constexpr int UPDATE_ROWS = 8;  // threadIdx.y extent of the update kernels
+constexpr int UPDATE_ROWS = 16;  // threadIdx.y extent of the update kernels (swept: 4, 8, 16, 32)
 constexpr int UPDATE_RPT = 32 / UPDATE_ROWS;  // rows per thread
 
 struct RowParams {
