@@ -400,6 +400,10 @@ FWI_MAX_Z = 4.5
 # (69.0 + 1.2 MB) on a cold cache; in the time loop the fields stay in L2 and
 # DRAM moves less
 FWI_STEP_DRAM_BYTES = 131.0e6
+# DRAM bytes of one time step of an exact gradient at C = 64 (ncu, cold cache):
+# forward with the velocity store 131 MB + adjoint velocity pass 195.6 MB +
+# adjoint stress pass 70.7 MB
+FWI_GRADIENT_STEP_DRAM_BYTES = 397.3e6
 
 
 class FwiWorkload:
@@ -464,6 +468,13 @@ class FwiWorkload:
     # muxz and writes sxx, szz, sxz: 20 FP32 words per cell and chain
     def stencil_bytes_per_step(self):
         return 80.0 * self.cells * self.chains
+
+    # algorithmic HBM bytes of one time step of an exact gradient: the forward
+    # step with the velocity store (80 + 8 B) plus the adjoint velocity pass
+    # (112 B: adjoint fields, temporaries, stored velocities of two steps,
+    # read-modify-write of five gradient accumulators) and stress pass (56 B)
+    def gradient_bytes_per_step(self):
+        return 256.0 * self.cells * self.chains
 
     def config(self):
         return {"workload": self.name, "grid": [self.cfg.nx, self.cfg.nz], "sponge_cells": self.cfg.pad,
@@ -860,6 +871,26 @@ def run_fwi_reference_arm(args, wl):
     print(json.dumps(line))
 
 
+def gradient_step_timing(lik, smp, n_iter=2):
+    """Seconds of one time step of an exact gradient (forward with store,
+    adjoint velocity and stress passes) over all chains: a 4-shot gradient
+    timed with CUDA events on the sampler stream, divided by shots x nt."""
+    import torch
+
+    st = smp.stream
+    h = st.cuda_stream
+    g = torch.empty_like(smp.q_cur)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        lik._device_gradient(smp.q_cur, g, False, "float32", h)
+        ev0.record(st)
+        for _ in range(n_iter):
+            lik._device_gradient(smp.q_cur, g, False, "float32", h)
+        ev1.record(st)
+    st.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / n_iter / (lik.config.n_shots * lik.config.nt)
+
+
 def forward_step_timing(lik, smp, n_iter=2):
     """Seconds of one forward time step (velocity + stress kernel) over all
     chains: the exact misfit (4 shots x nt steps of the two stencil kernels,
@@ -1070,6 +1101,7 @@ def run_fwi_arm(args, wl):
     host_q, host_x = smp_s.samples_host()
     t_e2e = time.perf_counter() - t_e2e0
     t_step = forward_step_timing(lik, smp_s)
+    t_gstep = gradient_step_timing(lik, smp_s) if sampler == "plain" else None
     qall = smp_s.samples_device[0]  # [(W+K)*B][d][C]
     qs = qall[W * B:]
     N = qs.shape[0]
@@ -1129,6 +1161,35 @@ def run_fwi_arm(args, wl):
     hbm, bf16, bf16s, src = peaks()
     achieved = wl.stencil_bytes_per_step() / t_step / 1e9
     l2 = l2_copy_rate()
+    forward_roof = {
+        "kernel": "fwi forward time step: velocity_tma_kernel + stress_tma_kernel (the exact misfit)",
+        "bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
+        "peak_source": "measured in this run: read + write rate of a copy over a 2 x 40 MB L2-resident buffer",
+        "hbm_peak": hbm, "hbm_peak_source": src, "frac_of_hbm": achieved / hbm,
+        "traffic": FWI_STEP_DRAM_BYTES, "traffic_source": "ncu capture of one velocity + one stress launch at "
+                                                          "C = 64, default (cold) cache control",
+        "step_s": t_step, "algorithmic_bytes_per_step": wl.stencil_bytes_per_step(),
+        "note": "one shot's fields and parameters (86 MB at 64 chains) stay in the 129 MB L2 over the time loop, so "
+                "the binding roof is the L2 rate, not HBM; DRAM traffic per step (`traffic`, cold cache) is 0.76 "
+                "of the algorithmic bytes"}
+    if t_gstep is not None:
+        # plain HMC spends its time in exact gradients: forward with store and
+        # the adjoint passes, whose fields, temporaries and accumulators
+        # (20 fields, 172 MB at 64 chains) exceed the L2
+        g_ach = wl.gradient_bytes_per_step() / t_gstep / 1e9
+        roof = {"kernel": "fwi exact-gradient time step: velocity_tma_kernel + stress_tma_kernel (with store), then "
+                          "adj_velocity_tma_kernel<1, true> + adj_stress_tma_kernel<4>",
+                "bound": "hbm", "achieved": g_ach, "peak": hbm, "unit": "GB/s", "frac": g_ach / hbm,
+                "peak_source": src, "traffic": FWI_GRADIENT_STEP_DRAM_BYTES,
+                "traffic_source": "ncu captures of the forward, adjoint velocity and adjoint stress launches at "
+                                  "C = 64, default (cold) cache control",
+                "step_s": t_gstep, "algorithmic_bytes_per_step": wl.gradient_bytes_per_step(),
+                "l2_peak": l2, "frac_of_l2": g_ach / l2,
+                "note": "part of the working set stays in L2, so the algorithmic rate can exceed the HBM copy rate; "
+                        "DRAM traffic per step (cold cache) is 0.72 of the algorithmic bytes",
+                "forward_stencil": forward_roof}
+    else:
+        roof = forward_roof
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -1177,17 +1238,7 @@ def run_fwi_arm(args, wl):
                                           "host start states, W + K blocks, samples back to the host); ESS over "
                                           "all its draws"},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "fwi forward time step: velocity_tma_kernel + stress_tma_kernel (the exact misfit)",
-                     "bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
-                     "peak_source": "measured in this run: read + write rate of a copy over a 2 x 40 MB "
-                                    "L2-resident buffer",
-                     "hbm_peak": hbm, "hbm_peak_source": src, "frac_of_hbm": achieved / hbm,
-                     "traffic": FWI_STEP_DRAM_BYTES, "traffic_source": "ncu capture of one velocity + one stress "
-                     "launch at C = 64, default (cold) cache control", "step_s": t_step,
-                     "algorithmic_bytes_per_step": wl.stencil_bytes_per_step(),
-                     "note": "one shot's fields and parameters (86 MB at 64 chains) stay in the 129 MB L2 over the "
-                             "time loop, so the binding roof is the L2 rate, not HBM; DRAM traffic per step "
-                             "(`traffic`, cold cache) is 0.76 of the algorithmic bytes"},
+        "roofline": roof,
         "clocks": clk,
     }
     if args.surrogate == "gradient":
