@@ -292,3 +292,24 @@ def test_create_default_gradient_step_and_uniform_sampling(cuda):
     assert q.shape == (lik.dimensions, 10)
     assert np.all(q >= lower - 1e-3) and np.all(q <= upper + 1e-3)
     assert np.all(np.isfinite(smp.samples_numpy()[0, -1, :]))
+
+
+def test_reader_opens_the_reference_configuration_file():
+    """The reference's own psvWave configuration
+    (tests/configurations/default_testing_configuration.ini of the reference)
+    parses, and its cell parametrisation has the 4800 free parameters the
+    reference's FWI tests ask create_default for (test_elasticFWI.py:20)."""
+    from oracle import ref_shim
+
+    path = os.path.join(ref_shim.REFERENCE_ROOT, "tests", "configurations", "default_testing_configuration.ini")
+    if not os.path.exists(path):
+        pytest.skip("the reference checkout is not on this machine")
+    cfg = FW.ElasticConfig.from_ini(path)
+    assert (cfg.nx, cfg.nz, cfg.pad, cfg.nt) == (40, 60, 25, 3000)
+    assert cfg.n_shots == 1 and len(cfg.shots[0]) == 4 and cfg.n_rec == 9
+    assert cfg.kernel_region == (0, 40, 10, 50)
+    zeros = np.zeros((cfg.n_shots, cfg.nt, cfg.n_rec))
+    d = H.Distributions.ElasticFullWaveform2D(path, ux_obs=zeros, uz_obs=zeros)
+    assert d.dimensions == 4800
+    with pytest.raises(InvalidCaseError):
+        H.Distributions.ElasticFullWaveform2D.create_default(4801, path)
