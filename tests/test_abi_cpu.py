@@ -113,3 +113,47 @@ def test_new_entry_points_reject_bad_arguments_on_the_host(lib):
     # FWI entry points with no descriptor
     assert lib.hmc_fwi_forward_shot(None, 0, 0, 0, 0, None) == E
     assert lib.hmc_fwi_adjoint_shot(None, 0, None) == E
+
+
+def _fake_fwi():
+    """An hmc_fwi whose buffers are non-null placeholders: only the host-side
+    validation below may look at it (every case fails before a launch)."""
+    s = _lib.HmcFwi()
+    s.nx, s.nz, s.nt, s.nrec, s.chains = 40, 30, 10, 3, 32
+    s.h, s.dt, s.w = 5.0, 5e-4, 1.0
+    dummy = 0x1000
+    for name in ("taper", "stf_host", "rec_map", "rho", "vp", "vs", "bx", "bz", "l2m", "lam", "muxz", "vx", "vz",
+                 "sxx", "szz", "sxz", "rec"):
+        setattr(s, name, dummy)
+    return s
+
+
+def test_fwi_source_validation_happens_on_the_host(lib):
+    s = _fake_fwi()
+    stf = (ctypes.c_float * 10)()
+
+    def sources(n, x=10, z=10, mxz=0.0, wavelet=True):
+        arr = (_lib.HmcFwiSource * n)()
+        for k in range(n):
+            arr[k].x, arr[k].z = x, z
+            arr[k].mxx, arr[k].mzz, arr[k].mxz = 1.0, 1.0, mxz
+            arr[k].stf_host = ctypes.cast(stf, ctypes.c_void_p).value if wavelet else None
+        return arr
+
+    for arr, why in ((sources(9, mxz=0.5), "stress terms"), (sources(1, x=0), "interior"),
+                     (sources(1, z=30), "interior"), (sources(1, wavelet=False), "wavelet")):
+        rc = lib.hmc_fwi_forward_shot_sources(ctypes.byref(s), 0, arr, len(arr), 0, None)
+        assert rc == _lib.HMC_ERR_INVALID_ARG
+        assert why in _lib.last_error()
+    rc = lib.hmc_fwi_forward_shot_sources(ctypes.byref(s), 0, None, 0, 0, None)
+    assert rc == _lib.HMC_ERR_INVALID_ARG
+    # storing for the adjoint needs the store buffer
+    rc = lib.hmc_fwi_forward_shot_sources(ctypes.byref(s), 0, sources(2), 2, 1, None)
+    assert rc == _lib.HMC_ERR_INVALID_ARG and "store" in _lib.last_error()
+
+
+def test_cell_parametrisation_and_fill_reject_bad_sizes(lib):
+    assert lib.hmc_fwi_cell_model(0, 4, None, None, None, None, None) == _lib.HMC_ERR_INVALID_ARG
+    assert lib.hmc_fwi_cell_gradient(5, 0, None, None, None, None, 0, None) == _lib.HMC_ERR_INVALID_ARG
+    assert lib.hmc_fill_zero(None, -1, None) == _lib.HMC_ERR_INVALID_ARG
+    assert lib.hmc_fill_zero(None, 0, None) == _lib.HMC_OK
