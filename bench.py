@@ -487,7 +487,7 @@ class FwiWorkload:
                               "gradient drives the leapfrog; BF16 weights, FP32 accumulate"),
                 "precision": "FP32 state and stencils, FP64 dH", "l2": "flushed between timed steps (256 MiB write)",
                 "snapshot_interval": self.snapshot_interval,
-                "start": "end states of the exact burn-in"}
+                "start": "posterior draws: final states of the reference plain-HMC run"}
 
 
 WORKLOADS = {"cfg1": Cfg1Workload, "dense": DenseWorkload, "tomo": TomoWorkload, "srcloc": SrclocWorkload,
