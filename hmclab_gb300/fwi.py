@@ -62,9 +62,10 @@ class ElasticConfig:
     i0 <= i < i1, j0 <= j < j1 (psvWave's nx/nz_inner_boundary) and
     `cell_block` = (npx, npz) groups its cells for the cell parametrisation;
     `medium` = (vp, vs, rho) makes the background homogeneous (default: the
-    layered model); `snapshot_interval` is recorded from a psvWave file (the gradient here is
-    the exact discrete adjoint whatever its value); `vmax` is the fastest
-    P velocity the time step must be stable for."""
+    layered model); `snapshot_interval` k > 1 makes the gradient correlate
+    the forward and adjoint fields at every k-th time step only, weighted by
+    k (psvWave's; 1, the default, is the exact discrete adjoint); `vmax` is
+    the fastest P velocity the time step must be stable for."""
 
     def __init__(self, nx=200, nz=100, pad=20, h=5.0, dt=5e-4, nt=1500, f0=25.0, sponge=0.015, amplitude=1e9,
                  src_x=(125.0, 375.0, 625.0, 875.0), src_z=10.0, rec_x=None, rec_z=10.0, shots=None, t0=None,
