@@ -17,10 +17,14 @@
 //   velocity:  vx += dt bx (Dx+ sxx + Dz- sxz),  vz += dt bz (Dx- sxz + Dz+ szz),
 //              then taper, record receivers, store (vx, vz) for the adjoint;
 //   stress:    sxx += dt ((l+2m) Dx- vx + l Dz- vz), szz += dt (l Dx- vx + (l+2m) Dz- vz),
-//              sxz += dt muxz (Dz+ vx + Dx+ vz), source into sxx and szz, taper.
+//              sxz += dt muxz (Dz+ vx + Dx+ vz), the sources' stress terms
+//              (an explosion into sxx and szz, a moment tensor also into the
+//              four sxz nodes around its cell), taper.
 // The adjoint runs the transpose of these maps backwards in time
 // ((Dx+)^T = -Dx-, (Dx-)^T = -Dx+, same in z), accumulating gradients with
-// respect to bx, bz, l+2m, l, muxz, which are then mapped to rho, vp, vs.
+// respect to bx, bz, l+2m, l, muxz, which are then mapped to rho, vp, vs;
+// with a snapshot interval k > 1 it accumulates at every k-th step only
+// (weight k) and otherwise just propagates the adjoint fields.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
